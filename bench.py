@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark: the wake run (4096 x 2304 FHP-III lattice, plate, inflow, walls,
+20,000 steps, 32 x 32 coarse-graining every 100 steps) in Gsite-updates/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One bench step is one whole wake run: 20,000 lattice steps plus 200 samples.
+`value` is device time (CUDA events on the lattice's stream) with the initial
+state already resident in HBM; `e2e` is the same run through the public API
+from page-locked host buffers: load the cells, run, read the field and the
+block sums back, every step.  Between timed steps a 256 MiB buffer is written
+to flush L2 (129 MB).  `--impl reference` times the reference's CPU update
+(the byte-per-cell Lattice::step, restated in C in oracle/) on the host's
+cores for a bounded sample of the same run.
+
+Under torchrun with N > 1 every rank runs its own replica of the run on its
+own GPU (the path has no exchange step); timings are maxed over ranks and the
+value counts the site-updates of all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "lattice-gas_gb300"))
+
+METRIC = "Gsite-updates/s (wake run, plain per-lattice step)"
+UNIT = "Gsite-updates/s"
+ALGO_BYTES_PER_SITE = 1.75   # 7 bits read + 7 bits written per site-update
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# Per-launch DRAM traffic of the step kernel on the wake run, from the ncu
+# capture summarised in profiles/step_wake_run.md (read + write bytes).
+STEP_TRAFFIC_BYTES = None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu),
+                                      "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        smax = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for name, v in zip(names, s[4:8]):
+                if v.strip().lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(world, x: float) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(world, x: float) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class L2Flusher:
+    """Writes a buffer larger than L2 on the device between timed steps."""
+
+    def __init__(self, device: int, nbytes: int = 256 << 20):
+        import torch
+        self.torch = torch
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device="cuda:%d" % device)
+
+    def __call__(self):
+        self.buf.fill_(1)
+        self.torch.cuda.synchronize()
+
+
+def cpu_reference_rate(wl, seconds: float, threads: int, chunk: int = 20):
+    """Site-updates/s of the reference's CPU update (oracle restatement of
+    Lattice::step, banded over `threads`) on the same lattice, sampling every
+    `wl.sample_every` steps, for about `seconds` of work."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle as O
+    lat = O.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, threads, wl.seed)
+    lat.set_cells(wl.cells)
+    field = O.Field(wl.w, wl.h, wl.block, wl.block)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        lat.advance(chunk)
+        steps += chunk
+        if steps % wl.sample_every == 0:
+            field.sample(lat.cells, wl.w, wl.h, wl.alpha)
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return wl.sites * steps / dt, steps, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from lattice_gas import workloads as W
+    wl = W.wake_run(steps=args.lattice_steps)
+    threads = os.cpu_count() or 1
+    # each bench step: a bounded sample of the run (~2 s of the host's cores)
+    for _ in range(args.warmup):
+        cpu_reference_rate(wl, 0.5, threads)
+    rates = []
+    total_steps = 0
+    total_t = 0.0
+    for _ in range(args.steps):
+        r, n, dt = cpu_reference_rate(wl, 2.0, threads)
+        rates.append(r)
+        total_steps += n
+        total_t += dt
+    value = wl.sites * total_steps / total_t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total_t / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "wake_run 4096x2304 FHP-III, plate + inflow + walls, 32x32 "
+                               "blocks every 100 steps", "w": wl.w, "h": wl.h,
+                   "lattice_steps_per_bench_step": "bounded sample (~2 s of CPU work)",
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
+                         "kind": "port",
+                         "sample": "%d lattice steps of the wake run in %d samples of ~2 s, "
+                                   "byte-per-cell Lattice::step restated in C (oracle/), "
+                                   "%d threads" % (total_steps, args.steps, threads)},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, world, rank, local):
+    import numpy as np
+    import lattice_gas as LG
+    from lattice_gas import workloads as W
+
+    LG.select_device(local)
+    peak, peak_kind = peaks()
+    wl = W.wake_run(steps=args.lattice_steps)
+    g = LG.GpuLattice(wl.w, wl.h, wl.rest, wl.seed)
+    g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, wl.rest)
+    g.attach_field(wl.block, wl.block)
+    g.load(wl.cells)
+    flush = L2Flusher(local)
+
+    def one_run():
+        g.timing_mark(0)
+        g.advance_sampling(wl.steps, wl.sample_every, wl.alpha)
+        g.timing_mark(1)
+        return g.timing_elapsed(0, 1)
+
+    for _ in range(args.warmup):
+        one_run()
+        flush()
+
+    # ---- device-resident timed region --------------------------------
+    clocks = ClockSampler(local)
+    launches0 = g.launches
+    dist_barrier(world)
+    clocks.start()
+    ms = []
+    for _ in range(args.steps):
+        flush()
+        ms.append(one_run())
+    dist_barrier(world)
+    clk = clocks.stop()
+    launches = g.launches - launches0
+    total_ms = dist_max(world, sum(ms))
+    sites_all = dist_sum(world, float(wl.sites * wl.steps * args.steps))
+    value = sites_all / (total_ms / 1e3) / 1e9
+
+    # ---- the step kernel alone: average launch duration ----------------
+    nk = 2000
+    flush()
+    g.timing_mark(2)
+    g.advance(nk)
+    g.timing_mark(3)
+    step_ms = g.timing_elapsed(2, 3) / nk
+    achieved = wl.sites * ALGO_BYTES_PER_SITE / (step_ms / 1e3) / 1e9
+
+    # ---- end to end through the public API from pinned host memory -----
+    nb = (wl.w // wl.block) * (wl.h // wl.block)
+    hcells = LG.PinnedBuffer(wl.sites)
+    hcells.array[:] = wl.cells
+    hout = [LG.PinnedBuffer(nb * 4, np.float32) for _ in range(4)]
+    hsum = [LG.PinnedBuffer(nb * 4, np.int32) for _ in range(4)]
+    f = LG.Field(wl.w, wl.h, wl.block, wl.block)
+    f.ux, f.uy, f.rho, f.solid = (b.array for b in hout)
+    e2e_ms = []
+    dist_barrier(world)
+    for _ in range(args.steps):
+        flush()
+        g.timing_mark(4)
+        g.restart(hcells.array, wl.seed)
+        g.advance_sampling(wl.steps, wl.sample_every, wl.alpha)
+        g.read_field(f)
+        LG._check(LG.lib().lgx_read_block_sums(g.handle, *[LG._p(b.array, LG.C.c_int32)
+                                                           for b in hsum], nb))
+        g.timing_mark(5)
+        e2e_ms.append(g.timing_elapsed(4, 5))
+    dist_barrier(world)
+    e2e_total = dist_max(world, sum(e2e_ms))
+    e2e_value = sites_all / (e2e_total / 1e3) / 1e9
+
+    # ---- reported CPU baseline (rank 0, N = 1 only) -------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, nsteps, dt = cpu_reference_rate(wl, args.cpu_seconds, threads)
+        cpu = {"value": round(rate / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d lattice steps of the wake run (%.1f s), byte-per-cell "
+                         "Lattice::step restated in C (oracle/), %d threads"
+                         % (nsteps, dt, threads)}
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 bitplanes (integer)",
+        "data": "synthetic (seeded wake-run lattice built with the reference's primitives)",
+        "config": {"workload": "wake_run: 4096x2304 FHP-III, plate at x=512 of 1/8 channel "
+                               "height, 8-column inflow u=0.2, density 0.3, walls at rows 0 and "
+                               "h-1; 20000 steps, 32x32 blocks every 100 steps",
+                   "w": wl.w, "h": wl.h, "lattice_steps_per_bench_step": wl.steps,
+                   "sample_every": wl.sample_every, "block": wl.block,
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "parallelism": "replicas x%d" % world},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": STEP_TRAFFIC_BYTES, "peak_kind": peak_kind,
+                     "kernel": "lgx_step_kernel", "step_kernel_us": round(step_ms * 1e3, 3),
+                     "algorithmic_bytes_per_launch": wl.sites * ALGO_BYTES_PER_SITE,
+                     "note": "integer-ALU bound; see int_pipe"},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": wl.sites,
+                "d2h_bytes_per_step": 8 * nb * 4},
+        "gpu_launches": launches // max(args.steps, 1) * args.steps,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "device": g.device_name(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--lattice-steps", type=int, default=20000)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_gb300(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,132 @@
+/*
+ * lgx.h -- C ABI of the GB300 FHP lattice-gas engine.
+ *
+ * Drop-in for the reference's bitplane lattice, `GpuLattice` in src/gpu.rs
+ * (daleobrien/lattice-gas), which the reference drives through `Sim`
+ * (src/sim.rs:35-174).  Every function returns an lgx_status (0 = success);
+ * on failure lgx_last_error() describes the error for the calling thread.  No
+ * C++ exception crosses this boundary.  A handle is used from one host thread
+ * at a time; each lattice owns one CUDA stream on the device that was current
+ * when it was created, and every call that the reference makes blocking
+ * (advance, load, store, read_field, total_particles) is blocking here too.
+ *
+ * Cell bytes follow src/hex.rs: bits 0-5 the six directions (0 = east, then
+ * counter-clockwise), bit 6 the rest particle, bit 7 the obstacle flag.
+ * Rows are w cells, row-major, h rows; h even, w > 4, h > 4.
+ */
+#ifndef LGX_H
+#define LGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  LGX_OK = 0,
+  LGX_ERR_ARG = 1,       /* size or argument mismatch (the reference asserts) */
+  LGX_ERR_CUDA = 2,      /* a CUDA call failed */
+  LGX_ERR_NO_DEVICE = 3, /* no CUDA device (the reference: "no Metal device") */
+  LGX_ERR_STATE = 4,     /* e.g. reading a field that was never attached */
+  LGX_ERR_ALLOC = 5,     /* device or host allocation failed */
+  LGX_ERR_BUSY = 6       /* server: over budget or queue full */
+} lgx_status;
+
+typedef struct lgx_lattice lgx_lattice;
+
+/* Last error message of the calling thread ("" if none). */
+const char *lgx_last_error(void);
+
+/* ---- the lattice (replaces GpuLattice, src/gpu.rs:453-755) -------------- */
+
+/* Make `ordinal` the device that later lgx_create calls on this thread use
+ * (the reference takes the system default Metal device, src/metal.rs:121). */
+int lgx_select_device(int ordinal);
+/* Page-locked host buffers, so load/store/read_field copies are true DMA. */
+int lgx_host_alloc(size_t bytes, void **out);
+int lgx_host_free(void *p);
+
+/* GpuLattice::new (src/gpu.rs:479-515): 7 bitplanes x 2 (ping-pong), solid
+ * plane, anysolid summary.  rest_particles selects the FHP-III rule. */
+int lgx_create(size_t w, size_t h, int rest_particles, uint64_t seed, lgx_lattice **out);
+/* Drop of GpuLattice: frees every device buffer and the stream. */
+int lgx_destroy(lgx_lattice *lat);
+/* GpuLattice::device_name (src/gpu.rs:517-519). */
+int lgx_device_name(lgx_lattice *lat, char *buf, size_t len);
+/* GpuLattice::set_inlet (src/gpu.rs:525-528): re-seed the leftmost `cols`
+ * columns from Equilibrium(density, (ux, uy), rest) every step. */
+int lgx_set_inlet(lgx_lattice *lat, size_t cols, float density, float ux, float uy,
+                  int rest_particles);
+/* GpuLattice::attach_field (src/gpu.rs:532-545): a (w/bx) x (h/by) block field
+ * on the device, zero-initialised. */
+int lgx_attach_field(lgx_lattice *lat, size_t bx, size_t by);
+/* GpuLattice::load (src/gpu.rs:572-610): n must be w*h. */
+int lgx_load(lgx_lattice *lat, const uint8_t *cells, size_t n);
+/* GpuLattice::restart (src/gpu.rs:616-620): load, then seed = seed, steps = 0. */
+int lgx_restart(lgx_lattice *lat, const uint8_t *cells, size_t n, uint64_t seed);
+/* GpuLattice::store (src/gpu.rs:630-652): n must be w*h. */
+int lgx_store(lgx_lattice *lat, uint8_t *cells, size_t n);
+/* GpuLattice::advance (src/gpu.rs:657-659). */
+int lgx_advance(lgx_lattice *lat, uint64_t n);
+/* GpuLattice::advance_sampling (src/gpu.rs:668-706): n steps, folding the
+ * lattice into the attached field every sample_every steps and after the last
+ * one; sample_every == 0 never samples. */
+int lgx_advance_sampling(lgx_lattice *lat, uint64_t n, uint64_t sample_every, float alpha);
+/* GpuLattice::sample_field (src/gpu.rs:710-721). */
+int lgx_sample_field(lgx_lattice *lat, float alpha);
+/* GpuLattice::read_field (src/gpu.rs:725-736): n_blocks must be bw*bh. */
+int lgx_read_field(lgx_lattice *lat, float *ux, float *uy, float *rho, float *sol,
+                   size_t n_blocks);
+/* New: the exact integer block sums (FLUID view, src/moments.rs:37-74) of the
+ * most recent sample: mass, px2 (half units), py2 (units of sqrt(3)/2), and
+ * the count of obstacle cells.  n_blocks must be bw*bh. */
+int lgx_read_block_sums(lgx_lattice *lat, int32_t *mass, int32_t *px2, int32_t *py2,
+                        int32_t *nsolid, size_t n_blocks);
+/* GpuLattice::total_particles (src/gpu.rs:740-754), counted in 64 bits. */
+int lgx_total_particles(lgx_lattice *lat, uint64_t *out);
+/* GpuLattice::steps (pub field, src/gpu.rs:471). */
+int lgx_steps(lgx_lattice *lat, uint64_t *out);
+/* Kernels this lattice has launched since it was created (instrumentation). */
+int lgx_launch_count(lgx_lattice *lat, uint64_t *out);
+/* The lattice's CUDA stream (cudaStream_t), for callers that order their own
+ * work after the engine's. */
+int lgx_stream(lgx_lattice *lat, void **stream);
+/* Device-time instrumentation: record event `slot` (0..7) on the lattice's
+ * stream; elapsed milliseconds between two recorded slots (waits for b). */
+int lgx_timing_mark(lgx_lattice *lat, int slot);
+int lgx_timing_elapsed(lgx_lattice *lat, int a, int b, float *ms);
+
+/* The exhaustive check of the circuit the step kernel runs, evaluated on the
+ * device (the lgca_verify kernel, src/gpu.rs:399-417): out[i], i < n_states*48,
+ * is the output state for state i/48 and draw (i/24%2, i/6%4, i%6), with bit
+ * 16 set if lanes disagreed.  n must be 48 * (rest ? 128 : 64). */
+int lgx_verify_circuit(int rest_particles, uint32_t *out, size_t n);
+
+/* ---- host-side lattice setup (src/lattice.rs, src/hex.rs) ---------------- */
+
+/* Equilibrium::new(..).thresholds() (src/lattice.rs:72-92): 24-bit thresholds,
+ * six directions then rest (0 without rest particles). */
+int lgx_equilibrium_thresholds(float density, float ux, float uy, int rest_particles,
+                               uint32_t out[7]);
+/* Lattice::init_equilibrium (src/lattice.rs:197-208) on caller-owned cells:
+ * one generator Rng::new(seed ^ 0xA5A51234) in cell order; obstacle cells
+ * become exactly SOLID_BIT. */
+int lgx_cells_init_equilibrium(uint8_t *cells, size_t n, float density, float ux, float uy,
+                               int rest_particles, uint64_t seed);
+/* Lattice::add_solid (src/lattice.rs:210-220) with a box predicate on
+ * hex::site_position (inclusive bounds, or strict when strict != 0). */
+int lgx_cells_add_box(uint8_t *cells, size_t w, size_t h, float x0, float x1, float y0, float y1,
+                      int strict);
+/* Lattice::add_solid with the disc (x-cx)^2 + (y-cy)^2 <= r^2 (src/main.rs:590). */
+int lgx_cells_add_circle(uint8_t *cells, size_t w, size_t h, float cx, float cy, float r);
+/* Shear-wave start of transport::viscosity (src/transport.rs:188-200): row y
+ * drawn from Equilibrium(density, ux_row[y], 0) with one Rng::new(rng_seed). */
+int lgx_cells_shear_wave(uint8_t *cells, size_t w, size_t h, float density, const float *ux_row,
+                         int rest_particles, uint64_t rng_seed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LGX_H */

@@ -1,0 +1,207 @@
+// lgx_field.cu -- coarse-graining, particle count, byte<->plane transposes and
+// the exhaustive circuit check.
+//
+// Coarse-graining (lgca_sample, src/gpu.rs:324-377): one warp per block of the
+// field.  Lanes take rows of the block; each row contributes the masked
+// popcounts of the one to several words the block's columns straddle.  The
+// sums are exact 32-bit integers (mass, px2 = sum CX2 * count, py2, nsolid),
+// reduced across the warp, and only then turned into f32 velocity and blended
+// into the running average with round-to-nearest intrinsics, so no fused
+// multiply-add can change the last bit (Moments::velocity, src/moments.rs:91).
+#include "lgx_device.cuh"
+#include "lgx_internal.hpp"
+
+namespace lgx {
+
+namespace {
+
+constexpr float kSqrt3_2 = 0.8660254f;  // src/hex.rs:25
+
+__global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t blk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (blk >= p.bw * p.bh) return;  // whole warp leaves together
+  const uint32_t jb = blk / p.bw, ib = blk - jb * p.bw;
+  const uint32_t x0 = ib * p.bx, x1 = x0 + p.bx;
+  const uint32_t w0 = x0 >> 5, w1 = (x1 - 1u) >> 5;
+  const size_t S = p.dm.total;
+  int mass = 0, px = 0, py = 0, nsolid = 0;
+  for (uint32_t r = lane; r < p.by; r += 32u) {
+    const size_t base = (size_t)(jb * p.by + r) * p.dm.wpr;
+    for (uint32_t wi = w0; wi <= w1; ++wi) {
+      const uint32_t lo = max(x0, wi << 5) - (wi << 5);
+      const uint32_t hi = min(x1, (wi + 1u) << 5) - (wi << 5);
+      const uint32_t m = (hi - lo >= 32u) ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << lo);
+      const uint32_t sm = __ldg(p.solid + base + wi) & m;
+      nsolid += __popc(sm);
+      const uint32_t fm = m & ~sm;
+      const int c0 = __popc(__ldg(p.a + 0 * S + base + wi) & fm);
+      const int c1 = __popc(__ldg(p.a + 1 * S + base + wi) & fm);
+      const int c2 = __popc(__ldg(p.a + 2 * S + base + wi) & fm);
+      const int c3 = __popc(__ldg(p.a + 3 * S + base + wi) & fm);
+      const int c4 = __popc(__ldg(p.a + 4 * S + base + wi) & fm);
+      const int c5 = __popc(__ldg(p.a + 5 * S + base + wi) & fm);
+      const int c6 = __popc(__ldg(p.a + 6 * S + base + wi) & fm);
+      mass += c0 + c1 + c2 + c3 + c4 + c5 + c6;
+      // CX2 = {2, 1, -1, -2, -1, 1}, CY2 = {0, 1, 1, 0, -1, -1}
+      px += 2 * (c0 - c3) + c1 - c2 - c4 + c5;
+      py += c1 + c2 - c4 - c5;
+    }
+  }
+  const unsigned FULL = 0xffffffffu;
+  mass = __reduce_add_sync(FULL, mass);
+  px = __reduce_add_sync(FULL, px);
+  py = __reduce_add_sync(FULL, py);
+  nsolid = __reduce_add_sync(FULL, nsolid);
+  if (lane != 0) return;
+  const uint32_t nb = p.bw * p.bh;
+  if (p.sums) {
+    p.sums[blk] = mass;
+    p.sums[nb + blk] = px;
+    p.sums[2 * nb + blk] = py;
+    p.sums[3 * nb + blk] = nsolid;
+  }
+  const float n = __uint2float_rn(p.bx * p.by);
+  const float m = __int2float_rn(mass);
+  float vx = 0.0f, vy = 0.0f;
+  if (mass > 0) {
+    vx = __fdiv_rn(__fmul_rn(__int2float_rn(px), 0.5f), m);
+    vy = __fdiv_rn(__fmul_rn(__int2float_rn(py), kSqrt3_2), m);
+  }
+  const float a = p.alpha;
+  const float u0 = p.ux[blk], v0 = p.uy[blk], r0 = p.rho[blk];
+  p.ux[blk] = __fadd_rn(u0, __fmul_rn(a, __fsub_rn(vx, u0)));
+  p.uy[blk] = __fadd_rn(v0, __fmul_rn(a, __fsub_rn(vy, v0)));
+  p.rho[blk] = __fadd_rn(r0, __fmul_rn(a, __fsub_rn(__fdiv_rn(m, n), r0)));
+  p.sol[blk] = __fdiv_rn(__int2float_rn(nsolid), n);
+}
+
+// Particles on the lattice, obstacle sites included, tail-masked
+// (lgca_count, src/gpu.rs:381-395), into a 64-bit counter.
+__global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restrict__ a, Dims dm,
+                                                        unsigned long long* out) {
+  unsigned long long acc = 0;
+  const size_t S = dm.total;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < dm.total;
+       g += gridDim.x * blockDim.x) {
+    const uint32_t j = g % dm.wpr;
+    const uint32_t m = (j == dm.lastword) ? dm.tail : 0xffffffffu;
+    uint32_t c = 0;
+#pragma unroll
+    for (int d = 0; d < 7; ++d) c += __popc(__ldg(a + d * S + g) & m);
+    acc += c;
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31u) == 0 && acc) atomicAdd(out, acc);
+}
+
+// Bytes -> planes: one warp per lattice word; lane k reads column 32 j + k and
+// eight ballots give the seven planes and the solid word (src/gpu.rs:572-610).
+__global__ void __launch_bounds__(256) lgx_pack_kernel(const uint8_t* __restrict__ cells, Dims dm,
+                                                       uint32_t* planes, uint32_t* solid,
+                                                       uint32_t* anysolid) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (g >= dm.total) return;
+  const uint32_t y = g / dm.wpr, j = g - y * dm.wpr;
+  const uint32_t x = j * 32u + lane;
+  const uint32_t c = (x < dm.w) ? cells[(size_t)y * dm.w + x] : 0u;
+  uint32_t mine = 0;
+#pragma unroll
+  for (int d = 0; d < 8; ++d) {
+    const uint32_t v = __ballot_sync(0xffffffffu, (c >> d) & 1u);
+    if (lane == (uint32_t)d) mine = v;
+  }
+  if (lane < 7u) planes[(size_t)lane * dm.total + g] = mine;
+  if (lane == 7u) {
+    solid[g] = mine;
+    if (mine) atomicOr(anysolid + (g >> 5), 1u << (g & 31u));
+  }
+}
+
+// Planes -> bytes (src/gpu.rs:630-652): bit k of the eight words of lattice
+// word j is the byte of column 32 j + k.
+__global__ void __launch_bounds__(256) lgx_unpack_kernel(const uint32_t* __restrict__ planes,
+                                                         const uint32_t* __restrict__ solid,
+                                                         Dims dm, uint8_t* cells) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (g >= dm.total) return;
+  const uint32_t y = g / dm.wpr, j = g - y * dm.wpr;
+  const uint32_t x = j * 32u + lane;
+  uint32_t word = (lane < 7u) ? __ldg(planes + (size_t)lane * dm.total + g)
+                              : (lane == 7u ? __ldg(solid + g) : 0u);
+  uint32_t c = 0;
+#pragma unroll
+  for (int d = 0; d < 8; ++d) c |= ((__shfl_sync(0xffffffffu, word, d) >> lane) & 1u) << d;
+  if (x < dm.w) cells[(size_t)y * dm.w + x] = (uint8_t)c;
+}
+
+// The exhaustive check of the circuit the step runs (lgca_verify,
+// src/gpu.rs:399-417): thread i evaluates collide on all-lanes-equal inputs
+// for state i / 48 and draw (i / 24 % 2, i / 6 % 4, i % 6).
+template <bool REST>
+__global__ void lgx_verify_kernel(uint32_t* out, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t five = i % 6u, three = (i / 6u) % 4u, two = (i / 24u) % 2u, state = i / 48u;
+  uint32_t nn[7];
+  for (int d = 0; d < 7; ++d) nn[d] = ((state >> d) & 1u) ? 0xffffffffu : 0u;
+  Draws s;
+  s.s2 = two ? 0xffffffffu : 0u;
+  for (int k = 0; k < 3; ++k) s.s3[k] = (three == (uint32_t)k) ? 0xffffffffu : 0u;
+  for (int k = 0; k < 5; ++k) s.s5[k] = (five == (uint32_t)k) ? 0xffffffffu : 0u;
+  uint32_t o[7];
+  collide<REST>(nn, s, o);
+  uint32_t r = 0u, bad = 0u;
+  for (int d = 0; d < 7; ++d) {
+    if (o[d] == 0xffffffffu)
+      r |= 1u << d;
+    else if (o[d] != 0u)
+      bad = 1u;
+  }
+  out[i] = r | (bad << 16);
+}
+
+}  // namespace
+
+cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st) {
+  const uint32_t nb = s.bw * s.bh;
+  if (nb == 0) return cudaSuccess;
+  lgx_sample_kernel<<<(nb + 7) / 8, 256, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
+                         cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  uint32_t blocks = (dm.total + 255) / 256;
+  if (blocks > 1216) blocks = 1216;  // 152 SMs x 8 resident blocks, grid-stride beyond
+  lgx_count_kernel<<<blocks, 256, 0, st>>>(a, dm, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const uint8_t* cells, const Dims& dm, uint32_t* planes, uint32_t* solid,
+                        uint32_t* anysolid, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(anysolid, 0, ((dm.total + 31) / 32) * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  lgx_pack_kernel<<<(dm.total + 7) / 8, 256, 0, st>>>(cells, dm, planes, solid, anysolid);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const uint32_t* planes, const uint32_t* solid, const Dims& dm,
+                          uint8_t* cells, cudaStream_t st) {
+  lgx_unpack_kernel<<<(dm.total + 7) / 8, 256, 0, st>>>(planes, solid, dm, cells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_verify(uint32_t* out, uint32_t n, bool rest, cudaStream_t st) {
+  if (rest)
+    lgx_verify_kernel<true><<<(n + 127) / 128, 128, 0, st>>>(out, n);
+  else
+    lgx_verify_kernel<false><<<(n + 127) / 128, 128, 0, st>>>(out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace lgx

@@ -1,0 +1,82 @@
+// lgx_internal.hpp -- declarations shared by the library's translation units.
+// Not part of the public C ABI (that is include/lgx.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace lgx {
+
+// Geometry of one lattice in the bitplane layout.
+struct Dims {
+  uint32_t w, h;
+  uint32_t wpr;       // words per row, ceil(w / 32)
+  uint32_t total;     // wpr * h, words per plane
+  uint32_t lastword;  // (w - 1) / 32
+  uint32_t lastbit;   // (w - 1) % 32
+  uint32_t tail;      // valid-bit mask of the last word of a row
+  uint32_t iw;        // words of a row the inlet touches, ceil(inlet_cols / 32)
+  uint32_t inlet_cols;
+};
+
+Dims make_dims(uint32_t w, uint32_t h, uint32_t inlet_cols);
+
+// One step of one lattice: a -> b.
+struct StepArgs {
+  const uint32_t* a;
+  uint32_t* b;
+  const uint32_t* solid;
+  const uint32_t* anysolid;
+  const uint32_t* inlet;  // Bernoulli words for this step, [h][iw][7]; null when iw == 0
+  Dims dm;
+  uint64_t seed;
+  uint64_t steps;  // steps taken before this one
+};
+
+// Inlet Bernoulli words for `nsteps` consecutive steps starting at `steps`,
+// written to out[s][y][jw][d].
+struct InletArgs {
+  uint32_t* out;
+  Dims dm;
+  uint64_t seed;
+  uint64_t steps;
+  uint32_t nsteps;
+  uint32_t thresh[7];
+};
+
+// Coarse-graining of one lattice into bw x bh blocks of bx x by cells.
+struct SampleArgs {
+  const uint32_t* a;
+  const uint32_t* solid;
+  Dims dm;
+  uint32_t bx, by, bw, bh;
+  float alpha;
+  float* ux;
+  float* uy;
+  float* rho;
+  float* sol;
+  int32_t* sums;  // [4][bw*bh]: mass, px2, py2, nsolid
+};
+
+cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st);
+cudaError_t launch_inlet(const InletArgs& s, cudaStream_t st);
+cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
+cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
+                         cudaStream_t st);
+// Byte cells (w*h, row-major) <-> planes + solid + anysolid.
+cudaError_t launch_pack(const uint8_t* cells, const Dims& dm, uint32_t* planes, uint32_t* solid,
+                        uint32_t* anysolid, cudaStream_t st);
+cudaError_t launch_unpack(const uint32_t* planes, const uint32_t* solid, const Dims& dm,
+                          uint8_t* cells, cudaStream_t st);
+// Exhaustive circuit check: out[i] for i < n_states * 48 (src/gpu.rs:399-417).
+cudaError_t launch_verify(uint32_t* out, uint32_t n, bool rest, cudaStream_t st);
+
+// Host-side equilibrium thresholds (src/lattice.rs:59-92), f32 without fusion.
+void equilibrium_thresholds(float density, float ux, float uy, bool rest, uint32_t out[7]);
+
+void set_error(const std::string& msg);
+
+}  // namespace lgx

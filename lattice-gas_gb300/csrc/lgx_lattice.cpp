@@ -1,0 +1,540 @@
+// lgx_lattice.cpp -- the lattice handle behind the C ABI (include/lgx.h).
+//
+// Mirrors GpuLattice (src/gpu.rs:453-755): it owns the ping-pong planes, the
+// solid plane and its one-bit-per-word summary, the coarse-grained field, and
+// a CUDA stream.  Steps are enqueued back to back on that stream and the call
+// waits once at the end, as the reference's advance_sampling commits its
+// command buffers and waits (src/gpu.rs:668-706).
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+
+#include "../../include/lgx.h"
+#include "lgx_internal.hpp"
+
+namespace lgx {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+Dims make_dims(uint32_t w, uint32_t h, uint32_t inlet_cols) {
+  Dims d;
+  d.w = w;
+  d.h = h;
+  d.wpr = (w + 31u) / 32u;
+  d.total = d.wpr * h;
+  d.lastword = (w - 1u) / 32u;
+  d.lastbit = (w - 1u) % 32u;
+  d.tail = (d.lastbit == 31u) ? 0xffffffffu : ((1u << (d.lastbit + 1u)) - 1u);
+  d.inlet_cols = std::min(inlet_cols, w);
+  d.iw = (d.inlet_cols + 31u) / 32u;
+  return d;
+}
+
+// Steps whose inlet draws are made in one launch.
+constexpr uint32_t kInletChunk = 64;
+
+}  // namespace lgx
+
+struct lgx_lattice {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  lgx::Dims dm{};
+  bool rest = true;
+  uint64_t seed = 0;
+  uint64_t steps = 0;
+  uint32_t thresh[7] = {0, 0, 0, 0, 0, 0, 0};
+  uint32_t* planes[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint32_t* solid = nullptr;
+  uint32_t* anysolid = nullptr;
+  uint8_t* cells = nullptr;  // staging for load/store, w*h bytes
+  unsigned long long* counter = nullptr;
+  // inlet draws for the current chunk of steps
+  uint32_t* inlet = nullptr;
+  uint32_t inlet_cap = 0;      // steps the buffer holds
+  uint64_t inlet_first = 0;    // step index of slot 0
+  uint32_t inlet_valid = 0;    // slots filled
+  // field
+  bool has_field = false;
+  uint32_t bx = 0, by = 0, bw = 0, bh = 0;
+  float* field = nullptr;      // ux | uy | rho | sol, bw*bh each
+  int32_t* sums = nullptr;     // mass | px2 | py2 | nsolid
+  cudaEvent_t ev[8] = {};
+  uint64_t launches = 0;     // kernels this handle has launched
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+  lgx::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return LGX_ERR_CUDA;
+}
+
+#define LGX_CUDA(call)                                        \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);       \
+  } while (0)
+
+int check_lat(lgx_lattice* lat) {
+  if (!lat) {
+    lgx::set_error("null lattice handle");
+    return LGX_ERR_ARG;
+  }
+  cudaError_t e = cudaSetDevice(lat->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  return LGX_OK;
+}
+
+void free_lattice(lgx_lattice* lat) {
+  cudaSetDevice(lat->device);
+  if (lat->stream) cudaStreamSynchronize(lat->stream);
+  cudaFree(lat->planes[0]);
+  cudaFree(lat->planes[1]);
+  cudaFree(lat->solid);
+  cudaFree(lat->anysolid);
+  cudaFree(lat->cells);
+  cudaFree(lat->counter);
+  cudaFree(lat->inlet);
+  cudaFree(lat->field);
+  cudaFree(lat->sums);
+  for (auto& e : lat->ev)
+    if (e) cudaEventDestroy(e);
+  if (lat->stream) cudaStreamDestroy(lat->stream);
+  delete lat;
+}
+
+// Draw the inlet words for the next `want` steps if the chunk in hand does
+// not cover step `lat->steps`.
+int ensure_inlet(lgx_lattice* lat, uint64_t want) {
+  if (lat->dm.iw == 0) return LGX_OK;
+  if (lat->steps >= lat->inlet_first && lat->steps < lat->inlet_first + lat->inlet_valid)
+    return LGX_OK;
+  const uint32_t n = (uint32_t)std::min<uint64_t>(want, lgx::kInletChunk);
+  if (n > lat->inlet_cap) {
+    // the buffer may still be read by enqueued steps
+    LGX_CUDA(cudaStreamSynchronize(lat->stream));
+    cudaFree(lat->inlet);
+    lat->inlet = nullptr;
+    const size_t bytes = (size_t)lgx::kInletChunk * lat->dm.h * lat->dm.iw * 7 * sizeof(uint32_t);
+    LGX_CUDA(cudaMalloc(&lat->inlet, bytes));
+    lat->inlet_cap = lgx::kInletChunk;
+  }
+  lgx::InletArgs ia;
+  ia.out = lat->inlet;
+  ia.dm = lat->dm;
+  ia.seed = lat->seed;
+  ia.steps = lat->steps;
+  ia.nsteps = n;
+  memcpy(ia.thresh, lat->thresh, sizeof(ia.thresh));
+  LGX_CUDA(lgx::launch_inlet(ia, lat->stream));
+  lat->launches += 1;
+  lat->inlet_first = lat->steps;
+  lat->inlet_valid = n;
+  return LGX_OK;
+}
+
+int launch_sample(lgx_lattice* lat, float alpha) {
+  if (!lat->has_field) return LGX_OK;
+  const size_t nb = (size_t)lat->bw * lat->bh;
+  lgx::SampleArgs sa;
+  sa.a = lat->planes[lat->cur];
+  sa.solid = lat->solid;
+  sa.dm = lat->dm;
+  sa.bx = lat->bx;
+  sa.by = lat->by;
+  sa.bw = lat->bw;
+  sa.bh = lat->bh;
+  sa.alpha = alpha;
+  sa.ux = lat->field;
+  sa.uy = lat->field + nb;
+  sa.rho = lat->field + 2 * nb;
+  sa.sol = lat->field + 3 * nb;
+  sa.sums = lat->sums;
+  LGX_CUDA(lgx::launch_sample(sa, lat->stream));
+  lat->launches += 1;
+  return LGX_OK;
+}
+
+int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
+  uint64_t left = n, since = 0;
+  while (left > 0) {
+    int rc = ensure_inlet(lat, left);
+    if (rc) return rc;
+    lgx::StepArgs sa;
+    sa.a = lat->planes[lat->cur];
+    sa.b = lat->planes[lat->cur ^ 1];
+    sa.solid = lat->solid;
+    sa.anysolid = lat->anysolid;
+    sa.inlet = lat->dm.iw
+                   ? lat->inlet + (size_t)(lat->steps - lat->inlet_first) * lat->dm.h *
+                                      lat->dm.iw * 7
+                   : nullptr;
+    sa.dm = lat->dm;
+    sa.seed = lat->seed;
+    sa.steps = lat->steps;
+    LGX_CUDA(lgx::launch_step(sa, lat->rest, lat->stream));
+    lat->launches += 1;
+    lat->cur ^= 1;
+    lat->steps += 1;
+    left -= 1;
+    since += 1;
+    if (every > 0 && (since >= every || left == 0)) {
+      since = 0;
+      rc = launch_sample(lat, alpha);
+      if (rc) return rc;
+    }
+  }
+  return LGX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lgx_last_error(void) { return lgx::g_last_error.c_str(); }
+
+int lgx_create(size_t w, size_t h, int rest, uint64_t seed, lgx_lattice** out) {
+  if (!out) {
+    lgx::set_error("lgx_create: null output");
+    return LGX_ERR_ARG;
+  }
+  *out = nullptr;
+  if (h % 2 != 0) {
+    lgx::set_error("row count must be even for the lattice to wrap cleanly in y");
+    return LGX_ERR_ARG;
+  }
+  if (w <= 4 || h <= 4) {
+    lgx::set_error("lattice is too small");
+    return LGX_ERR_ARG;
+  }
+  const size_t wpr = (w + 31) / 32;
+  if (wpr * h * 7 >= (1ull << 32) || w >= (1ull << 31)) {
+    lgx::set_error("lattice is too large for 32-bit word indices");
+    return LGX_ERR_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    lgx::set_error("no CUDA device on this machine");
+    return LGX_ERR_NO_DEVICE;
+  }
+  lgx_lattice* lat = new (std::nothrow) lgx_lattice();
+  if (!lat) {
+    lgx::set_error("out of host memory");
+    return LGX_ERR_ALLOC;
+  }
+  cudaGetDevice(&lat->device);
+  lat->dm = lgx::make_dims((uint32_t)w, (uint32_t)h, 0);
+  lat->rest = rest != 0;
+  lat->seed = seed;
+  const size_t total = lat->dm.total;
+  cudaError_t e = cudaStreamCreateWithFlags(&lat->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&lat->planes[0], total * 7 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&lat->planes[1], total * 7 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&lat->solid, total * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&lat->anysolid, ((total + 31) / 32) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&lat->cells, w * h);
+  if (e == cudaSuccess) e = cudaMalloc(&lat->counter, sizeof(unsigned long long));
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&lat->ev[i]);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lat->planes[0], 0, total * 7 * 4, lat->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lat->planes[1], 0, total * 7 * 4, lat->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lat->solid, 0, total * 4, lat->stream);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(lat->anysolid, 0, ((total + 31) / 32) * 4, lat->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(lat->stream);
+  if (e != cudaSuccess) {
+    const int rc = (e == cudaErrorMemoryAllocation) ? LGX_ERR_ALLOC : LGX_ERR_CUDA;
+    lgx::set_error(std::string("lgx_create: ") + cudaGetErrorString(e));
+    free_lattice(lat);
+    return rc;
+  }
+  *out = lat;
+  return LGX_OK;
+}
+
+int lgx_destroy(lgx_lattice* lat) {
+  if (!lat) return LGX_OK;
+  free_lattice(lat);
+  return LGX_OK;
+}
+
+int lgx_device_name(lgx_lattice* lat, char* buf, size_t len) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  cudaDeviceProp prop;
+  LGX_CUDA(cudaGetDeviceProperties(&prop, lat->device));
+  if (buf && len) snprintf(buf, len, "%s", prop.name);
+  return LGX_OK;
+}
+
+int lgx_set_inlet(lgx_lattice* lat, size_t cols, float density, float ux, float uy, int rest) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  lat->dm = lgx::make_dims(lat->dm.w, lat->dm.h, (uint32_t)std::min<size_t>(cols, lat->dm.w));
+  lgx::equilibrium_thresholds(density, ux, uy, rest != 0, lat->thresh);
+  lat->inlet_valid = 0;  // draws depend on the thresholds
+  return LGX_OK;
+}
+
+int lgx_attach_field(lgx_lattice* lat, size_t bx, size_t by) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (bx == 0 || by == 0) {
+    lgx::set_error("block size must be positive");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  cudaFree(lat->field);
+  cudaFree(lat->sums);
+  lat->field = nullptr;
+  lat->sums = nullptr;
+  lat->has_field = false;
+  lat->bx = (uint32_t)bx;
+  lat->by = (uint32_t)by;
+  lat->bw = lat->dm.w / (uint32_t)bx;
+  lat->bh = lat->dm.h / (uint32_t)by;
+  const size_t nb = std::max<size_t>((size_t)lat->bw * lat->bh, 1);
+  LGX_CUDA(cudaMalloc(&lat->field, 4 * nb * sizeof(float)));
+  LGX_CUDA(cudaMalloc(&lat->sums, 4 * nb * sizeof(int32_t)));
+  LGX_CUDA(cudaMemsetAsync(lat->field, 0, 4 * nb * sizeof(float), lat->stream));
+  LGX_CUDA(cudaMemsetAsync(lat->sums, 0, 4 * nb * sizeof(int32_t), lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  lat->has_field = true;
+  return LGX_OK;
+}
+
+int lgx_load(lgx_lattice* lat, const uint8_t* cells, size_t n) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (n != (size_t)lat->dm.w * lat->dm.h || !cells) {
+    lgx::set_error("wrong number of cells");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaMemcpyAsync(lat->cells, cells, n, cudaMemcpyHostToDevice, lat->stream));
+  LGX_CUDA(lgx::launch_pack(lat->cells, lat->dm, lat->planes[lat->cur], lat->solid,
+                            lat->anysolid, lat->stream));
+  lat->launches += 1;
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_restart(lgx_lattice* lat, const uint8_t* cells, size_t n, uint64_t seed) {
+  int rc = lgx_load(lat, cells, n);
+  if (rc) return rc;
+  lat->seed = seed;
+  lat->steps = 0;
+  lat->inlet_valid = 0;
+  return LGX_OK;
+}
+
+int lgx_store(lgx_lattice* lat, uint8_t* cells, size_t n) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (n != (size_t)lat->dm.w * lat->dm.h || !cells) {
+    lgx::set_error("wrong number of cells");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(lgx::launch_unpack(lat->planes[lat->cur], lat->solid, lat->dm, lat->cells,
+                              lat->stream));
+  lat->launches += 1;
+  LGX_CUDA(cudaMemcpyAsync(cells, lat->cells, n, cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_advance(lgx_lattice* lat, uint64_t n) { return lgx_advance_sampling(lat, n, 0, 0.0f); }
+
+int lgx_advance_sampling(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  rc = enqueue_steps(lat, n, every, alpha);
+  if (rc) return rc;
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_sample_field(lgx_lattice* lat, float alpha) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  rc = launch_sample(lat, alpha);
+  if (rc) return rc;
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_read_field(lgx_lattice* lat, float* ux, float* uy, float* rho, float* sol,
+                   size_t n_blocks) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!lat->has_field) {
+    lgx::set_error("no field attached to this lattice");
+    return LGX_ERR_STATE;
+  }
+  const size_t nb = (size_t)lat->bw * lat->bh;
+  if (n_blocks != nb) {
+    lgx::set_error("the field on the device has a different block grid from the one being filled");
+    return LGX_ERR_ARG;
+  }
+  float* dst[4] = {ux, uy, rho, sol};
+  for (int i = 0; i < 4; ++i)
+    if (dst[i] && nb)
+      LGX_CUDA(cudaMemcpyAsync(dst[i], lat->field + i * nb, nb * sizeof(float),
+                               cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_read_block_sums(lgx_lattice* lat, int32_t* mass, int32_t* px2, int32_t* py2,
+                        int32_t* nsolid, size_t n_blocks) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!lat->has_field) {
+    lgx::set_error("no field attached to this lattice");
+    return LGX_ERR_STATE;
+  }
+  const size_t nb = (size_t)lat->bw * lat->bh;
+  if (n_blocks != nb) {
+    lgx::set_error("block grid mismatch");
+    return LGX_ERR_ARG;
+  }
+  int32_t* dst[4] = {mass, px2, py2, nsolid};
+  for (int i = 0; i < 4; ++i)
+    if (dst[i] && nb)
+      LGX_CUDA(cudaMemcpyAsync(dst[i], lat->sums + i * nb, nb * sizeof(int32_t),
+                               cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_total_particles(lgx_lattice* lat, uint64_t* out) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!out) {
+    lgx::set_error("null output");
+    return LGX_ERR_ARG;
+  }
+  unsigned long long v = 0;
+  LGX_CUDA(lgx::launch_count(lat->planes[lat->cur], lat->dm, lat->counter, lat->stream));
+  lat->launches += 1;
+  LGX_CUDA(cudaMemcpyAsync(&v, lat->counter, sizeof(v), cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  *out = v;
+  return LGX_OK;
+}
+
+int lgx_steps(lgx_lattice* lat, uint64_t* out) {
+  if (!lat || !out) {
+    lgx::set_error("null argument");
+    return LGX_ERR_ARG;
+  }
+  *out = lat->steps;
+  return LGX_OK;
+}
+
+int lgx_launch_count(lgx_lattice* lat, uint64_t* out) {
+  if (!lat || !out) {
+    lgx::set_error("null argument");
+    return LGX_ERR_ARG;
+  }
+  *out = lat->launches;
+  return LGX_OK;
+}
+
+int lgx_stream(lgx_lattice* lat, void** stream) {
+  if (!lat || !stream) {
+    lgx::set_error("null argument");
+    return LGX_ERR_ARG;
+  }
+  *stream = (void*)lat->stream;
+  return LGX_OK;
+}
+
+int lgx_timing_mark(lgx_lattice* lat, int slot) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (slot < 0 || slot >= 8) {
+    lgx::set_error("timing slot out of range");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaEventRecord(lat->ev[slot], lat->stream));
+  return LGX_OK;
+}
+
+int lgx_timing_elapsed(lgx_lattice* lat, int a, int b, float* ms) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (a < 0 || a >= 8 || b < 0 || b >= 8 || !ms) {
+    lgx::set_error("timing slot out of range");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaEventSynchronize(lat->ev[b]));
+  LGX_CUDA(cudaEventElapsedTime(ms, lat->ev[a], lat->ev[b]));
+  return LGX_OK;
+}
+
+int lgx_select_device(int ordinal) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    lgx::set_error("no CUDA device on this machine");
+    return LGX_ERR_NO_DEVICE;
+  }
+  if (ordinal < 0 || ordinal >= ndev) {
+    lgx::set_error("device ordinal out of range");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaSetDevice(ordinal));
+  return LGX_OK;
+}
+
+int lgx_host_alloc(size_t bytes, void** out) {
+  if (!out) {
+    lgx::set_error("null output");
+    return LGX_ERR_ARG;
+  }
+  *out = nullptr;
+  cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    lgx::set_error(std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? LGX_ERR_ALLOC : LGX_ERR_CUDA;
+  }
+  return LGX_OK;
+}
+
+int lgx_host_free(void* p) {
+  if (p) LGX_CUDA(cudaFreeHost(p));
+  return LGX_OK;
+}
+
+int lgx_verify_circuit(int rest, uint32_t* out, size_t n) {
+  const size_t want = (size_t)48 * (rest ? 128 : 64);
+  if (!out || n != want) {
+    lgx::set_error("lgx_verify_circuit: n must be 48 * n_states");
+    return LGX_ERR_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    lgx::set_error("no CUDA device on this machine");
+    return LGX_ERR_NO_DEVICE;
+  }
+  uint32_t* d = nullptr;
+  LGX_CUDA(cudaMalloc(&d, n * sizeof(uint32_t)));
+  cudaError_t e = lgx::launch_verify(d, (uint32_t)n, rest != 0, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "lgx_verify_circuit");
+  return LGX_OK;
+}
+
+}  // extern "C"

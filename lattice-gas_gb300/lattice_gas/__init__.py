@@ -1,0 +1,310 @@
+"""lattice_gas -- Python host mirror of the GB300 lattice-gas engine.
+
+A ctypes binding of the C ABI in include/lgx.h (liblgx.so, built by
+lattice-gas_gb300/build.py).  The names follow the reference crate
+(daleobrien/lattice-gas): ``GpuLattice`` is ``lattice_gas::gpu::GpuLattice``
+(src/gpu.rs:453-755) with the same methods, argument meaning and panics turned
+into ``LgxError``; ``Field`` is ``render::Field``'s data; ``Batch`` and
+``Server`` are the batched and served front ends.
+
+There is no CPU fallback: if liblgx.so is missing or no CUDA device is
+present, the first call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblgx.so")
+
+__all__ = ["GpuLattice", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
+           "add_box", "add_circle", "shear_wave", "verify_circuit", "SQRT3_2"]
+
+SQRT3_2 = np.float32(0.8660254)
+SOLID_BIT = 0x80
+REST_BIT = 0x40
+STATE_MASK = 0x7F
+
+_lock = threading.Lock()
+_lib = None
+
+u8p = C.POINTER(C.c_uint8)
+u32p = C.POINTER(C.c_uint32)
+i32p = C.POINTER(C.c_int32)
+f32p = C.POINTER(C.c_float)
+sz = C.c_size_t
+vp = C.c_void_p
+
+
+class LgxError(RuntimeError):
+    """A C-ABI call returned a non-zero lgx_status."""
+
+    def __init__(self, code, msg):
+        super().__init__("lgx error %d: %s" % (code, msg))
+        self.code = code
+
+
+def _sig(L, name, *args):
+    f = getattr(L, name)
+    f.restype = C.c_int
+    f.argtypes = list(args)
+
+
+def lib():
+    """Load liblgx.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("liblgx.so is not built; run lattice-gas_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        L.lgx_last_error.restype = C.c_char_p
+        L.lgx_last_error.argtypes = []
+        _sig(L, "lgx_create", sz, sz, C.c_int, C.c_uint64, C.POINTER(vp))
+        _sig(L, "lgx_destroy", vp)
+        _sig(L, "lgx_device_name", vp, C.c_char_p, sz)
+        _sig(L, "lgx_set_inlet", vp, sz, C.c_float, C.c_float, C.c_float, C.c_int)
+        _sig(L, "lgx_attach_field", vp, sz, sz)
+        _sig(L, "lgx_load", vp, u8p, sz)
+        _sig(L, "lgx_restart", vp, u8p, sz, C.c_uint64)
+        _sig(L, "lgx_store", vp, u8p, sz)
+        _sig(L, "lgx_advance", vp, C.c_uint64)
+        _sig(L, "lgx_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
+        _sig(L, "lgx_sample_field", vp, C.c_float)
+        _sig(L, "lgx_read_field", vp, f32p, f32p, f32p, f32p, sz)
+        _sig(L, "lgx_read_block_sums", vp, i32p, i32p, i32p, i32p, sz)
+        _sig(L, "lgx_total_particles", vp, C.POINTER(C.c_uint64))
+        _sig(L, "lgx_steps", vp, C.POINTER(C.c_uint64))
+        _sig(L, "lgx_stream", vp, C.POINTER(vp))
+        _sig(L, "lgx_launch_count", vp, C.POINTER(C.c_uint64))
+        _sig(L, "lgx_timing_mark", vp, C.c_int)
+        _sig(L, "lgx_timing_elapsed", vp, C.c_int, C.c_int, C.POINTER(C.c_float))
+        _sig(L, "lgx_verify_circuit", C.c_int, u32p, sz)
+        _sig(L, "lgx_select_device", C.c_int)
+        _sig(L, "lgx_host_alloc", sz, C.POINTER(vp))
+        _sig(L, "lgx_host_free", vp)
+        _sig(L, "lgx_equilibrium_thresholds", C.c_float, C.c_float, C.c_float, C.c_int, u32p)
+        _sig(L, "lgx_cells_init_equilibrium", u8p, sz, C.c_float, C.c_float, C.c_float, C.c_int,
+             C.c_uint64)
+        _sig(L, "lgx_cells_add_box", u8p, sz, sz, C.c_float, C.c_float, C.c_float, C.c_float,
+             C.c_int)
+        _sig(L, "lgx_cells_add_circle", u8p, sz, sz, C.c_float, C.c_float, C.c_float)
+        _sig(L, "lgx_cells_shear_wave", u8p, sz, sz, C.c_float, f32p, C.c_int, C.c_uint64)
+        _lib = L
+        return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise LgxError(rc, lib().lgx_last_error().decode(errors="replace"))
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _u64(x):
+    return int(x) & (2 ** 64 - 1)
+
+
+class Field:
+    """The coarse-grained field's arrays (render::Field, src/render.rs:22-48)."""
+
+    def __init__(self, w, h, bx, by):
+        self.bx, self.by = bx, by
+        self.bw, self.bh = w // bx, h // by
+        n = self.bw * self.bh
+        self.ux = np.zeros(n, np.float32)
+        self.uy = np.zeros(n, np.float32)
+        self.rho = np.zeros(n, np.float32)
+        self.solid = np.zeros(n, np.float32)
+
+
+class GpuLattice:
+    """The lattice on the GPU, as bitplanes (src/gpu.rs:453-755)."""
+
+    def __init__(self, w: int, h: int, rest_particles: bool, seed: int):
+        L = lib()
+        self.w, self.h = int(w), int(h)
+        self.rest = bool(rest_particles)
+        self._h = vp()
+        _check(L.lgx_create(self.w, self.h, int(self.rest), _u64(seed), C.byref(self._h)))
+        self._field = None
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().lgx_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_name(self) -> str:
+        buf = C.create_string_buffer(256)
+        _check(lib().lgx_device_name(self._h, buf, 256))
+        return buf.value.decode()
+
+    def set_inlet(self, cols, density, inflow, rest):
+        _check(lib().lgx_set_inlet(self._h, int(cols), float(density), float(inflow[0]),
+                                   float(inflow[1]), int(bool(rest))))
+
+    def attach_field(self, bx, by):
+        _check(lib().lgx_attach_field(self._h, int(bx), int(by)))
+        self._field = (int(bx), int(by), self.w // int(bx), self.h // int(by))
+
+    def load(self, cells):
+        c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+        _check(lib().lgx_load(self._h, _p(c, C.c_uint8), c.size))
+
+    def restart(self, cells, seed):
+        c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+        _check(lib().lgx_restart(self._h, _p(c, C.c_uint8), c.size, _u64(seed)))
+
+    def store(self, out=None) -> np.ndarray:
+        if out is None:
+            out = np.zeros(self.w * self.h, np.uint8)
+        _check(lib().lgx_store(self._h, _p(out, C.c_uint8), out.size))
+        return out
+
+    def advance(self, n):
+        _check(lib().lgx_advance(self._h, int(n)))
+
+    def advance_sampling(self, n, sample_every, alpha):
+        _check(lib().lgx_advance_sampling(self._h, int(n), int(sample_every), float(alpha)))
+
+    def sample_field(self, alpha):
+        _check(lib().lgx_sample_field(self._h, float(alpha)))
+
+    def read_field(self, f: Field | None = None) -> Field:
+        if self._field is None:
+            raise LgxError(4, "no field attached to this lattice")
+        bx, by, bw, bh = self._field
+        if f is None:
+            f = Field(self.w, self.h, bx, by)
+        if (f.bw, f.bh, f.bx, f.by) != (bw, bh, bx, by):
+            raise LgxError(1, "the field on the device has a different block grid from the "
+                              "one being filled")
+        _check(lib().lgx_read_field(self._h, _p(f.ux, C.c_float), _p(f.uy, C.c_float),
+                                    _p(f.rho, C.c_float), _p(f.solid, C.c_float), bw * bh))
+        return f
+
+    def read_block_sums(self):
+        if self._field is None:
+            raise LgxError(4, "no field attached to this lattice")
+        _, _, bw, bh = self._field
+        outs = [np.zeros(bw * bh, np.int32) for _ in range(4)]
+        _check(lib().lgx_read_block_sums(self._h, *[_p(o, C.c_int32) for o in outs], bw * bh))
+        return outs
+
+    def total_particles(self) -> int:
+        v = C.c_uint64()
+        _check(lib().lgx_total_particles(self._h, C.byref(v)))
+        return int(v.value)
+
+    @property
+    def steps(self) -> int:
+        v = C.c_uint64()
+        _check(lib().lgx_steps(self._h, C.byref(v)))
+        return int(v.value)
+
+    @property
+    def launches(self) -> int:
+        v = C.c_uint64()
+        _check(lib().lgx_launch_count(self._h, C.byref(v)))
+        return int(v.value)
+
+    @property
+    def stream(self) -> int:
+        v = vp()
+        _check(lib().lgx_stream(self._h, C.byref(v)))
+        return int(v.value or 0)
+
+    def timing_mark(self, slot):
+        _check(lib().lgx_timing_mark(self._h, int(slot)))
+
+    def timing_elapsed(self, a, b) -> float:
+        ms = C.c_float()
+        _check(lib().lgx_timing_elapsed(self._h, int(a), int(b), C.byref(ms)))
+        return float(ms.value)
+
+
+# ---- host-side setup (src/lattice.rs, src/hex.rs, src/transport.rs) --------
+
+def thresholds(density, ux, uy, rest):
+    out = np.zeros(7, np.uint32)
+    _check(lib().lgx_equilibrium_thresholds(float(density), float(ux), float(uy), int(bool(rest)),
+                                            _p(out, C.c_uint32)))
+    return out
+
+
+def init_equilibrium(cells, density, ux, uy, rest, seed):
+    """Lattice::init_equilibrium on a byte array (in place; returns it)."""
+    assert cells.dtype == np.uint8 and cells.flags["C_CONTIGUOUS"]
+    _check(lib().lgx_cells_init_equilibrium(_p(cells, C.c_uint8), cells.size, float(density),
+                                            float(ux), float(uy), int(bool(rest)), _u64(seed)))
+    return cells
+
+
+def add_box(cells, w, h, x0, x1, y0, y1, strict=False):
+    _check(lib().lgx_cells_add_box(_p(cells, C.c_uint8), w, h, float(x0), float(x1), float(y0),
+                                   float(y1), int(bool(strict))))
+    return cells
+
+
+def add_circle(cells, w, h, cx, cy, r):
+    _check(lib().lgx_cells_add_circle(_p(cells, C.c_uint8), w, h, float(cx), float(cy), float(r)))
+    return cells
+
+
+def shear_wave(w, h, density, ux_row, rest, rng_seed):
+    cells = np.zeros(w * h, np.uint8)
+    u = np.ascontiguousarray(ux_row, dtype=np.float32)
+    _check(lib().lgx_cells_shear_wave(_p(cells, C.c_uint8), w, h, float(density),
+                                      _p(u, C.c_float), int(bool(rest)), _u64(rng_seed)))
+    return cells
+
+
+def select_device(ordinal: int):
+    _check(lib().lgx_select_device(int(ordinal)))
+
+
+class PinnedBuffer:
+    """A page-locked host buffer viewed as a numpy array."""
+
+    def __init__(self, nbytes: int, dtype=np.uint8):
+        self._p = vp()
+        _check(lib().lgx_host_alloc(int(nbytes), C.byref(self._p)))
+        self.nbytes = int(nbytes)
+        buf = (C.c_uint8 * max(self.nbytes, 1)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=np.uint8)[:self.nbytes].view(dtype)
+
+    def free(self):
+        if self._p and self._p.value:
+            lib().lgx_host_free(self._p)
+            self._p = vp()
+            self.array = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def verify_circuit(rest) -> np.ndarray:
+    n = 48 * (128 if rest else 64)
+    out = np.zeros(n, np.uint32)
+    _check(lib().lgx_verify_circuit(int(bool(rest)), _p(out, C.c_uint32), n))
+    return out

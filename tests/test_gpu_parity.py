@@ -1,0 +1,347 @@
+"""The CUDA engine against the oracle, through the C ABI.
+
+Bit-exact: after N steps from the same cells and seed, the lattice state, the
+integer block sums, the f32 field and the particle count are identical to the
+oracle's restatement of the reference's bitplane path (src/gpu.rs).  The
+reference's own GPU tests (src/gpu.rs:773-1451) are restated against the
+engine as well.  Every test here needs a GPU.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DX_EVEN = (1, 0, -1, -1, -1, 0)
+DX_ODD = (1, 1, 0, -1, 0, 1)
+DY = (0, 1, 1, 0, -1, -1)
+THREADS = max(1, min(16, os.cpu_count() or 1))
+
+
+def pair(LG, O, w, h, rest, seed, cells, inlet=None, block=None):
+    g = LG.GpuLattice(w, h, rest, seed)
+    o = O.BitplaneLattice(w, h, rest, seed, THREADS)
+    if inlet:
+        g.set_inlet(*inlet)
+        o.set_inlet(*inlet)
+    if block:
+        g.attach_field(block, block)
+        o.attach_field(block, block)
+    g.load(cells)
+    o.load(cells)
+    return g, o
+
+
+def assert_same(g, o, with_field=True):
+    a, b = g.store(), o.store()
+    if not np.array_equal(a, b):
+        bad = np.nonzero(a != b)[0]
+        raise AssertionError("%d cells differ; first at %d (x=%d, y=%d): gpu %02x oracle %02x"
+                             % (bad.size, bad[0], bad[0] % g.w, bad[0] // g.w, a[bad[0]],
+                                b[bad[0]]))
+    assert g.total_particles() == o.total_particles()
+    assert g.steps == o.steps
+    if with_field and g._field is not None:
+        for x, y in zip(g.read_block_sums(), o.read_block_sums()):
+            assert np.array_equal(x, y)
+        f = g.read_field()
+        for x, y in zip((f.ux, f.uy, f.rho, f.solid), o.read_field()):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+# ---- the reference's GPU tests, restated ---------------------------------
+
+@pytest.mark.parametrize("rest", [True, False])
+def test_the_device_rule_matches_the_enumeration(LG, O, rest):
+    """src/gpu.rs:775-820, on the circuit the step kernel runs."""
+    got = LG.verify_circuit(rest)
+    L = O.lib()
+    for i, v in enumerate(got):
+        five, three, two, state = i % 6, (i // 6) % 4, (i // 24) % 2, i // 48
+        assert v >> 16 == 0, "lanes disagreed on state %d" % state
+        assert (v & 0xFF) == L.lgo_collide_lane(int(rest), state, two, three, five)
+
+
+@pytest.mark.parametrize("w", [64, 80, 20, 33, 100])
+def test_a_single_particle_travels_in_a_straight_line(LG, w):
+    """src/gpu.rs:826-863, plus one-word (w=20) and one-bit-tail (w=33) rows."""
+    h, steps = 48, 8
+    for d in range(6):
+        for start_row in (10, 11):
+            g = LG.GpuLattice(w, h, True, 1)
+            cells = np.zeros(w * h, np.uint8)
+            x0, y0 = min(24, w - 2), start_row
+            cells[y0 * w + x0] = 1 << d
+            g.load(cells)
+            g.advance(steps)
+            out = g.store()
+            live = np.nonzero(out & 0x7F)[0]
+            assert len(live) == 1 and out[live[0]] == 1 << d
+            x, y = x0, y0
+            for _ in range(steps):
+                x = (x + (DX_ODD[d] if y & 1 else DX_EVEN[d])) % w
+                y = (y + DY[d]) % h
+            assert live[0] == y * w + x, (w, d, start_row)
+
+
+def test_walls_reverse_particles(LG):
+    """src/gpu.rs:867-885."""
+    w, h = 64, 48
+    g = LG.GpuLattice(w, h, True, 1)
+    cells = np.zeros(w * h, np.uint8)
+    cells[24 * w + 23] = 0x80
+    cells[24 * w + 20] = 1
+    g.load(cells)
+    g.advance(6)
+    out = g.store()
+    live = np.nonzero(out & 0x7F)[0]
+    assert len(live) == 1 and out[live[0]] & 0x7F == 1 << 3 and live[0] == 24 * w + 20
+
+
+@pytest.mark.parametrize("rest", [True, False])
+def test_a_periodic_box_conserves_mass_and_momentum(LG, O, rest):
+    """src/gpu.rs:889-924."""
+    w, h = 128, 64
+    d = np.zeros(w * h, np.uint64)
+    O.lib().lgo_rng_draws(7, O.ptr(d, O.C.c_uint64), d.size)
+    cells = ((d >> np.uint64(32)) & np.uint64(0xFF)).astype(np.uint8) & (0x7F if rest else 0x3F)
+    before = O.invariants(cells)
+    g = LG.GpuLattice(w, h, rest, 0xC0FFEE)
+    g.load(cells)
+    g.advance(250)
+    assert O.invariants(g.store()) == before
+
+
+@pytest.mark.parametrize("w", [64, 100, 33, 20])
+def test_load_and_store_round_trip(LG, O, w):
+    """src/gpu.rs:929-948."""
+    h = 16
+    d = np.zeros(w * h, np.uint64)
+    O.lib().lgo_rng_draws(11, O.ptr(d, O.C.c_uint64), d.size)
+    b = ((d >> np.uint64(32)) & np.uint64(0xFF)).astype(np.uint8)
+    want = np.where(b & 0x80, 0x80, b & 0x7F).astype(np.uint8)
+    g = LG.GpuLattice(w, h, True, 1)
+    g.load(want)
+    assert np.array_equal(g.store(), want)
+
+
+@pytest.mark.parametrize("w,h,block", [(256, 128, 20), (200, 96, 16)])
+def test_the_gpu_coarse_grains_the_same_field(LG, O, w, h, block):
+    """src/gpu.rs:955-994, bit-exact against the CPU Field::sample."""
+    cpu = O.Lattice(w, h, 0.22, (0.3, 0.0), 0, True, 4, 0x5EED)
+    yc = np.float32(h) * O.SQRT3_2 / np.float32(2.0)
+    cpu.add_circle(np.float32(60.0), yc, np.float32(18.0))
+    cpu.init_equilibrium()
+    cpu.advance(30)
+    want = O.Field(w, h, block, block)
+    want.sample(cpu.cells, w, h, 1.0)
+    g = LG.GpuLattice(w, h, True, 1)
+    g.attach_field(block, block)
+    g.load(cpu.cells.copy())
+    g.sample_field(1.0)
+    f = g.read_field()
+    for a, b in zip((want.ux, want.uy, want.rho, want.solid), (f.ux, f.uy, f.rho, f.solid)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    for a, b in zip(O.block_sums(cpu.cells, w, h, block, block), g.read_block_sums()):
+        assert np.array_equal(a, b)
+
+
+def test_the_gpu_field_averages_over_time(LG, O):
+    """src/gpu.rs:999-1032, bit-exact."""
+    ALPHA = 0.2
+    w, h, block = 192, 96, 16
+    cpu = O.Lattice(w, h, 0.22, (0.3, 0.0), 4, True, 1, 0x5EED)
+    cpu.init_equilibrium()
+    want = O.Field(w, h, block, block)
+    g = LG.GpuLattice(w, h, True, 1)
+    g.attach_field(block, block)
+    g.load(cpu.cells.copy())
+    for _ in range(6):
+        want.sample(cpu.cells, w, h, ALPHA)
+        g.sample_field(ALPHA)
+        cpu.advance(5)
+        g.load(cpu.cells.copy())
+    f = g.read_field()
+    assert np.array_equal(want.ux, f.ux) and np.array_equal(want.rho, f.rho)
+
+
+@pytest.mark.parametrize("w,h", [(256, 64), (100, 32), (129, 18)])
+def test_the_gpu_counts_the_same_particles(LG, O, w, h):
+    """src/gpu.rs:1036-1053."""
+    cpu = O.Lattice(w, h, 0.3, (0.2, 0.0), 0, True, 1, 0x5EED)
+    cpu.add_box(20.0, 30.0, 5.0, 15.0, strict=True)
+    cpu.init_equilibrium()
+    cpu.advance(20)
+    g = LG.GpuLattice(w, h, True, 1)
+    g.load(cpu.cells.copy())
+    assert g.total_particles() == cpu.total_particles()
+
+
+@pytest.mark.parametrize("cols", [8, 40])
+def test_the_inlet_reseeds_at_the_requested_equilibrium(LG, O, cols):
+    """src/gpu.rs:1058-1103."""
+    w, h, steps = 128, 64, 60
+    g = LG.GpuLattice(w, h, True, 0xC0FFEE)
+    g.set_inlet(cols, 0.22, (0.4, 0.0), True)
+    g.load(np.zeros(w * h, np.uint8))
+    hits = np.zeros(7)
+    n = 0
+    for _ in range(steps):
+        g.advance(1)
+        c = g.store().reshape(h, w)[:, :cols]
+        for d in range(7):
+            hits[d] += ((c >> d) & 1).sum()
+        n += c.size
+    want = O.thresholds(0.22, 0.4, 0.0, True)
+    for d in range(7):
+        p = float(want[d]) / 2 ** 24
+        assert abs(hits[d] / n - p) < 5 * (p * (1 - p) / n) ** 0.5
+
+
+def test_the_inlet_does_not_seed_obstacles(LG):
+    """src/gpu.rs:1109-1125."""
+    w, h = 96, 32
+    g = LG.GpuLattice(w, h, True, 5)
+    g.set_inlet(w, 0.4, (0.3, 0.0), True)
+    g.load(np.full(w * h, 0x80, np.uint8))
+    g.advance(10)
+    assert (g.store() == 0x80).all()
+
+
+def test_the_inlet_leaves_the_rest_of_the_lattice_alone(LG):
+    """src/gpu.rs:1129-1152."""
+    w, h, cols = 128, 32, 8
+    g = LG.GpuLattice(w, h, True, 9)
+    g.set_inlet(cols, 0.4, (0.3, 0.0), True)
+    g.load(np.zeros(w * h, np.uint8))
+    g.advance(1)
+    c = g.store().reshape(h, w)
+    assert (c[:, cols:] == 0).all() and (c[:, :cols] != 0).sum() > h * cols / 2
+
+
+def test_the_gpu_agrees_with_the_cpu_on_the_bulk_numbers(LG, O):
+    """src/gpu.rs:1424-1451."""
+    w, h = 256, 128
+    cpu = O.Lattice(w, h, 0.22, (0.3, 0.0), 0, True, 4, 0x5EED)
+    cpu.init_equilibrium()
+    g = LG.GpuLattice(w, h, True, 0x5EED)
+    g.load(cpu.cells.copy())
+    cpu.advance(120)
+    g.advance(120)
+    gl = O.Lattice(w, h, 0.22, (0.3, 0.0), 0, True, 1, 1)
+    gl.set_cells(g.store())
+    (ax, ay), (bx, by) = cpu.mean_velocity(), gl.mean_velocity()
+    assert abs(ax - bx) < 0.02 and abs(ay - by) < 0.02
+    assert abs(cpu.total_particles() - gl.total_particles()) / cpu.total_particles() < 0.01
+
+
+# ---- bit-exact against the oracle ----------------------------------------
+
+def test_periodic_box_bit_exact(LG, O):
+    """256x128 periodic FHP-III box, Bernoulli(0.25), 500 steps, 8x8 block sums."""
+    from lattice_gas import workloads as W
+    wl = W.periodic_box()
+    g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells, block=8)
+    before = O.invariants(wl.cells)
+    g.advance_sampling(500, 100, 1.0)
+    o.advance_sampling(500, 100, 1.0)
+    assert_same(g, o)
+    assert O.invariants(g.store()) == before
+    mass, px, py, _ = g.read_block_sums()
+    assert (int(mass.sum()), int(px.sum()), int(py.sum())) == before
+
+
+@pytest.mark.parametrize("w,h,inlet,rest", [
+    (100, 34, 40, True),    # ragged width, two-word inlet
+    (33, 20, 8, True),      # one valid bit in the last word
+    (20, 16, 8, True),      # one word per row: both wraps hit the same word
+    (64, 18, 0, False),     # no rest particles
+    (129, 40, 70, False),   # no rest, three-word inlet, ragged
+    (1000, 64, 8, True),    # many warps per row, rows straddling warps
+])
+def test_small_lattices_bit_exact(LG, O, w, h, inlet, rest):
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, w / 2.0, h * 0.43, min(w, h) / 5.0)
+    LG.init_equilibrium(cells, 0.3, 0.2, 0.0, rest, 1234 + w)
+    g, o = pair(LG, O, w, h, rest, 0xDEADBEEF12345678 + w, cells,
+                inlet=(inlet, 0.3, (0.2, 0.0), rest) if inlet else None, block=8)
+    for chunk in (1, 7, 64, 100):   # crosses inlet draw chunks
+        g.advance_sampling(chunk, 10, 0.3)
+        o.advance_sampling(chunk, 10, 0.3)
+        assert_same(g, o)
+
+
+def test_restart_resets_the_stream(LG, O):
+    w, h = 96, 32
+    cells = np.zeros(w * h, np.uint8)
+    LG.init_equilibrium(cells, 0.3, 0.1, 0.0, True, 5)
+    g, o = pair(LG, O, w, h, True, 1, cells, inlet=(8, 0.3, (0.1, 0.0), True))
+    g.advance(37)
+    o.advance(37)
+    g.restart(cells, 99)
+    o.restart(cells, 99)
+    g.advance(20)
+    o.advance(20)
+    assert_same(g, o)
+
+
+def test_wake_run_reduced_bit_exact(LG, O):
+    """The wake run's geometry (plate, inflow, walls) at 512 x 288, 300 steps."""
+    from lattice_gas import workloads as W
+    wl = W.wake_run(w=512, h=288, steps=300)
+    g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells,
+                inlet=(wl.inlet_cols, wl.density, wl.inflow, True), block=wl.block)
+    g.advance_sampling(300, wl.sample_every, wl.alpha)
+    o.advance_sampling(300, wl.sample_every, wl.alpha)
+    assert_same(g, o)
+
+
+def test_wake_run_full_size_bit_exact(LG, O):
+    """4096 x 2304, the full-size wake run, 40 steps against the oracle."""
+    from lattice_gas import workloads as W
+    wl = W.wake_run()
+    g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells,
+                inlet=(wl.inlet_cols, wl.density, wl.inflow, True), block=wl.block)
+    g.advance_sampling(40, 20, wl.alpha)
+    o.advance_sampling(40, 20, wl.alpha)
+    assert_same(g, o)
+
+
+def test_roofline_geometry_reduced_bit_exact(LG, O):
+    """Circles + inflow (the roofline case's geometry) at 2048 x 1024, 30 steps."""
+    from lattice_gas import workloads as W
+    wl = W.roofline_case(w=2048, h=1024, n_circles=12)
+    g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells,
+                inlet=(wl.inlet_cols, wl.density, wl.inflow, True), block=32)
+    g.advance_sampling(30, 10, 1.0)
+    o.advance_sampling(30, 10, 1.0)
+    assert_same(g, o)
+
+
+def test_transport_sweep_members_bit_exact(LG, O):
+    """Three lattices of the transport sweep (shear-wave starts), 200 steps."""
+    from lattice_gas import workloads as W
+    for wl in W.transport_sweep(n=3, wmax=600, hmax=400):
+        g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells, block=wl.block)
+        g.advance_sampling(200, wl.sample_every, wl.alpha)
+        o.advance_sampling(200, wl.sample_every, wl.alpha)
+        assert_same(g, o)
+
+
+def test_full_size_periodic_conservation(LG, O):
+    """32768 x 16384 without inlet: mass and momentum exact after 20 steps (the
+    roofline case's size; a size-independent invariant)."""
+    w, h = 32768, 16384
+    cells = np.zeros(w * h, np.uint8)
+    LG.init_equilibrium(cells, 0.2, 0.0, 0.0, True, 77)
+    before = O.invariants(cells)
+    g = LG.GpuLattice(w, h, True, 77)
+    g.attach_field(32, 32)
+    g.load(cells)
+    del cells
+    g.advance_sampling(20, 20, 1.0)
+    mass, px, py, _ = g.read_block_sums()
+    assert (int(mass.sum(dtype=np.int64)), int(px.sum(dtype=np.int64)),
+            int(py.sum(dtype=np.int64))) == before
+    assert g.total_particles() == before[0]
