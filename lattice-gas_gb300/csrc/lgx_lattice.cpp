@@ -60,6 +60,7 @@ struct lgx_lattice {
   // inlet draws for the current chunk of steps
   uint32_t* inlet = nullptr;
   uint32_t inlet_cap = 0;      // steps the buffer holds
+  size_t inlet_words = 0;      // its size in words
   uint64_t inlet_first = 0;    // step index of slot 0
   uint32_t inlet_valid = 0;    // slots filled
   // field
@@ -119,14 +120,18 @@ int ensure_inlet(lgx_lattice* lat, uint64_t want) {
   if (lat->steps >= lat->inlet_first && lat->steps < lat->inlet_first + lat->inlet_valid)
     return LGX_OK;
   const uint32_t n = (uint32_t)std::min<uint64_t>(want, lgx::kInletChunk);
-  if (n > lat->inlet_cap) {
+  // words one step of draws occupies; the inlet width can change between calls
+  const size_t per_step = (size_t)lat->dm.h * lat->dm.iw * 7;
+  if (n > lat->inlet_cap || per_step * lgx::kInletChunk > lat->inlet_words) {
     // the buffer may still be read by enqueued steps
     LGX_CUDA(cudaStreamSynchronize(lat->stream));
     cudaFree(lat->inlet);
     lat->inlet = nullptr;
-    const size_t bytes = (size_t)lgx::kInletChunk * lat->dm.h * lat->dm.iw * 7 * sizeof(uint32_t);
-    LGX_CUDA(cudaMalloc(&lat->inlet, bytes));
+    lat->inlet_cap = 0;
+    lat->inlet_words = 0;
+    LGX_CUDA(cudaMalloc(&lat->inlet, per_step * lgx::kInletChunk * sizeof(uint32_t)));
     lat->inlet_cap = lgx::kInletChunk;
+    lat->inlet_words = per_step * lgx::kInletChunk;
   }
   lgx::InletArgs ia;
   ia.out = lat->inlet;
