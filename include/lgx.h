@@ -104,6 +104,12 @@ int lgx_timing_elapsed(lgx_lattice *lat, int a, int b, float *ms);
  * 16 set if lanes disagreed.  n must be 48 * (rest ? 128 : 64). */
 int lgx_verify_circuit(int rest_particles, uint32_t *out, size_t n);
 
+/* Instrumentation: the current device's throughput, in instructions per
+ * second, of one integer instruction kind issued from eight independent
+ * chains per thread on every SM: op 0 = lop3, 1 = 32-bit multiply-add,
+ * 2 = funnel shift, 3 = add, 4 = high-half multiply.  The denominators of the step's integer roofline. */
+int lgx_probe_int_rate(int op, double *ops_per_s);
+
 /* ---- host-side lattice setup (src/lattice.rs, src/hex.rs) ---------------- */
 
 /* Equilibrium::new(..).thresholds() (src/lattice.rs:72-92): 24-bit thresholds,

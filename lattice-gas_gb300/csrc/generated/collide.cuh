@@ -48,6 +48,11 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x03(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x03;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0x04(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x04;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0x07(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x07;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
@@ -61,6 +66,11 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x08(uint32_t a, uint32_t b, uint32
 __device__ __forceinline__ uint32_t lgx_lop3_0x0c(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x0c;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x0f(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x0f;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0x10(uint32_t a, uint32_t b, uint32_t c) {
@@ -78,6 +88,21 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x15(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x15;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0x17(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x17;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x18(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x18;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x1b(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x1b;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0x1f(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x1f;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
@@ -88,9 +113,14 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x20(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x20;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0x23(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0x24(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0x23;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0x24;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x27(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x27;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0x2a(uint32_t a, uint32_t b, uint32_t c) {
@@ -98,9 +128,24 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x2a(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x2a;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0x2e(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x2e;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x2f(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x2f;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0x30(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x30;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x31(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x31;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0x35(uint32_t a, uint32_t b, uint32_t c) {
@@ -108,9 +153,9 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x35(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x35;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0x3a(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0x3c(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0x3a;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0x3c;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0x40(uint32_t a, uint32_t b, uint32_t c) {
@@ -118,19 +163,24 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x40(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x40;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0x42(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x42;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0x45(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x45;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0x51(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0x4f(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0x51;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0x4f;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0x53(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0x50(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0x53;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0x50;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0x54(uint32_t a, uint32_t b, uint32_t c) {
@@ -138,9 +188,24 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x54(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x54;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0x69(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x69;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0x70(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x70;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x73(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x73;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x7c(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x7c;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0x80(uint32_t a, uint32_t b, uint32_t c) {
@@ -148,14 +213,39 @@ __device__ __forceinline__ uint32_t lgx_lop3_0x80(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0x80;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0x81(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x81;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x87(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x87;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0x8a(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0x8a;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0xab(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0x8e(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0xab;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0x8e;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0x8f(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0x8f;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0xa3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xa3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0xa8(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xa8;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0xac(uint32_t a, uint32_t b, uint32_t c) {
@@ -163,14 +253,29 @@ __device__ __forceinline__ uint32_t lgx_lop3_0xac(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0xac;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
+__device__ __forceinline__ uint32_t lgx_lop3_0xb3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xb3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0xb5(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xb5;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0xbc(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xbc;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
 __device__ __forceinline__ uint32_t lgx_lop3_0xc0(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
   asm("lop3.b32 %0, %1, %2, %3, 0xc0;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0xc5(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0xc3(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0xc5;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0xc3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 __device__ __forceinline__ uint32_t lgx_lop3_0xc8(uint32_t a, uint32_t b, uint32_t c) {
@@ -183,9 +288,14 @@ __device__ __forceinline__ uint32_t lgx_lop3_0xca(uint32_t a, uint32_t b, uint32
   asm("lop3.b32 %0, %1, %2, %3, 0xca;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
-__device__ __forceinline__ uint32_t lgx_lop3_0xd0(uint32_t a, uint32_t b, uint32_t c) {
+__device__ __forceinline__ uint32_t lgx_lop3_0xe5(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
-  asm("lop3.b32 %0, %1, %2, %3, 0xd0;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  asm("lop3.b32 %0, %1, %2, %3, 0xe5;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t lgx_lop3_0xe8(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xe8;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
   return r;
 }
 #endif
@@ -198,7 +308,7 @@ __device__ __forceinline__ uint32_t lgx_lop3_0xd0(uint32_t a, uint32_t b, uint32
 
 #endif
 
-// lgx_collide_rest: 261 lop3 per 32-cell word (rest particles: yes)
+// lgx_collide_rest: 161 lop3 per 32-cell word (rest particles: yes)
 LGX_HD_INLINE void lgx_collide_rest(const uint32_t n[7], uint32_t s2, const uint32_t s3[3],
                       const uint32_t s5[5], uint32_t o[7]) {
   const uint32_t n0 = n[0];
@@ -216,274 +326,174 @@ LGX_HD_INLINE void lgx_collide_rest(const uint32_t n[7], uint32_t s2, const uint
   const uint32_t s5_2 = s5[2];
   const uint32_t s5_3 = s5[3];
   const uint32_t s5_4 = s5[4];
-  const uint32_t t17 = LGX_LOP3(n0, n3, 0u, 0x03);
-  const uint32_t t18 = LGX_LOP3(n0, n3, 0u, 0x30);
-  const uint32_t t19 = LGX_LOP3(n0, n3, 0u, 0x0c);
-  const uint32_t t20 = LGX_LOP3(n0, n3, 0u, 0xc0);
-  const uint32_t t21 = LGX_LOP3(n1, n4, 0u, 0x03);
-  const uint32_t t22 = LGX_LOP3(n1, n4, 0u, 0x30);
-  const uint32_t t24 = LGX_LOP3(n1, n4, 0u, 0xc0);
-  const uint32_t t25 = LGX_LOP3(n2, n5, 0u, 0x03);
-  const uint32_t t26 = LGX_LOP3(n2, n5, 0u, 0x30);
-  const uint32_t t28 = LGX_LOP3(n2, n5, 0u, 0xc0);
-  const uint32_t t29 = LGX_LOP3(n1, n4, t26, 0x08);
-  const uint32_t t30 = LGX_LOP3(n0, n3, t29, 0x02);
-  const uint32_t t31 = LGX_LOP3(n1, n4, t25, 0x02);
-  const uint32_t t32 = LGX_LOP3(n0, n3, t31, 0x08);
-  const uint32_t t35 = LGX_LOP3(n6, t30, t32, 0x53);
-  const uint32_t t36 = LGX_LOP3(n2, n5, t21, 0x08);
-  const uint32_t t37 = LGX_LOP3(n0, n3, t36, 0x08);
-  const uint32_t t38 = LGX_LOP3(n1, n4, t25, 0x08);
-  const uint32_t t39 = LGX_LOP3(n0, n3, t38, 0x02);
-  const uint32_t t42 = LGX_LOP3(n6, t37, t39, 0x53);
-  const uint32_t t43 = LGX_LOP3(n1, n4, t25, 0x20);
-  const uint32_t t44 = LGX_LOP3(n0, n3, t43, 0x08);
-  const uint32_t t45 = LGX_LOP3(n2, n5, t21, 0x20);
-  const uint32_t t46 = LGX_LOP3(n0, n3, t45, 0x02);
-  const uint32_t t49 = LGX_LOP3(n6, t44, t46, 0x53);
-  const uint32_t t51 = LGX_LOP3(n1, n4, t25, 0x80);
-  const uint32_t t52 = LGX_LOP3(n0, n3, t51, 0x02);
-  const uint32_t t53 = LGX_LOP3(n1, n4, t28, 0x02);
-  const uint32_t t55 = LGX_LOP3(t20, t31, t52, 0x15);
-  const uint32_t t56 = LGX_LOP3(t17, t53, t55, 0x2a);
-  const uint32_t t57 = LGX_LOP3(n6, t56, 0u, 0x03);
-  const uint32_t t58 = LGX_LOP3(n0, n3, t38, 0x20);
-  const uint32_t t59 = LGX_LOP3(n0, n3, t36, 0x02);
-  const uint32_t t62 = LGX_LOP3(n6, t58, t59, 0x53);
-  const uint32_t t63 = LGX_LOP3(n0, n3, t45, 0x20);
-  const uint32_t t64 = LGX_LOP3(n0, n3, t43, 0x02);
-  const uint32_t t67 = LGX_LOP3(n6, t63, t64, 0x53);
-  const uint32_t t68 = LGX_LOP3(n2, n5, t22, 0x08);
-  const uint32_t t69 = LGX_LOP3(n0, n3, t68, 0x02);
-  const uint32_t t70 = LGX_LOP3(n0, n3, t31, 0x20);
-  const uint32_t t73 = LGX_LOP3(n6, t69, t70, 0x53);
-  const uint32_t t76 = LGX_LOP3(t19, t51, t53, 0x1f);
-  const uint32_t t79 = LGX_LOP3(n6, t30, t76, 0x3a);
-  const uint32_t t80 = LGX_LOP3(n0, n3, t38, 0x80);
-  const uint32_t t81 = LGX_LOP3(n1, n4, t28, 0x08);
-  const uint32_t t83 = LGX_LOP3(t17, t80, t81, 0x13);
-  const uint32_t t86 = LGX_LOP3(n6, t37, t83, 0x3a);
-  const uint32_t t88 = LGX_LOP3(n2, n5, t24, 0x20);
-  const uint32_t t89 = LGX_LOP3(n0, n3, t88, 0x02);
-  const uint32_t t90 = LGX_LOP3(t20, t45, t89, 0x15);
-  const uint32_t t93 = LGX_LOP3(n6, t44, t90, 0x3a);
-  const uint32_t t95 = LGX_LOP3(n0, n3, t68, 0x08);
-  const uint32_t t96 = LGX_LOP3(t18, t29, t95, 0x15);
-  const uint32_t t99 = LGX_LOP3(n6, t56, t96, 0xca);
-  const uint32_t t101 = LGX_LOP3(n2, n5, t24, 0x08);
-  const uint32_t t102 = LGX_LOP3(n0, n3, t101, 0x02);
-  const uint32_t t103 = LGX_LOP3(t20, t36, t102, 0x15);
-  const uint32_t t106 = LGX_LOP3(n6, t58, t103, 0x3a);
-  const uint32_t t108 = LGX_LOP3(n1, n4, t28, 0x20);
-  const uint32_t t109 = LGX_LOP3(n0, n3, t108, 0x02);
-  const uint32_t t110 = LGX_LOP3(t20, t43, t109, 0x15);
-  const uint32_t t113 = LGX_LOP3(n6, t63, t110, 0x3a);
-  const uint32_t t116 = LGX_LOP3(t18, t51, t53, 0x1f);
-  const uint32_t t119 = LGX_LOP3(n6, t69, t116, 0x3a);
-  const uint32_t t120 = LGX_LOP3(n0, n3, t29, 0x80);
-  const uint32_t t123 = LGX_LOP3(n6, t76, t120, 0xc5);
-  const uint32_t t124 = LGX_LOP3(n0, n3, t101, 0x08);
-  const uint32_t t127 = LGX_LOP3(n6, t83, t124, 0xc5);
-  const uint32_t t128 = LGX_LOP3(n0, n3, t108, 0x08);
-  const uint32_t t131 = LGX_LOP3(n6, t90, t128, 0xc5);
-  const uint32_t t134 = LGX_LOP3(n1, n4, t28, 0x80);
-  const uint32_t t136 = LGX_LOP3(t20, t51, t53, 0x1f);
-  const uint32_t t137 = LGX_LOP3(t17, t134, t136, 0x2a);
-  const uint32_t t140 = LGX_LOP3(n6, t96, t137, 0xca);
-  const uint32_t t141 = LGX_LOP3(n0, n3, t81, 0x20);
-  const uint32_t t144 = LGX_LOP3(n6, t103, t141, 0xc5);
-  const uint32_t t145 = LGX_LOP3(n0, n3, t88, 0x20);
-  const uint32_t t148 = LGX_LOP3(n6, t110, t145, 0xc5);
-  const uint32_t t149 = LGX_LOP3(n0, n3, t68, 0x80);
-  const uint32_t t152 = LGX_LOP3(n6, t116, t149, 0xc5);
-  const uint32_t t153 = LGX_LOP3(n0, n3, t134, 0x08);
-  const uint32_t t156 = LGX_LOP3(n6, t120, t153, 0x35);
-  const uint32_t t157 = LGX_LOP3(n0, n3, t81, 0x80);
-  const uint32_t t160 = LGX_LOP3(n6, t124, t157, 0x35);
-  const uint32_t t161 = LGX_LOP3(n0, n3, t88, 0x80);
-  const uint32_t t164 = LGX_LOP3(n6, t128, t161, 0x35);
-  const uint32_t t165 = LGX_LOP3(n6, t137, 0u, 0x30);
-  const uint32_t t166 = LGX_LOP3(n0, n3, t101, 0x80);
-  const uint32_t t169 = LGX_LOP3(n6, t141, t166, 0x35);
-  const uint32_t t170 = LGX_LOP3(n0, n3, t108, 0x80);
-  const uint32_t t173 = LGX_LOP3(n6, t145, t170, 0x35);
-  const uint32_t t174 = LGX_LOP3(n0, n3, t134, 0x20);
-  const uint32_t t177 = LGX_LOP3(n6, t149, t174, 0x35);
-  const uint32_t t179 = LGX_LOP3(s3_0, s3_1, s3_2, 0x01);
-  const uint32_t t181 = LGX_LOP3(s5_2, s5_3, 0u, 0x03);
-  const uint32_t t182 = LGX_LOP3(s5_0, s5_1, t181, 0x02);
-  const uint32_t t185 = LGX_LOP3(t49, t62, 0u, 0xc0);
-  const uint32_t t187 = LGX_LOP3(t156, t160, 0u, 0xc0);
-  const uint32_t t188 = LGX_LOP3(t164, t169, 0u, 0xc0);
-  const uint32_t t190 = LGX_LOP3(t35, t42, t185, 0x80);
-  const uint32_t t191 = LGX_LOP3(t67, t73, t187, 0x80);
-  const uint32_t t192 = LGX_LOP3(t173, t177, t188, 0x80);
-  const uint32_t t194 = LGX_LOP3(t190, t191, t192, 0x80);
-  const uint32_t t195 = LGX_LOP3(t57, t79, 0u, 0x0c);
-  const uint32_t t196 = LGX_LOP3(t86, t93, 0u, 0xc0);
-  const uint32_t t197 = LGX_LOP3(t106, t113, 0u, 0xc0);
-  const uint32_t t198 = LGX_LOP3(t119, t123, 0u, 0xc0);
-  const uint32_t t199 = LGX_LOP3(t127, t131, 0u, 0xc0);
-  const uint32_t t200 = LGX_LOP3(t144, t148, 0u, 0xc0);
-  const uint32_t t201 = LGX_LOP3(t152, t165, 0u, 0x30);
-  const uint32_t t202 = LGX_LOP3(t195, t196, 0u, 0xc0);
-  const uint32_t t205 = LGX_LOP3(t197, t198, t202, 0x80);
-  const uint32_t t206 = LGX_LOP3(t199, t200, t201, 0x80);
-  const uint32_t t208 = LGX_LOP3(t179, t205, t206, 0x07);
-  const uint32_t t209 = LGX_LOP3(t99, t140, 0u, 0xc0);
-  const uint32_t t210 = LGX_LOP3(s5_4, t182, t209, 0x51);
-  const uint32_t t212 = LGX_LOP3(t194, t208, t210, 0x10);
-  const uint32_t t213 = LGX_LOP3(n0, t212, 0u, 0xc0);
-  const uint32_t t215 = LGX_LOP3(t160, t164, 0u, 0xc0);
-  const uint32_t t216 = LGX_LOP3(t169, t173, 0u, 0xc0);
-  const uint32_t t217 = LGX_LOP3(t62, t67, t215, 0x80);
-  const uint32_t t218 = LGX_LOP3(t177, t216, 0u, 0xc0);
-  const uint32_t t221 = LGX_LOP3(t73, t156, t216, 0x80);
-  const uint32_t t223 = LGX_LOP3(s2, t217, t218, 0x70);
-  const uint32_t t224 = LGX_LOP3(s2, t177, t221, 0x07);
-  const uint32_t t226 = LGX_LOP3(t57, t86, 0u, 0x0c);
-  const uint32_t t227 = LGX_LOP3(t93, t106, 0u, 0xc0);
-  const uint32_t t228 = LGX_LOP3(t113, t119, 0u, 0xc0);
-  const uint32_t t230 = LGX_LOP3(t148, t152, 0u, 0xc0);
-  const uint32_t t231 = LGX_LOP3(t226, t227, 0u, 0xc0);
-  const uint32_t t232 = LGX_LOP3(t123, t144, t228, 0x80);
-  const uint32_t t233 = LGX_LOP3(t165, t230, 0u, 0x0c);
-  const uint32_t t235 = LGX_LOP3(t231, t232, t233, 0x80);
-  const uint32_t t237 = LGX_LOP3(t119, t127, 0u, 0xc0);
-  const uint32_t t238 = LGX_LOP3(t131, t144, 0u, 0xc0);
-  const uint32_t t240 = LGX_LOP3(t233, t237, t238, 0x80);
-  const uint32_t t241 = LGX_LOP3(s3_1, t240, 0u, 0x30);
-  const uint32_t t243 = LGX_LOP3(s3_2, t152, t197, 0x70);
-  const uint32_t t244 = LGX_LOP3(s5_0, t209, 0u, 0x30);
-  const uint32_t t245 = LGX_LOP3(s5_1, t140, 0u, 0x30);
-  const uint32_t t246 = LGX_LOP3(s5_2, t99, 0u, 0x30);
-  const uint32_t t247 = LGX_LOP3(s5_3, t140, 0u, 0x30);
-  const uint32_t t248 = LGX_LOP3(t213, t223, t224, 0x01);
-  const uint32_t t249 = LGX_LOP3(s3_0, t235, t241, 0x45);
-  const uint32_t t250 = LGX_LOP3(s5_0, t209, t243, 0x45);
-  const uint32_t t253 = LGX_LOP3(t245, t246, t250, 0x02);
-  const uint32_t t254 = LGX_LOP3(t248, t249, t253, 0x80);
-  const uint32_t t255 = LGX_LOP3(s5_3, t140, t254, 0x8a);
-  const uint32_t t258 = LGX_LOP3(t156, t164, 0u, 0xc0);
-  const uint32_t t259 = LGX_LOP3(t49, t73, t258, 0x80);
-  const uint32_t t262 = LGX_LOP3(t164, t173, 0u, 0xc0);
-  const uint32_t t263 = LGX_LOP3(t67, t160, t262, 0x80);
-  const uint32_t t265 = LGX_LOP3(s2, t218, t259, 0x70);
-  const uint32_t t266 = LGX_LOP3(s2, t177, t263, 0x07);
-  const uint32_t t267 = LGX_LOP3(t265, t266, 0u, 0x03);
-  const uint32_t t270 = LGX_LOP3(t79, t113, t237, 0x80);
-  const uint32_t t271 = LGX_LOP3(t131, t148, t201, 0x80);
-  const uint32_t t273 = LGX_LOP3(s3_0, t270, t271, 0x70);
-  const uint32_t t276 = LGX_LOP3(t57, t93, t197, 0x08);
-  const uint32_t t277 = LGX_LOP3(t123, t148, t152, 0x80);
-  const uint32_t t279 = LGX_LOP3(s3_1, t276, t277, 0x70);
-  const uint32_t t281 = LGX_LOP3(t148, t165, 0u, 0x30);
-  const uint32_t t282 = LGX_LOP3(t93, t119, t238, 0x80);
-  const uint32_t t284 = LGX_LOP3(s3_2, t281, t282, 0x70);
-  const uint32_t t285 = LGX_LOP3(s5_0, t140, 0u, 0x30);
-  const uint32_t t287 = LGX_LOP3(s5_2, t140, 0u, 0x30);
-  const uint32_t t289 = LGX_LOP3(s5_4, t140, 0u, 0x30);
-  const uint32_t t290 = LGX_LOP3(n1, t212, t267, 0x2a);
-  const uint32_t t293 = LGX_LOP3(s5_1, t99, t287, 0x45);
-  const uint32_t t294 = LGX_LOP3(s5_3, t99, t289, 0x45);
-  const uint32_t t295 = LGX_LOP3(t273, t279, t290, 0x02);
-  const uint32_t t296 = LGX_LOP3(t284, t285, t293, 0x02);
-  const uint32_t t298 = LGX_LOP3(t294, t295, t296, 0x80);
-  const uint32_t t301 = LGX_LOP3(t35, t67, t187, 0x80);
-  const uint32_t t303 = LGX_LOP3(t177, t262, t301, 0x80);
-  const uint32_t t305 = LGX_LOP3(t49, t156, t188, 0x80);
-  const uint32_t t306 = LGX_LOP3(t173, t305, 0u, 0xc0);
-  const uint32_t t309 = LGX_LOP3(s2, t303, t306, 0xca);
-  const uint32_t t311 = LGX_LOP3(t93, t123, t238, 0x80);
-  const uint32_t t313 = LGX_LOP3(s3_0, t148, t311, 0x70);
-  const uint32_t t314 = LGX_LOP3(t79, t86, 0u, 0xc0);
-  const uint32_t t317 = LGX_LOP3(t93, t113, t314, 0x80);
-  const uint32_t t318 = LGX_LOP3(t119, t131, t165, 0x40);
-  const uint32_t t320 = LGX_LOP3(s3_1, t317, t318, 0x70);
-  const uint32_t t322 = LGX_LOP3(t113, t123, t195, 0x80);
-  const uint32_t t324 = LGX_LOP3(t199, t230, t322, 0x80);
-  const uint32_t t326 = LGX_LOP3(s3_2, t165, t324, 0xd0);
-  const uint32_t t329 = LGX_LOP3(n2, t212, t309, 0x2a);
-  const uint32_t t331 = LGX_LOP3(s5_0, t99, t326, 0x45);
-  const uint32_t t333 = LGX_LOP3(s5_4, t99, t247, 0x45);
-  const uint32_t t334 = LGX_LOP3(t313, t320, t329, 0x02);
-  const uint32_t t335 = LGX_LOP3(t245, t287, t331, 0x02);
-  const uint32_t t337 = LGX_LOP3(t333, t334, t335, 0x80);
-  const uint32_t t340 = LGX_LOP3(t42, t49, t187, 0x80);
-  const uint32_t t342 = LGX_LOP3(t173, t188, t340, 0x80);
-  const uint32_t t344 = LGX_LOP3(t35, t156, t215, 0x80);
-  const uint32_t t345 = LGX_LOP3(t177, t344, 0u, 0xc0);
-  const uint32_t t348 = LGX_LOP3(s2, t342, t345, 0xca);
-  const uint32_t t349 = LGX_LOP3(t123, t127, 0u, 0xc0);
-  const uint32_t t352 = LGX_LOP3(t131, t152, t165, 0x40);
-  const uint32_t t353 = LGX_LOP3(t197, t202, t349, 0x80);
-  const uint32_t t355 = LGX_LOP3(s3_0, t352, t353, 0x70);
-  const uint32_t t357 = LGX_LOP3(t79, t123, t199, 0x80);
-  const uint32_t t359 = LGX_LOP3(t165, t200, t357, 0x08);
-  const uint32_t t362 = LGX_LOP3(s3_2, t123, t196, 0x70);
-  const uint32_t t363 = LGX_LOP3(s5_1, t209, 0u, 0x30);
-  const uint32_t t364 = LGX_LOP3(n3, t212, t348, 0x2a);
-  const uint32_t t365 = LGX_LOP3(s3_1, t355, t359, 0x23);
-  const uint32_t t367 = LGX_LOP3(s5_1, t209, t246, 0x45);
-  const uint32_t t369 = LGX_LOP3(t285, t362, t367, 0x02);
-  const uint32_t t370 = LGX_LOP3(t364, t365, t369, 0x80);
-  const uint32_t t371 = LGX_LOP3(s5_4, t140, t370, 0x8a);
-  const uint32_t t374 = LGX_LOP3(t35, t62, t187, 0x80);
-  const uint32_t t376 = LGX_LOP3(t177, t188, t374, 0x80);
-  const uint32_t t377 = LGX_LOP3(t42, t156, 0u, 0xc0);
-  const uint32_t t379 = LGX_LOP3(t160, t169, t377, 0x80);
-  const uint32_t t380 = LGX_LOP3(t173, t379, 0u, 0xc0);
-  const uint32_t t383 = LGX_LOP3(s2, t376, t380, 0xca);
-  const uint32_t t384 = LGX_LOP3(t127, t144, 0u, 0xc0);
-  const uint32_t t386 = LGX_LOP3(t148, t165, t384, 0x20);
-  const uint32_t t387 = LGX_LOP3(t198, t314, t386, 0x80);
-  const uint32_t t388 = LGX_LOP3(s3_0, t387, 0u, 0x30);
-  const uint32_t t390 = LGX_LOP3(t152, t231, t349, 0x80);
-  const uint32_t t394 = LGX_LOP3(t79, t106, t199, 0x80);
-  const uint32_t t395 = LGX_LOP3(t144, t165, t394, 0x20);
-  const uint32_t t398 = LGX_LOP3(n4, t212, t383, 0x2a);
-  const uint32_t t399 = LGX_LOP3(s3_1, t388, t390, 0x23);
-  const uint32_t t400 = LGX_LOP3(s3_2, t244, t395, 0x23);
-  const uint32_t t401 = LGX_LOP3(t398, t399, 0u, 0xc0);
-  const uint32_t t403 = LGX_LOP3(t287, t400, t401, 0x08);
-  const uint32_t t404 = LGX_LOP3(s5_3, t209, t403, 0x8a);
-  const uint32_t t405 = LGX_LOP3(n5, t212, 0u, 0xc0);
-  const uint32_t t407 = LGX_LOP3(t42, t73, t187, 0x80);
-  const uint32_t t410 = LGX_LOP3(t62, t160, t188, 0x80);
-  const uint32_t t412 = LGX_LOP3(s2, t218, t407, 0x70);
-  const uint32_t t413 = LGX_LOP3(s2, t177, t410, 0x07);
-  const uint32_t t416 = LGX_LOP3(t106, t127, t238, 0x80);
-  const uint32_t t418 = LGX_LOP3(s3_0, t152, t416, 0x70);
-  const uint32_t t421 = LGX_LOP3(t119, t144, t165, 0x40);
-  const uint32_t t422 = LGX_LOP3(t197, t314, t421, 0x80);
-  const uint32_t t425 = LGX_LOP3(t230, t384, 0u, 0xc0);
-  const uint32_t t426 = LGX_LOP3(t198, t226, t425, 0x80);
-  const uint32_t t428 = LGX_LOP3(s3_2, t165, t426, 0xd0);
-  const uint32_t t430 = LGX_LOP3(t405, t412, t413, 0x01);
-  const uint32_t t431 = LGX_LOP3(s3_1, t418, t422, 0x23);
-  const uint32_t t434 = LGX_LOP3(t287, t363, t428, 0x01);
-  const uint32_t t435 = LGX_LOP3(t430, t431, t434, 0x80);
-  const uint32_t t436 = LGX_LOP3(s5_4, t209, t435, 0x8a);
-  const uint32_t t437 = LGX_LOP3(n6, t212, 0u, 0xc0);
-  const uint32_t t439 = LGX_LOP3(s3_0, t165, 0u, 0xc0);
-  const uint32_t t441 = LGX_LOP3(t233, t238, t349, 0x80);
-  const uint32_t t444 = LGX_LOP3(t228, t349, 0u, 0xc0);
-  const uint32_t t446 = LGX_LOP3(t227, t314, t444, 0x80);
-  const uint32_t t447 = LGX_LOP3(t165, t230, t238, 0x08);
-  const uint32_t t449 = LGX_LOP3(s3_2, t446, t447, 0x70);
-  const uint32_t t450 = LGX_LOP3(s2, t194, t437, 0x54);
-  const uint32_t t451 = LGX_LOP3(s3_1, t439, t441, 0x23);
-  const uint32_t t452 = LGX_LOP3(s5_3, s5_4, t209, 0xab);
-  const uint32_t t454 = LGX_LOP3(t246, t449, 0u, 0x03);
-  const uint32_t t455 = LGX_LOP3(t450, t451, t454, 0x80);
-  const uint32_t t456 = LGX_LOP3(t452, t455, 0u, 0xc0);
-  o[0] = ~t255;
-  o[1] = ~t298;
-  o[2] = ~t337;
-  o[3] = ~t371;
-  o[4] = ~t404;
-  o[5] = ~t436;
-  o[6] = ~t456;
+  const uint32_t t22 = LGX_LOP3(n0, n1, n2, 0x69);
+  const uint32_t t26 = LGX_LOP3(n0, n1, n2, 0x17);
+  const uint32_t t32 = LGX_LOP3(n3, n4, n5, 0x69);
+  const uint32_t t36 = LGX_LOP3(n3, n4, n5, 0x17);
+  const uint32_t t40 = LGX_LOP3(n6, t22, t32, 0x8e);
+  const uint32_t t44 = LGX_LOP3(t26, t36, t40, 0xe8);
+  const uint32_t t65 = LGX_LOP3(n6, t44, 0u, 0x3c);
+  const uint32_t t68 = LGX_LOP3(s2, t44, 0u, 0x3c);
+  const uint32_t t71 = LGX_LOP3(s3_0, s3_2, t44, 0x1b);
+  const uint32_t t74 = LGX_LOP3(s3_1, t44, 0u, 0x0f);
+  const uint32_t t77 = LGX_LOP3(s3_0, s3_2, t44, 0x27);
+  const uint32_t t80 = LGX_LOP3(s5_0, s5_4, t44, 0x1b);
+  const uint32_t t83 = LGX_LOP3(s5_1, s5_3, t44, 0x1b);
+  const uint32_t t89 = LGX_LOP3(s5_1, s5_3, t44, 0x27);
+  const uint32_t t92 = LGX_LOP3(s5_0, s5_4, t44, 0x27);
+  const uint32_t t93 = LGX_LOP3(n0, n3, t44, 0x42);
+  const uint32_t t94 = LGX_LOP3(n0, n3, t44, 0x24);
+  const uint32_t t95 = LGX_LOP3(n0, n3, t44, 0x18);
+  const uint32_t t96 = LGX_LOP3(n0, n3, t44, 0x81);
+  const uint32_t t97 = LGX_LOP3(n1, n4, t44, 0x42);
+  const uint32_t t98 = LGX_LOP3(n1, n4, t44, 0x24);
+  const uint32_t t99 = LGX_LOP3(n1, n4, t44, 0x18);
+  const uint32_t t100 = LGX_LOP3(n1, n4, t44, 0x81);
+  const uint32_t t101 = LGX_LOP3(n2, n5, t44, 0x42);
+  const uint32_t t102 = LGX_LOP3(n2, n5, t44, 0x24);
+  const uint32_t t103 = LGX_LOP3(n2, n5, t44, 0x18);
+  const uint32_t t104 = LGX_LOP3(n2, n5, t44, 0x81);
+  const uint32_t t105 = LGX_LOP3(t93, t99, 0u, 0xc0);
+  const uint32_t t106 = LGX_LOP3(t102, t105, 0u, 0xc0);
+  const uint32_t t107 = LGX_LOP3(t95, t97, 0u, 0xc0);
+  const uint32_t t108 = LGX_LOP3(t101, t107, 0u, 0xc0);
+  const uint32_t t111 = LGX_LOP3(t65, t106, t108, 0x35);
+  const uint32_t t112 = LGX_LOP3(t103, t107, 0u, 0xc0);
+  const uint32_t t113 = LGX_LOP3(t101, t105, 0u, 0xc0);
+  const uint32_t t116 = LGX_LOP3(t65, t112, t113, 0x35);
+  const uint32_t t118 = LGX_LOP3(t95, t98, t101, 0x80);
+  const uint32_t t119 = LGX_LOP3(t93, t97, 0u, 0xc0);
+  const uint32_t t120 = LGX_LOP3(t102, t119, 0u, 0xc0);
+  const uint32_t t123 = LGX_LOP3(t65, t118, t120, 0x35);
+  const uint32_t t124 = LGX_LOP3(t96, t97, 0u, 0xc0);
+  const uint32_t t126 = LGX_LOP3(t93, t100, 0u, 0xc0);
+  const uint32_t t129 = LGX_LOP3(t101, t124, t126, 0x1f);
+  const uint32_t t130 = LGX_LOP3(t104, t119, t129, 0x2a);
+  const uint32_t t131 = LGX_LOP3(t65, t130, 0u, 0x30);
+  const uint32_t t132 = LGX_LOP3(t94, t99, 0u, 0xc0);
+  const uint32_t t133 = LGX_LOP3(t94, t99, t101, 0x80);
+  const uint32_t t134 = LGX_LOP3(t103, t119, 0u, 0xc0);
+  const uint32_t t137 = LGX_LOP3(t65, t133, t134, 0x35);
+  const uint32_t t138 = LGX_LOP3(t94, t97, 0u, 0xc0);
+  const uint32_t t139 = LGX_LOP3(t102, t138, 0u, 0xc0);
+  const uint32_t t140 = LGX_LOP3(t93, t98, 0u, 0xc0);
+  const uint32_t t141 = LGX_LOP3(t101, t140, 0u, 0xc0);
+  const uint32_t t144 = LGX_LOP3(t65, t139, t141, 0x35);
+  const uint32_t t145 = LGX_LOP3(t103, t140, 0u, 0xc0);
+  const uint32_t t146 = LGX_LOP3(t101, t138, 0u, 0xc0);
+  const uint32_t t149 = LGX_LOP3(t65, t145, t146, 0x35);
+  const uint32_t t151 = LGX_LOP3(t95, t100, t101, 0x80);
+  const uint32_t t153 = LGX_LOP3(t104, t107, t151, 0x15);
+  const uint32_t t156 = LGX_LOP3(t65, t106, t153, 0xa3);
+  const uint32_t t158 = LGX_LOP3(t96, t99, t101, 0x80);
+  const uint32_t t160 = LGX_LOP3(t104, t105, t158, 0x15);
+  const uint32_t t163 = LGX_LOP3(t65, t112, t160, 0xa3);
+  const uint32_t t166 = LGX_LOP3(t102, t124, t126, 0x1f);
+  const uint32_t t169 = LGX_LOP3(t65, t118, t166, 0xa3);
+  const uint32_t t171 = LGX_LOP3(t95, t98, t103, 0x80);
+  const uint32_t t172 = LGX_LOP3(t102, t132, t171, 0x15);
+  const uint32_t t175 = LGX_LOP3(t65, t130, t172, 0xac);
+  const uint32_t t178 = LGX_LOP3(t103, t124, t126, 0x1f);
+  const uint32_t t181 = LGX_LOP3(t65, t133, t178, 0xa3);
+  const uint32_t t183 = LGX_LOP3(t96, t98, t101, 0x80);
+  const uint32_t t185 = LGX_LOP3(t104, t140, t183, 0x15);
+  const uint32_t t188 = LGX_LOP3(t65, t139, t185, 0xa3);
+  const uint32_t t190 = LGX_LOP3(t94, t100, t101, 0x80);
+  const uint32_t t192 = LGX_LOP3(t104, t138, t190, 0x15);
+  const uint32_t t195 = LGX_LOP3(t65, t145, t192, 0xa3);
+  const uint32_t t197 = LGX_LOP3(s3_0, s3_1, s3_2, 0x01);
+  const uint32_t t199 = LGX_LOP3(s5_2, s5_3, 0u, 0x03);
+  const uint32_t t200 = LGX_LOP3(s5_0, s5_1, t199, 0x02);
+  const uint32_t t202 = LGX_LOP3(t111, t116, 0u, 0xc0);
+  const uint32_t t205 = LGX_LOP3(t123, t137, t202, 0x80);
+  const uint32_t t206 = LGX_LOP3(t144, t149, t205, 0x80);
+  const uint32_t t207 = LGX_LOP3(t131, t156, 0u, 0x0c);
+  const uint32_t t208 = LGX_LOP3(t163, t169, 0u, 0xc0);
+  const uint32_t t209 = LGX_LOP3(t181, t188, 0u, 0xc0);
+  const uint32_t t210 = LGX_LOP3(t207, t208, 0u, 0xc0);
+  const uint32_t t212 = LGX_LOP3(t195, t209, t210, 0x80);
+  const uint32_t t214 = LGX_LOP3(s5_4, t175, t200, 0x31);
+  const uint32_t t215 = LGX_LOP3(t197, t206, t212, 0xc8);
+  const uint32_t t216 = LGX_LOP3(t214, t215, 0u, 0x0c);
+  const uint32_t t217 = LGX_LOP3(t137, t144, 0u, 0xc0);
+  const uint32_t t220 = LGX_LOP3(t68, t149, t217, 0xca);
+  const uint32_t t221 = LGX_LOP3(t131, t163, 0u, 0x0c);
+  const uint32_t t222 = LGX_LOP3(t169, t181, 0u, 0xc0);
+  const uint32_t t223 = LGX_LOP3(t188, t195, 0u, 0xc0);
+  const uint32_t t224 = LGX_LOP3(t221, t222, 0u, 0xc0);
+  const uint32_t t226 = LGX_LOP3(t71, t223, t224, 0x07);
+  const uint32_t t229 = LGX_LOP3(t80, t175, 0u, 0x03);
+  const uint32_t t230 = LGX_LOP3(s5_2, t44, t175, 0x50);
+  const uint32_t t231 = LGX_LOP3(t77, t209, t229, 0x54);
+  const uint32_t t232 = LGX_LOP3(t74, t195, t226, 0x54);
+  const uint32_t t234 = LGX_LOP3(t230, t231, t232, 0x08);
+  const uint32_t t238 = LGX_LOP3(t44, t220, t234, 0x87);
+  const uint32_t t241 = LGX_LOP3(n0, t216, t238, 0x2e);
+  const uint32_t t242 = LGX_LOP3(t123, t149, 0u, 0xc0);
+  const uint32_t t245 = LGX_LOP3(t68, t144, t242, 0xca);
+  const uint32_t t247 = LGX_LOP3(t156, t188, t195, 0x80);
+  const uint32_t t250 = LGX_LOP3(t131, t169, t209, 0x08);
+  const uint32_t t251 = LGX_LOP3(s3_1, t44, t250, 0x50);
+  const uint32_t t253 = LGX_LOP3(t77, t169, t195, 0x07);
+  const uint32_t t254 = LGX_LOP3(t83, t175, 0u, 0x03);
+  const uint32_t t255 = LGX_LOP3(t89, t175, 0u, 0x03);
+  const uint32_t t256 = LGX_LOP3(t71, t247, t251, 0x54);
+  const uint32_t t257 = LGX_LOP3(t254, t255, 0u, 0x03);
+  const uint32_t t259 = LGX_LOP3(t253, t256, t257, 0x08);
+  const uint32_t t263 = LGX_LOP3(t44, t245, t259, 0x87);
+  const uint32_t t266 = LGX_LOP3(n1, t216, t263, 0x2e);
+  const uint32_t t267 = LGX_LOP3(t111, t144, 0u, 0xc0);
+  const uint32_t t270 = LGX_LOP3(t68, t123, t267, 0xca);
+  const uint32_t t272 = LGX_LOP3(t156, t163, 0u, 0xc0);
+  const uint32_t t274 = LGX_LOP3(t169, t188, t272, 0x80);
+  const uint32_t t276 = LGX_LOP3(t74, t195, t274, 0x07);
+  const uint32_t t278 = LGX_LOP3(t77, t188, t207, 0x07);
+  const uint32_t t279 = LGX_LOP3(t92, t175, 0u, 0x03);
+  const uint32_t t281 = LGX_LOP3(t71, t169, t276, 0x54);
+  const uint32_t t282 = LGX_LOP3(t229, t278, t281, 0x02);
+  const uint32_t t284 = LGX_LOP3(t270, t279, t282, 0x20);
+  const uint32_t t287 = LGX_LOP3(t44, t284, 0u, 0xc3);
+  const uint32_t t290 = LGX_LOP3(n2, t216, t287, 0x2e);
+  const uint32_t t291 = LGX_LOP3(t116, t123, 0u, 0xc0);
+  const uint32_t t294 = LGX_LOP3(t68, t111, t291, 0xca);
+  const uint32_t t296 = LGX_LOP3(t71, t209, t210, 0x07);
+  const uint32_t t300 = LGX_LOP3(t74, t156, t296, 0x54);
+  const uint32_t t301 = LGX_LOP3(t77, t208, t300, 0xa8);
+  const uint32_t t302 = LGX_LOP3(t230, t254, t301, 0x02);
+  const uint32_t t306 = LGX_LOP3(t44, t294, t302, 0x87);
+  const uint32_t t309 = LGX_LOP3(n3, t216, t306, 0x2e);
+  const uint32_t t310 = LGX_LOP3(t111, t137, 0u, 0xc0);
+  const uint32_t t313 = LGX_LOP3(t68, t116, t310, 0xca);
+  const uint32_t t315 = LGX_LOP3(t71, t195, t272, 0x07);
+  const uint32_t t318 = LGX_LOP3(t77, t156, t181, 0x07);
+  const uint32_t t320 = LGX_LOP3(t74, t224, t315, 0x54);
+  const uint32_t t321 = LGX_LOP3(t229, t318, t320, 0x02);
+  const uint32_t t323 = LGX_LOP3(t255, t313, t321, 0x08);
+  const uint32_t t326 = LGX_LOP3(t44, t323, 0u, 0xc3);
+  const uint32_t t329 = LGX_LOP3(n4, t216, t326, 0x2e);
+  const uint32_t t330 = LGX_LOP3(t116, t149, 0u, 0xc0);
+  const uint32_t t333 = LGX_LOP3(t68, t137, t330, 0xca);
+  const uint32_t t336 = LGX_LOP3(t195, t209, t272, 0x80);
+  const uint32_t t337 = LGX_LOP3(s3_1, t44, t336, 0x50);
+  const uint32_t t339 = LGX_LOP3(t77, t195, t221, 0x07);
+  const uint32_t t340 = LGX_LOP3(t71, t181, t337, 0x54);
+  const uint32_t t341 = LGX_LOP3(t254, t279, 0u, 0x03);
+  const uint32_t t343 = LGX_LOP3(t339, t340, t341, 0x08);
+  const uint32_t t347 = LGX_LOP3(t44, t333, t343, 0x87);
+  const uint32_t t350 = LGX_LOP3(n5, t216, t347, 0x2e);
+  const uint32_t t353 = LGX_LOP3(t222, t223, t272, 0x80);
+  const uint32_t t356 = LGX_LOP3(t230, t255, t279, 0x01);
+  const uint32_t t357 = LGX_LOP3(t77, t353, t356, 0xa8);
+  const uint32_t t358 = LGX_LOP3(t68, t206, t357, 0x8a);
+  const uint32_t t361 = LGX_LOP3(t44, t358, 0u, 0xc3);
+  const uint32_t t364 = LGX_LOP3(n6, t216, t361, 0x2e);
+  o[0] = ~t241;
+  o[1] = ~t266;
+  o[2] = ~t290;
+  o[3] = ~t309;
+  o[4] = ~t329;
+  o[5] = ~t350;
+  o[6] = ~t364;
 }
 
 // lgx_collide_norest: 83 lop3 per 32-cell word (rest particles: no)
@@ -592,4 +602,78 @@ LGX_HD_INLINE void lgx_collide_norest(const uint32_t n[7], uint32_t s2, const ui
   o[6] = n6;
 }
 
-// stats: lgx_collide_rest {'aig_ands': 440, 'lop3': 261, 'checked': 6144}; lgx_collide_norest {'aig_ands': 140, 'lop3': 83, 'checked': 6144}
+// lgx_selectors: 44 lop3; r[0..17] are hashes 2..19 of the chain
+LGX_HD_INLINE void lgx_selectors(const uint32_t r[18], uint32_t s3[3], uint32_t s5[5]) {
+  const uint32_t r1 = r[0];
+  const uint32_t r2 = r[1];
+  const uint32_t r3 = r[2];
+  const uint32_t r4 = r[3];
+  const uint32_t r5 = r[4];
+  const uint32_t r6 = r[5];
+  const uint32_t r7 = r[6];
+  const uint32_t r8 = r[7];
+  const uint32_t r9 = r[8];
+  const uint32_t r10 = r[9];
+  const uint32_t r11 = r[10];
+  const uint32_t r12 = r[11];
+  const uint32_t r13 = r[12];
+  const uint32_t r14 = r[13];
+  const uint32_t r15 = r[14];
+  const uint32_t r16 = r[15];
+  const uint32_t r17 = r[16];
+  const uint32_t r18 = r[17];
+  const uint32_t t19 = LGX_LOP3(r5, r6, 0u, 0x03);
+  const uint32_t t23 = LGX_LOP3(r3, r4, t19, 0x7c);
+  const uint32_t t27 = LGX_LOP3(r1, r2, t23, 0xbc);
+  const uint32_t t28 = LGX_LOP3(r5, r6, 0u, 0x30);
+  const uint32_t t31 = LGX_LOP3(r3, r4, t28, 0x4f);
+  const uint32_t t34 = LGX_LOP3(r1, r2, t31, 0x8f);
+  const uint32_t t35 = LGX_LOP3(r5, r6, 0u, 0x0c);
+  const uint32_t t38 = LGX_LOP3(r3, r4, t35, 0x73);
+  const uint32_t t41 = LGX_LOP3(r1, r2, t38, 0xb3);
+  const uint32_t t43 = LGX_LOP3(r16, r17, r18, 0x01);
+  const uint32_t t44 = LGX_LOP3(r13, r14, 0u, 0x03);
+  const uint32_t t46 = LGX_LOP3(r13, r14, r15, 0xa8);
+  const uint32_t t48 = LGX_LOP3(r15, t43, t44, 0xb5);
+  const uint32_t t49 = LGX_LOP3(r10, r11, 0u, 0x03);
+  const uint32_t t51 = LGX_LOP3(r10, r11, r12, 0xa8);
+  const uint32_t t53 = LGX_LOP3(r12, t48, t49, 0xe5);
+  const uint32_t t54 = LGX_LOP3(r7, r8, 0u, 0x03);
+  const uint32_t t56 = LGX_LOP3(r7, r8, r9, 0xa8);
+  const uint32_t t58 = LGX_LOP3(r9, t53, t54, 0xe5);
+  const uint32_t t60 = LGX_LOP3(r16, r17, r18, 0x10);
+  const uint32_t t62 = LGX_LOP3(r13, r14, r15, 0x10);
+  const uint32_t t64 = LGX_LOP3(t46, t60, t62, 0x15);
+  const uint32_t t66 = LGX_LOP3(r10, r11, r12, 0x10);
+  const uint32_t t68 = LGX_LOP3(t51, t64, t66, 0x45);
+  const uint32_t t70 = LGX_LOP3(r7, r8, r9, 0x10);
+  const uint32_t t72 = LGX_LOP3(t56, t68, t70, 0x45);
+  const uint32_t t74 = LGX_LOP3(r16, r17, r18, 0x04);
+  const uint32_t t76 = LGX_LOP3(r13, r14, r15, 0x04);
+  const uint32_t t78 = LGX_LOP3(t46, t74, t76, 0x15);
+  const uint32_t t80 = LGX_LOP3(r10, r11, r12, 0x04);
+  const uint32_t t82 = LGX_LOP3(t51, t78, t80, 0x45);
+  const uint32_t t84 = LGX_LOP3(r7, r8, r9, 0x04);
+  const uint32_t t86 = LGX_LOP3(t56, t82, t84, 0x45);
+  const uint32_t t88 = LGX_LOP3(r16, r17, r18, 0x40);
+  const uint32_t t90 = LGX_LOP3(r13, r14, r15, 0x40);
+  const uint32_t t92 = LGX_LOP3(t46, t88, t90, 0x15);
+  const uint32_t t94 = LGX_LOP3(r10, r11, r12, 0x40);
+  const uint32_t t96 = LGX_LOP3(t51, t92, t94, 0x45);
+  const uint32_t t98 = LGX_LOP3(r7, r8, r9, 0x40);
+  const uint32_t t100 = LGX_LOP3(t56, t96, t98, 0x45);
+  const uint32_t t101 = LGX_LOP3(r16, r17, r18, 0x02);
+  const uint32_t t104 = LGX_LOP3(r15, t44, t101, 0x1f);
+  const uint32_t t107 = LGX_LOP3(r12, t49, t104, 0x2f);
+  const uint32_t t110 = LGX_LOP3(r9, t54, t107, 0x2f);
+  s3[0] = ~t27;
+  s3[1] = ~t34;
+  s3[2] = ~t41;
+  s5[0] = ~t58;
+  s5[1] = ~t72;
+  s5[2] = ~t86;
+  s5[3] = ~t100;
+  s5[4] = ~t110;
+}
+
+// stats: lgx_collide_rest {'aig_ands': 348, 'lop3': 161, 'checked': 6144}; lgx_collide_norest {'aig_ands': 140, 'lop3': 83, 'checked': 6144}; lgx_selectors {'aig_ands': 92, 'lop3': 44, 'checked': 4096}

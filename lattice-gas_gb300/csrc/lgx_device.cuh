@@ -36,7 +36,9 @@ __host__ __device__ __forceinline__ uint32_t mix(uint32_t x) {
 
 // Selectors for the collision of one word: a fair bit, a one-hot choice of
 // three and a one-hot choice of five by rejection sampling, 19 hashes in one
-// chain (src/gpu.rs:157-180).  A lane left unresolved keeps its state.
+// chain (src/gpu.rs:157-180).  A lane left unresolved keeps its state.  The
+// one-hot words come from the generated lgx_selectors (nested form, mapped to
+// lop3).
 struct Draws {
   uint32_t s2;
   uint32_t s3[3];
@@ -45,45 +47,15 @@ struct Draws {
 
 __host__ __device__ __forceinline__ Draws draws(uint32_t key) {
   Draws d;
-  uint32_t r = mix(key);
-  d.s2 = r;
-  uint32_t t0 = 0u, t1 = 0u, t2 = 0u, open = 0xffffffffu;
+  uint32_t r[18];
+  uint32_t x = mix(key);
+  d.s2 = x;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    r = mix(r);
-    const uint32_t a = r;
-    r = mix(r);
-    const uint32_t b = r;
-    t0 |= open & ~a & ~b;
-    t1 |= open & a & ~b;
-    t2 |= open & ~a & b;
-    open &= a & b;
+  for (int i = 0; i < 18; ++i) {
+    x = mix(x);
+    r[i] = x;
   }
-  d.s3[0] = t0;
-  d.s3[1] = t1;
-  d.s3[2] = t2;
-  uint32_t f0 = 0u, f1 = 0u, f2 = 0u, f3 = 0u, f4 = 0u, open5 = 0xffffffffu;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    r = mix(r);
-    const uint32_t a = r;
-    r = mix(r);
-    const uint32_t b = r;
-    r = mix(r);
-    const uint32_t c = r;
-    const uint32_t nc = open5 & ~c;
-    f0 |= nc & ~a & ~b;
-    f1 |= nc & a & ~b;
-    f2 |= nc & ~a & b;
-    f3 |= nc & a & b;
-    f4 |= open5 & c & ~a & ~b;
-    open5 &= c & (a | b);
-  }
-  d.s5[0] = f0;
-  d.s5[1] = f1;
-  d.s5[2] = f2;
-  d.s5[3] = f3;
-  d.s5[4] = f4;
+  lgx_selectors(r, d.s3, d.s5);
   return d;
 }
 

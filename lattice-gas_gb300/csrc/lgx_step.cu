@@ -21,7 +21,10 @@ namespace lgx {
 
 namespace {
 
-constexpr int kStepThreads = 256;
+#ifndef LGX_STEP_THREADS
+#define LGX_STEP_THREADS 256
+#endif
+constexpr int kStepThreads = LGX_STEP_THREADS;
 
 // Word to the left of `j` in the same row, with the row's periodic wrap: for
 // j == 0 the bit that enters is bit `lastbit` of the last word, placed at 31.

@@ -214,6 +214,167 @@ def build_rule_aig(rest: bool):
     return g, outs
 
 
+def build_rule_aig_folded(order=(2, 0, 1), reverse_terms=True):
+    """FHP-III rule through its particle-hole symmetry.
+
+    Complementing all seven bits maps class (m, px2, py2) onto (7 - m, -px2,
+    -py2) and reverses the ascending member order, so
+    class'[k] = ~class[size - 1 - k].  With z = [mass >= 4] (bit 2 of the
+    population count), the circuit evaluates only the fourteen classes of
+    mass 2 and 3 on m = n ^ z, with the selectors order-reversed where z is
+    set (s2 -> ~s2, s3[k] -> s3[2-k], s5[k] -> s5[4-k]), and complements the
+    picked member back.  Singleton classes map onto singleton classes, so a
+    lane with nothing to do keeps its state whatever z is.
+    """
+    g = AIG()
+    n = [g.input("n%d" % d) for d in range(7)]
+    s2 = g.input("s2")
+    s3 = [g.input("s3_%d" % k) for k in range(3)]
+    s5 = [g.input("s5_%d" % k) for k in range(5)]
+
+    def XOR(a, b):
+        return g.OR(g.AND(a, b ^ 1), g.AND(a ^ 1, b))
+
+    def MAJ(a, b, c):
+        return g.OR(g.AND(a, b), g.AND(c, g.OR(a, b)))
+
+    # bit 2 of popcount(n0..n6) by full adders
+    s_a = XOR(XOR(n[0], n[1]), n[2])
+    c_a = MAJ(n[0], n[1], n[2])
+    s_b = XOR(XOR(n[3], n[4]), n[5])
+    c_b = MAJ(n[3], n[4], n[5])
+    c_c = MAJ(s_a, s_b, n[6])
+    z = MAJ(c_a, c_b, c_c)
+
+    m = [XOR(n[d], z) for d in range(7)]
+    t2 = XOR(s2, z)
+    t3 = [g.MUX(z, s3[2 - k], s3[k]) for k in range(3)]
+    t5 = [g.MUX(z, s5[4 - k], s5[k]) for k in range(5)]
+
+    pair = []
+    for k in range(3):
+        lo, hi = m[k], m[k + 3]
+        pair.append({(0, 0): g.AND(lo ^ 1, hi ^ 1), (1, 0): g.AND(lo, hi ^ 1),
+                     (0, 1): g.AND(lo ^ 1, hi), (1, 1): g.AND(lo, hi)})
+
+    def minterm6(s):
+        ps = [pair[k][(s >> k & 1, s >> (k + 3) & 1)] for k in range(3)]
+        a, b, c = (ps[i] for i in order)
+        return g.AND(a, g.AND(b, c))
+
+    def member_set(states):
+        r0 = [s for s in states if not s >> REST & 1]
+        r1 = [s & 0x3F for s in states if s >> REST & 1]
+        a = g.OR_n([minterm6(s) for s in r0]) if r0 else 0
+        b = g.OR_n([minterm6(s) for s in r1]) if r1 else 0
+        return g.OR(g.AND(m[REST] ^ 1, a), g.AND(m[REST], b))
+
+    lower = [c for c in classes(True) if len(c) > 1 and invariants(c[0])[0] <= 3]
+    assert len(lower) == 14
+    ind = {tuple(c): member_set(c) for c in lower}
+    by_size = {2: [], 3: [], 5: []}
+    for c in lower:
+        by_size[len(c)].append(c)
+    any3 = g.OR_n(s3)
+    any5 = g.OR_n(s5)
+    acted = [g.OR_n([ind[tuple(c)] for c in by_size[2]]),
+             g.AND(g.OR_n([ind[tuple(c)] for c in by_size[3]]), any3),
+             g.AND(g.OR_n([ind[tuple(c)] for c in by_size[5]]), any5)]
+    keep = g.OR_n(acted) ^ 1
+    outs = []
+    for d in range(7):
+        A = g.OR_n([ind[tuple(c)] for c in by_size[2] if c[0] >> d & 1])
+        B = g.OR_n([ind[tuple(c)] for c in by_size[2] if c[1] >> d & 1])
+        terms = [g.MUX(t2, A, B)]
+        for size, sel in ((3, t3), (5, t5)):
+            for k in range(size):
+                X = g.OR_n([ind[tuple(c)] for c in by_size[size] if c[k] >> d & 1])
+                terms.append(g.AND(sel[k], X))
+        if reverse_terms:
+            terms = terms[::-1]
+        target = XOR(g.OR_n(terms), z)
+        outs.append(g.MUX(keep, n[d], target))
+    return g, outs
+
+
+def build_selector_aig():
+    """One-hot selectors from the hash chain (src/gpu.rs:157-180) in nested form.
+
+    The reference accumulates s3[j] |= open & f_j(a, b) round by round with
+    open &= a & b (and s5 likewise with open5 &= c & (a | b)).  The rounds are
+    nested, so the same selectors are
+        s3[j] = f_j(r0) | g(r0) & (f_j(r1) | g(r1) & f_j(r2))
+    with g the continue condition of a round; that form maps onto fewer
+    three-input tables.  Inputs r1..r18 are the 2nd..19th hashes of the chain.
+    """
+    g = AIG()
+    r = [None] + [g.input("r%d" % i) for i in range(1, 19)]
+    f3 = [lambda a, b: g.AND(a ^ 1, b ^ 1), lambda a, b: g.AND(a, b ^ 1),
+          lambda a, b: g.AND(a ^ 1, b)]
+    c3 = lambda a, b: g.AND(a, b)
+    rounds3 = [(r[1], r[2]), (r[3], r[4]), (r[5], r[6])]
+    outs = []
+    for j in range(3):
+        acc = f3[j](*rounds3[2])
+        for a, b in (rounds3[1], rounds3[0]):
+            acc = g.OR(f3[j](a, b), g.AND(c3(a, b), acc))
+        outs.append(acc)
+    f5 = [lambda a, b, c: g.AND_n([a ^ 1, b ^ 1, c ^ 1]), lambda a, b, c: g.AND_n([a, b ^ 1, c ^ 1]),
+          lambda a, b, c: g.AND_n([a ^ 1, b, c ^ 1]), lambda a, b, c: g.AND_n([a, b, c ^ 1]),
+          lambda a, b, c: g.AND_n([a ^ 1, b ^ 1, c])]
+    c5 = lambda a, b, c: g.AND(c, g.OR(a, b))
+    rounds5 = [(r[7], r[8], r[9]), (r[10], r[11], r[12]), (r[13], r[14], r[15]),
+               (r[16], r[17], r[18])]
+    for j in range(5):
+        acc = f5[j](*rounds5[3])
+        for rd in (rounds5[2], rounds5[1], rounds5[0]):
+            acc = g.OR(f5[j](*rd), g.AND(c5(*rd), acc))
+        outs.append(acc)
+    return g, outs
+
+
+def selector_reference(rs):
+    """The reference's accumulate-with-mask form, for verification."""
+    M = (1 << 64) - 1
+    s3 = [0, 0, 0]
+    open_ = M
+    for k in range(3):
+        a, b = rs[1 + 2 * k], rs[2 + 2 * k]
+        s3[0] |= open_ & ~a & ~b & M
+        s3[1] |= open_ & a & ~b & M
+        s3[2] |= open_ & ~a & b & M
+        open_ &= a & b
+    s5 = [0] * 5
+    open5 = M
+    for k in range(4):
+        a, b, c = rs[7 + 3 * k], rs[8 + 3 * k], rs[9 + 3 * k]
+        s5[0] |= open5 & ~a & ~b & ~c & M
+        s5[1] |= open5 & a & ~b & ~c & M
+        s5[2] |= open5 & ~a & b & ~c & M
+        s5[3] |= open5 & a & b & ~c & M
+        s5[4] |= open5 & ~a & ~b & c & M
+        open5 &= c & (a | b)
+    return s3 + s5
+
+
+def verify_selectors(g, luts, outs):
+    """Exhaustive per lane: all 2^12 bit patterns of the s5 rounds, each lane
+    also carrying one of the 2^6 patterns of the s3 rounds."""
+    for base in range(0, 4096, 64):
+        rs = [None] + [0] * 18
+        for lane in range(64):
+            i = base + lane
+            for b in range(6):
+                if (i % 64) >> b & 1:
+                    rs[1 + b] |= 1 << lane
+            for b in range(12):
+                if i >> b & 1:
+                    rs[7 + b] |= 1 << lane
+        if eval_luts(g, luts, outs, rs[1:]) != selector_reference(rs):
+            return False
+    return True
+
+
 # ---------------------------------------------------------------------------
 # Cut-based mapping onto three-input LUTs (one lop3 each).
 # ---------------------------------------------------------------------------
@@ -445,6 +606,28 @@ def emit(rest, g, luts, outs, fname):
     return "\n".join(lines)
 
 
+def emit_selectors(g, luts, outs):
+    names = {nid: g.names[nid] for nid in g.inputs}
+    lines = ["// lgx_selectors: %d lop3; r[0..17] are hashes 2..19 of the chain" % len(luts),
+             "LGX_HD_INLINE void lgx_selectors(const uint32_t r[18], uint32_t s3[3], uint32_t s5[5]) {"]
+    used = set()
+    for _, leaves, _ in luts:
+        used.update(leaves)
+    for nid in g.inputs:
+        if nid in used:
+            lines.append("  const uint32_t %s = r[%d];" % (names[nid], int(names[nid][1:]) - 1))
+    for v, leaves, table in luts:
+        names[v] = "t%d" % v
+        args = [names[l] for l in leaves] + ["0u"] * (3 - len(leaves))
+        lines.append("  const uint32_t t%d = LGX_LOP3(%s, %s, %s, 0x%02x);"
+                     % (v, args[0], args[1], args[2], table))
+    dst = ["s3[0]", "s3[1]", "s3[2]", "s5[0]", "s5[1]", "s5[2]", "s5[3]", "s5[4]"]
+    for d, o in zip(dst, outs):
+        lines.append("  %s = %s%s;" % (d, "~" if o & 1 else "", names[o >> 1]))
+    lines.append("}")
+    return "\n".join(lines)
+
+
 HEADER = """// Generated by lattice-gas_gb300/gen/collide_gen.py -- do not edit.
 //
 // The FHP collision rule as three-input lookup tables, one lop3.b32 each.
@@ -500,7 +683,9 @@ def generate(stats=False):
     bodies = []
     report = {}
     for rest, fname in ((True, "lgx_collide_rest"), (False, "lgx_collide_norest")):
-        g, outs = build_rule_aig(rest)
+        # Without rest particles mass 3 is its own complement, so the folded
+        # form would not halve anything; that rule is built directly.
+        g, outs = build_rule_aig_folded() if rest else build_rule_aig(rest)
         luts = map_lut3(g, outs)
         total, bad = verify(rest, g, luts, outs)
         if bad:
@@ -511,6 +696,15 @@ def generate(stats=False):
         for _, _, t in luts:
             tables.add(t)
         bodies.append(emit(rest, g, luts, outs, fname))
+    gs, souts = build_selector_aig()
+    sluts = map_lut3(gs, souts)
+    if not verify_selectors(gs, sluts, souts):
+        raise SystemExit("generated selectors disagree with the reference's rejection sampling")
+    report["lgx_selectors"] = dict(aig_ands=sum(1 for f in gs.fanins if f is not None),
+                                   lop3=len(sluts), checked=64 * 64)
+    for _, _, t in sluts:
+        tables.add(t)
+    bodies.append(emit_selectors(gs, sluts, souts))
     parts.append(HEADER)
     parts.append(lop3_device_helpers(tables))
     parts.append("#if defined(__CUDA_ARCH__)")

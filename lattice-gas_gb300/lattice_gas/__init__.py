@@ -86,6 +86,7 @@ def lib():
         _sig(L, "lgx_timing_elapsed", vp, C.c_int, C.c_int, C.POINTER(C.c_float))
         _sig(L, "lgx_verify_circuit", C.c_int, u32p, sz)
         _sig(L, "lgx_select_device", C.c_int)
+        _sig(L, "lgx_probe_int_rate", C.c_int, C.POINTER(C.c_double))
         _sig(L, "lgx_host_alloc", sz, C.POINTER(vp))
         _sig(L, "lgx_host_free", vp)
         _sig(L, "lgx_equilibrium_thresholds", C.c_float, C.c_float, C.c_float, C.c_int, u32p)
@@ -274,6 +275,13 @@ def shear_wave(w, h, density, ux_row, rest, rng_seed):
     _check(lib().lgx_cells_shear_wave(_p(cells, C.c_uint8), w, h, float(density),
                                       _p(u, C.c_float), int(bool(rest)), _u64(rng_seed)))
     return cells
+
+
+def probe_int_rate(op: int) -> float:
+    """Measured integer throughput (instructions/s) for op 0 lop3, 1 imad, 2 shf, 3 add."""
+    v = C.c_double()
+    _check(lib().lgx_probe_int_rate(int(op), C.byref(v)))
+    return float(v.value)
 
 
 def select_device(ordinal: int):
