@@ -74,6 +74,15 @@ int lgx_advance(lgx_lattice *lat, uint64_t n);
  * lattice into the attached field every sample_every steps and after the last
  * one; sample_every == 0 never samples. */
 int lgx_advance_sampling(lgx_lattice *lat, uint64_t n, uint64_t sample_every, float alpha);
+/* How steps are launched.  AUTO (default) and SINGLE launch one kernel per
+ * step, as the reference dispatches one lgca_step per step, with programmatic
+ * dependent launch so each step's state-independent draws overlap the
+ * previous step's tail.  WAVE runs up to 128 steps per cooperative launch of a
+ * persistent kernel (each block owns a fixed range of words and waits, with a
+ * bounded spin, only for the blocks owning the rows next to its own).
+ * Results are identical in every mode. */
+enum { LGX_STEP_AUTO = 0, LGX_STEP_SINGLE = 1, LGX_STEP_WAVE = 2 };
+int lgx_set_step_mode(lgx_lattice *lat, int mode);
 /* GpuLattice::sample_field (src/gpu.rs:710-721). */
 int lgx_sample_field(lgx_lattice *lat, float alpha);
 /* GpuLattice::read_field (src/gpu.rs:725-736): n_blocks must be bw*bh. */

@@ -45,15 +45,27 @@ struct Draws {
   uint32_t s5[5];
 };
 
+// The chain r_{k+1} = mix(r_k) for k = 0..18, r_{-1} = key.  The hash both
+// begins and ends with x ^= x >> 16, and that map is an involution (the high
+// half is unchanged and the low half is xored with it twice), so in the
+// conjugated variable u_k = r_k ^ (r_k >> 16) the chain is
+//     u_{k+1} = M2(S15(M1(u_k))),   M1 = *0x7feb352d, S15 = ^(>>15), M2 = *0x846ca68b
+// and each output is recovered as r_k = u_k ^ (u_k >> 16).  Same values, two
+// fewer logic instructions per hash.
 __host__ __device__ __forceinline__ Draws draws(uint32_t key) {
   Draws d;
   uint32_t r[18];
-  uint32_t x = mix(key);
-  d.s2 = x;
+  uint32_t u = key ^ (key >> 16);
+  u *= 0x7feb352du;
+  u ^= u >> 15;
+  u *= 0x846ca68bu;
+  d.s2 = u ^ (u >> 16);
 #pragma unroll
   for (int i = 0; i < 18; ++i) {
-    x = mix(x);
-    r[i] = x;
+    u *= 0x7feb352du;
+    u ^= u >> 15;
+    u *= 0x846ca68bu;
+    r[i] = u ^ (u >> 16);
   }
   lgx_selectors(r, d.s3, d.s5);
   return d;

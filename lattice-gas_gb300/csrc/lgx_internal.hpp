@@ -36,6 +36,22 @@ struct StepArgs {
   uint64_t steps;  // steps taken before this one
 };
 
+// `nsteps` steps of one lattice in one cooperative launch.  The state after
+// local step s lives in planes[s & 1]; done[b] is the last step CTA b has
+// published (zeroed before the launch); error is set if a wait times out.
+struct WaveArgs {
+  uint32_t* planes[2];
+  const uint32_t* solid;
+  const uint32_t* anysolid;
+  const uint32_t* inlet;  // [nsteps][h][iw][7]; null when iw == 0
+  Dims dm;
+  uint64_t seed;
+  uint64_t steps;  // steps taken before the first of these
+  uint32_t nsteps;
+  uint32_t* done;
+  uint32_t* error;
+};
+
 // Inlet Bernoulli words for `nsteps` consecutive steps starting at `steps`,
 // written to out[s][y][jw][d].
 struct InletArgs {
@@ -63,6 +79,10 @@ struct SampleArgs {
 
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st);
 cudaError_t launch_inlet(const InletArgs& s, cudaStream_t st);
+// Co-resident CTAs for the persistent kernel on the current device (at most
+// one per 32-word chunk).
+cudaError_t wave_grid(bool rest, uint32_t total, uint32_t* grid);
+cudaError_t launch_wave(const WaveArgs& w, bool rest, uint32_t grid, cudaStream_t st);
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
                          cudaStream_t st);

@@ -38,8 +38,9 @@ Dims make_dims(uint32_t w, uint32_t h, uint32_t inlet_cols) {
   return d;
 }
 
-// Steps whose inlet draws are made in one launch.
-constexpr uint32_t kInletChunk = 64;
+// Steps whose inlet draws are made in one launch, and the most steps one
+// persistent launch runs.
+constexpr uint32_t kInletChunk = 128;
 
 }  // namespace lgx
 
@@ -70,6 +71,11 @@ struct lgx_lattice {
   int32_t* sums = nullptr;     // mass | px2 | py2 | nsolid
   cudaEvent_t ev[8] = {};
   uint64_t launches = 0;     // kernels this handle has launched
+  // persistent multi-step kernel
+  int step_mode = LGX_STEP_AUTO;
+  uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
+  uint32_t* done = nullptr;  // [wave_grid] published step per CTA
+  uint32_t* error = nullptr; // timeout flag
 };
 
 namespace {
@@ -107,6 +113,8 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->inlet);
   cudaFree(lat->field);
   cudaFree(lat->sums);
+  cudaFree(lat->done);
+  cudaFree(lat->error);
   for (auto& e : lat->ev)
     if (e) cudaEventDestroy(e);
   if (lat->stream) cudaStreamDestroy(lat->stream);
@@ -169,34 +177,96 @@ int launch_sample(lgx_lattice* lat, float alpha) {
   return LGX_OK;
 }
 
+int enqueue_wave(lgx_lattice* lat, uint32_t k) {
+  if (lat->wave_grid == 0) {
+    uint32_t grid = 0;
+    LGX_CUDA(lgx::wave_grid(lat->rest, lat->dm.total, &grid));
+    LGX_CUDA(cudaMalloc(&lat->done, grid * sizeof(uint32_t)));
+    LGX_CUDA(cudaMalloc(&lat->error, sizeof(uint32_t)));
+    LGX_CUDA(cudaMemsetAsync(lat->error, 0, sizeof(uint32_t), lat->stream));
+    lat->wave_grid = grid;
+  }
+  lgx::WaveArgs wa;
+  wa.planes[0] = lat->planes[lat->cur];
+  wa.planes[1] = lat->planes[lat->cur ^ 1];
+  wa.solid = lat->solid;
+  wa.anysolid = lat->anysolid;
+  wa.inlet = lat->dm.iw ? lat->inlet + (size_t)(lat->steps - lat->inlet_first) * lat->dm.h *
+                                           lat->dm.iw * 7
+                        : nullptr;
+  wa.dm = lat->dm;
+  wa.seed = lat->seed;
+  wa.steps = lat->steps;
+  wa.nsteps = k;
+  wa.done = lat->done;
+  wa.error = lat->error;
+  LGX_CUDA(cudaMemsetAsync(lat->done, 0, lat->wave_grid * sizeof(uint32_t), lat->stream));
+  LGX_CUDA(lgx::launch_wave(wa, lat->rest, lat->wave_grid, lat->stream));
+  lat->launches += 1;
+  lat->cur ^= (int)(k & 1u);
+  lat->steps += k;
+  return LGX_OK;
+}
+
+int enqueue_single(lgx_lattice* lat) {
+  lgx::StepArgs sa;
+  sa.a = lat->planes[lat->cur];
+  sa.b = lat->planes[lat->cur ^ 1];
+  sa.solid = lat->solid;
+  sa.anysolid = lat->anysolid;
+  sa.inlet = lat->dm.iw ? lat->inlet + (size_t)(lat->steps - lat->inlet_first) * lat->dm.h *
+                                           lat->dm.iw * 7
+                        : nullptr;
+  sa.dm = lat->dm;
+  sa.seed = lat->seed;
+  sa.steps = lat->steps;
+  LGX_CUDA(lgx::launch_step(sa, lat->rest, lat->stream));
+  lat->launches += 1;
+  lat->cur ^= 1;
+  lat->steps += 1;
+  return LGX_OK;
+}
+
+// Enqueue n steps, sampling every `every` steps and after the last
+// (src/gpu.rs:668-706).  In the persistent mode one launch runs up to the
+// next sampling point, the end of the inlet chunk in hand, or kInletChunk.
 int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
   uint64_t left = n, since = 0;
+  const bool wave = lat->step_mode == LGX_STEP_WAVE;
   while (left > 0) {
     int rc = ensure_inlet(lat, left);
     if (rc) return rc;
-    lgx::StepArgs sa;
-    sa.a = lat->planes[lat->cur];
-    sa.b = lat->planes[lat->cur ^ 1];
-    sa.solid = lat->solid;
-    sa.anysolid = lat->anysolid;
-    sa.inlet = lat->dm.iw
-                   ? lat->inlet + (size_t)(lat->steps - lat->inlet_first) * lat->dm.h *
-                                      lat->dm.iw * 7
-                   : nullptr;
-    sa.dm = lat->dm;
-    sa.seed = lat->seed;
-    sa.steps = lat->steps;
-    LGX_CUDA(lgx::launch_step(sa, lat->rest, lat->stream));
-    lat->launches += 1;
-    lat->cur ^= 1;
-    lat->steps += 1;
-    left -= 1;
-    since += 1;
+    uint64_t k = 1;
+    if (wave) {
+      k = std::min<uint64_t>(left, lgx::kInletChunk);
+      if (every > 0) k = std::min<uint64_t>(k, every - since);
+      if (lat->dm.iw) k = std::min<uint64_t>(k, lat->inlet_first + lat->inlet_valid - lat->steps);
+      rc = enqueue_wave(lat, (uint32_t)k);
+    } else {
+      rc = enqueue_single(lat);
+    }
+    if (rc) return rc;
+    left -= k;
+    since += k;
     if (every > 0 && (since >= every || left == 0)) {
       since = 0;
       rc = launch_sample(lat, alpha);
       if (rc) return rc;
     }
+  }
+  return LGX_OK;
+}
+
+// After a sync: did a persistent launch time out waiting on a peer?
+int check_wave_error(lgx_lattice* lat) {
+  if (!lat->error) return LGX_OK;
+  uint32_t v = 0;
+  LGX_CUDA(cudaMemcpy(&v, lat->error, sizeof(v), cudaMemcpyDeviceToHost));
+  if (v) {
+    cudaMemset(lat->error, 0, sizeof(uint32_t));
+    lgx::set_error("persistent step kernel timed out waiting for a neighbouring block; "
+                   "the lattice state is undefined");
+    return LGX_ERR_CUDA;
   }
   return LGX_OK;
 }
@@ -364,6 +434,15 @@ int lgx_advance_sampling(lgx_lattice* lat, uint64_t n, uint64_t every, float alp
   rc = enqueue_steps(lat, n, every, alpha);
   if (rc) return rc;
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return check_wave_error(lat);
+}
+
+int lgx_set_step_mode(lgx_lattice* lat, int mode) {
+  if (!lat || (mode != LGX_STEP_AUTO && mode != LGX_STEP_SINGLE && mode != LGX_STEP_WAVE)) {
+    lgx::set_error("lgx_set_step_mode: bad handle or mode");
+    return LGX_ERR_ARG;
+  }
+  lat->step_mode = mode;
   return LGX_OK;
 }
 

@@ -19,8 +19,9 @@ DY = (0, 1, 1, 0, -1, -1)
 THREADS = max(1, min(16, os.cpu_count() or 1))
 
 
-def pair(LG, O, w, h, rest, seed, cells, inlet=None, block=None):
+def pair(LG, O, w, h, rest, seed, cells, inlet=None, block=None, mode=0):
     g = LG.GpuLattice(w, h, rest, seed)
+    g.set_step_mode(mode)
     o = O.BitplaneLattice(w, h, rest, seed, THREADS)
     if inlet:
         g.set_inlet(*inlet)
@@ -252,6 +253,10 @@ def test_periodic_box_bit_exact(LG, O):
     assert (int(mass.sum()), int(px.sum()), int(py.sum())) == before
 
 
+MODES = [1, 2]   # one launch per step (programmatic dependent launch), persistent waves
+
+
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("w,h,inlet,rest", [
     (100, 34, 40, True),    # ragged width, two-word inlet
     (33, 20, 8, True),      # one valid bit in the last word
@@ -260,13 +265,13 @@ def test_periodic_box_bit_exact(LG, O):
     (129, 40, 70, False),   # no rest, three-word inlet, ragged
     (1000, 64, 8, True),    # many warps per row, rows straddling warps
 ])
-def test_small_lattices_bit_exact(LG, O, w, h, inlet, rest):
+def test_small_lattices_bit_exact(LG, O, w, h, inlet, rest, mode):
     cells = np.zeros(w * h, np.uint8)
     LG.add_circle(cells, w, h, w / 2.0, h * 0.43, min(w, h) / 5.0)
     LG.init_equilibrium(cells, 0.3, 0.2, 0.0, rest, 1234 + w)
     g, o = pair(LG, O, w, h, rest, 0xDEADBEEF12345678 + w, cells,
-                inlet=(inlet, 0.3, (0.2, 0.0), rest) if inlet else None, block=8)
-    for chunk in (1, 7, 64, 100):   # crosses inlet draw chunks
+                inlet=(inlet, 0.3, (0.2, 0.0), rest) if inlet else None, block=8, mode=mode)
+    for chunk in (1, 7, 64, 100, 300):   # crosses inlet draw chunks and launch lengths
         g.advance_sampling(chunk, 10, 0.3)
         o.advance_sampling(chunk, 10, 0.3)
         assert_same(g, o)
@@ -286,12 +291,13 @@ def test_restart_resets_the_stream(LG, O):
     assert_same(g, o)
 
 
-def test_wake_run_reduced_bit_exact(LG, O):
+@pytest.mark.parametrize("mode", MODES)
+def test_wake_run_reduced_bit_exact(LG, O, mode):
     """The wake run's geometry (plate, inflow, walls) at 512 x 288, 300 steps."""
     from lattice_gas import workloads as W
     wl = W.wake_run(w=512, h=288, steps=300)
     g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells,
-                inlet=(wl.inlet_cols, wl.density, wl.inflow, True), block=wl.block)
+                inlet=(wl.inlet_cols, wl.density, wl.inflow, True), block=wl.block, mode=mode)
     g.advance_sampling(300, wl.sample_every, wl.alpha)
     o.advance_sampling(300, wl.sample_every, wl.alpha)
     assert_same(g, o)
@@ -327,6 +333,28 @@ def test_transport_sweep_members_bit_exact(LG, O):
         g.advance_sampling(200, wl.sample_every, wl.alpha)
         o.advance_sampling(200, wl.sample_every, wl.alpha)
         assert_same(g, o)
+
+
+def test_step_modes_agree_on_the_full_wake_run(LG):
+    """4096 x 2304, 1000 steps with sampling: persistent launches and one launch
+    per step give the same lattice, field and block sums."""
+    from lattice_gas import workloads as W
+    wl = W.wake_run()
+    out = []
+    for mode in (1, 2):
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.set_step_mode(mode)
+        g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)
+        g.attach_field(wl.block, wl.block)
+        g.load(wl.cells)
+        g.advance_sampling(1000, wl.sample_every, wl.alpha)
+        f = g.read_field()
+        out.append((g.store(), g.read_block_sums(), f.ux.copy(), g.steps))
+        g.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(out[0][2], out[1][2]) and out[0][3] == out[1][3] == 1000
 
 
 def test_full_size_periodic_conservation(LG, O):
