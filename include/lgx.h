@@ -119,6 +119,27 @@ int lgx_verify_circuit(int rest_particles, uint32_t *out, size_t n);
  * 2 = funnel shift, 3 = add, 4 = high-half multiply.  The denominators of the step's integer roofline. */
 int lgx_probe_int_rate(int op, double *ops_per_s);
 
+/* ---- batches: many lattices advanced together ---------------------------- */
+
+/* A batch borrows lattices made with lgx_create (planes, fields, inlets) and
+ * advances them together: one kernel launch steps every lattice, and a
+ * sampling interval's launches are one CUDA graph, captured on first use and
+ * replayed.  The reference runs independent lattices one per host thread and
+ * Metal queue (src/transport.rs:299-313).  While a lattice belongs to a live
+ * batch, advance it only through the batch. */
+typedef struct lgx_batch lgx_batch;
+int lgx_batch_create(lgx_lattice *const *lats, size_t n, lgx_batch **out);
+int lgx_batch_destroy(lgx_batch *b);
+/* Every lattice advances n steps, sampling into its own attached field every
+ * sample_every steps and after the last (as lgx_advance_sampling). */
+int lgx_batch_advance_sampling(lgx_batch *b, uint64_t n, uint64_t sample_every, float alpha);
+int lgx_batch_advance(lgx_batch *b, uint64_t n);
+/* Instrumentation: kernels and graph launches issued so far; device-time
+ * events on the batch's stream (as lgx_timing_mark / lgx_timing_elapsed). */
+int lgx_batch_launch_count(lgx_batch *b, uint64_t *kernels, uint64_t *graphs);
+int lgx_batch_timing_mark(lgx_batch *b, int slot);
+int lgx_batch_timing_elapsed(lgx_batch *b, int a, int c, float *ms);
+
 /* ---- host-side lattice setup (src/lattice.rs, src/hex.rs) ---------------- */
 
 /* Equilibrium::new(..).thresholds() (src/lattice.rs:72-92): 24-bit thresholds,

@@ -1,0 +1,147 @@
+// lgx_batch.cu -- many lattices of uneven sizes advanced together.
+//
+// The reference advances one lattice per command buffer and, when it wants
+// several (transport::measure's two measurements), one per host thread and
+// Metal queue (src/transport.rs:299-313).  Small lattices cannot fill a GPU,
+// so here one launch steps every lattice of a batch: blocks of 256 threads
+// are laid over the concatenated word ranges (each lattice padded to whole
+// blocks), a per-block table names the lattice, and each block runs the
+// same per-word update as the single-lattice kernel.  The step kernels are
+// chained with programmatic dependent launch, a batched coarse-graining
+// kernel samples every lattice's field, and a sampling interval's launches
+// are captured once into a CUDA graph that is replayed for every interval:
+// a device-side counter of batch steps (advanced by the graph's last node)
+// gives each replay its step numbers, ping-pong parity and seeds.
+#include <algorithm>
+
+#include "lgx_batch.hpp"
+#include "lgx_device.cuh"
+#include "lgx_step_impl.cuh"
+
+namespace lgx {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <bool REST>
+__device__ __forceinline__ void batch_word(const LatDesc& d, uint64_t local, uint32_t k,
+                                           uint32_t g, bool live, const Draws& s) {
+  const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
+  const uint32_t* src = par ? d.planes[1] : d.planes[0];
+  uint32_t* dst = par ? d.planes[0] : d.planes[1];
+  const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)k * d.dm.h * d.dm.iw * 7u : nullptr;
+  step_word<REST, false>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, g, live);
+}
+
+// One step of every lattice of one rule in the batch (blocks first_block ..
+// first_block + gridDim.x - 1 of the block table).  `k` is the step's index
+// within the captured interval; the batch step is *base + k.
+template <bool REST>
+__global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepArgs p) {
+  const uint32_t blk = p.first_block + blockIdx.x;
+  const LatDesc& d = p.descs[p.block_lat[blk]];
+  uint32_t g = p.block_word0[blk] + threadIdx.x;
+  const bool live = g < d.dm.total;
+  if (!live) g = d.dm.total - 1u;
+  const uint64_t local = *p.base + p.k;
+  const Draws s = draws(g ^ step_seed32(d.seed, d.steps0 + local));
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  batch_word<REST>(d, local, p.k, g, live, s);
+}
+
+// Inlet draws for steps base .. base + nsteps - 1 of every lattice with an
+// inlet: one thread per (lattice, step, row, inlet word).
+__global__ void __launch_bounds__(128) lgx_batch_inlet_kernel(BatchInletArgs p) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= p.total_items) return;
+  // lattice by binary search over the item prefix
+  uint32_t lo = 0, hi = p.nlat;
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (p.item0[mid] <= idx) lo = mid; else hi = mid;
+  }
+  const LatDesc& d = p.descs[lo];
+  const uint32_t per_step = d.dm.h * d.dm.iw;
+  const uint32_t rel = idx - p.item0[lo];
+  const uint32_t s = rel / per_step;
+  const uint32_t rem = rel - s * per_step;
+  const uint32_t y = rem / d.dm.iw;
+  const uint32_t jw = rem - y * d.dm.iw;
+  const uint32_t word = y * d.dm.wpr + jw;
+  const uint64_t local = *p.base + s;
+  uint32_t r = mix(word ^ step_seed32(d.seed, d.steps0 + local) ^ kGolden32);
+  uint32_t* out = d.inlet + (size_t)rel * 7u;
+#pragma unroll 1
+  for (int k = 0; k < 7; ++k) out[k] = bernoulli(d.thresh[k], r);
+}
+
+// Coarse-graining of every lattice with a field: one warp per field block,
+// the lattice found by binary search over the block prefix.  The state read
+// is the one after batch step *base + k_after.
+__global__ void __launch_bounds__(256) lgx_batch_sample_kernel(BatchSampleArgs p) {
+  const uint32_t task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (task >= p.total_blocks) return;
+  uint32_t lo = 0, hi = p.nlat;
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (p.blk0[mid] <= task) lo = mid; else hi = mid;
+  }
+  const LatDesc& d = p.descs[lo];
+  const uint64_t local = *p.base + p.k_after;
+  const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
+  SampleArgs sa;
+  sa.a = par ? d.planes[1] : d.planes[0];
+  sa.solid = d.solid;
+  sa.dm = d.dm;
+  sa.bx = d.bx;
+  sa.by = d.by;
+  sa.bw = d.bw;
+  sa.bh = d.bh;
+  sa.alpha = d.alpha;
+  const uint32_t nb = d.bw * d.bh;
+  sa.ux = d.field;
+  sa.uy = d.field + nb;
+  sa.rho = d.field + 2 * nb;
+  sa.sol = d.field + 3 * nb;
+  sa.sums = d.sums;
+  sample_block(sa, task - p.blk0[lo]);
+}
+
+__global__ void lgx_batch_base_kernel(uint64_t* base, uint32_t n) { *base += n; }
+
+}  // namespace
+
+cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, bool rest,
+                              cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (rest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<true>, a);
+  return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<false>, a);
+}
+
+cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st) {
+  if (a.total_items == 0) return cudaSuccess;
+  lgx_batch_inlet_kernel<<<(a.total_items + 127) / 128, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st) {
+  if (a.total_blocks == 0) return cudaSuccess;
+  lgx_batch_sample_kernel<<<(a.total_blocks + 7) / 8, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_base(uint64_t* base, uint32_t n, cudaStream_t st) {
+  lgx_batch_base_kernel<<<1, 1, 0, st>>>(base, n);
+  return cudaGetLastError();
+}
+
+}  // namespace lgx

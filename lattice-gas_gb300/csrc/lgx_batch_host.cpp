@@ -1,0 +1,335 @@
+// lgx_batch_host.cpp -- the batch handle: many lattices, one launch per step.
+//
+// A batch borrows lattices created with lgx_create (their planes, fields and
+// inlet settings) and advances all of them together.  For each sampling
+// interval it replays a CUDA graph captured on first use:
+//   [batched inlet draws] -> L x batched step (programmatic dependent launch)
+//   -> [batched coarse-graining] -> batch step counter += L
+// The graph holds only device pointers to the descriptor table and the step
+// counter, so one capture serves every interval of the same length.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lgx.h"
+#include "lgx_batch.hpp"
+#include "lgx_handle.hpp"
+
+namespace {
+
+struct GraphEntry {
+  uint32_t len;
+  bool sample;
+  cudaGraphExec_t exec;
+};
+
+int cuda_fail(cudaError_t e, const char* what) {
+  lgx::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return LGX_ERR_CUDA;
+}
+
+#define LGX_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+}  // namespace
+
+struct lgx_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<lgx_lattice*> lats;
+  std::vector<lgx::LatDesc> descs;
+  lgx::LatDesc* d_descs = nullptr;
+  uint32_t* d_block_lat = nullptr;
+  uint32_t* d_block_word0 = nullptr;
+  uint32_t* d_item0 = nullptr;
+  uint32_t* d_blk0 = nullptr;
+  uint64_t* d_base = nullptr;
+  uint32_t nblocks = 0;
+  uint32_t rest_blocks = 0;     // leading block-table entries of rest-particle lattices
+  uint32_t items_per_step = 0;  // inlet draw items of one step, all lattices
+  uint32_t field_blocks = 0;
+  std::vector<uint32_t*> inlet_bufs;
+  std::vector<GraphEntry> graphs;
+  uint64_t launches = 0;
+  uint64_t graph_launches = 0;
+  cudaEvent_t ev[8] = {};
+};
+
+namespace {
+
+void free_batch(lgx_batch* b) {
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto* p : b->inlet_bufs) cudaFree(p);
+  cudaFree(b->d_descs);
+  cudaFree(b->d_block_lat);
+  cudaFree(b->d_block_word0);
+  cudaFree(b->d_item0);
+  cudaFree(b->d_blk0);
+  cudaFree(b->d_base);
+  for (auto& ev : b->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+// Snapshot the member lattices into descriptors (steps, parity, field).
+int setup_descs(lgx_batch* b, float alpha) {
+  const size_t n = b->lats.size();
+  b->descs.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    lgx_lattice* l = b->lats[i];
+    lgx::LatDesc& d = b->descs[i];
+    d.planes[0] = l->planes[l->cur];
+    d.planes[1] = l->planes[l->cur ^ 1];
+    d.solid = l->solid;
+    d.anysolid = l->anysolid;
+    d.inlet = b->inlet_bufs[i];
+    d.dm = l->dm;
+    d.seed = l->seed;
+    d.steps0 = l->steps;
+    d.cur0 = 0;
+    d.rest = l->rest ? 1u : 0u;
+    for (int k = 0; k < 7; ++k) d.thresh[k] = l->thresh[k];
+    d.field = l->has_field ? l->field : nullptr;
+    d.sums = l->has_field ? l->sums : nullptr;
+    d.bx = l->bx;
+    d.by = l->by;
+    d.bw = l->has_field ? l->bw : 0;
+    d.bh = l->has_field ? l->bh : 0;
+    d.alpha = alpha;
+  }
+  LGX_CUDA(cudaMemcpyAsync(b->d_descs, b->descs.data(), n * sizeof(lgx::LatDesc),
+                           cudaMemcpyHostToDevice, b->stream));
+  LGX_CUDA(cudaMemsetAsync(b->d_base, 0, sizeof(uint64_t), b->stream));
+  return LGX_OK;
+}
+
+int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
+  cudaGraph_t graph = nullptr;
+  LGX_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  if (b->items_per_step) {
+    lgx::BatchInletArgs ia{b->d_descs, b->d_item0, (uint32_t)b->lats.size(),
+                           b->items_per_step * len, b->d_base};
+    // the draws of one lattice are laid out step-major in its own buffer, so
+    // the item prefix scales with the interval length
+    e = lgx::launch_batch_inlet(ia, b->stream);
+  }
+  for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
+    // rest-particle lattices' blocks first, then the six-direction ones
+    if (b->rest_blocks) {
+      lgx::BatchStepArgs sa{b->d_descs, b->d_block_lat, b->d_block_word0, b->d_base, k, 0};
+      e = lgx::launch_batch_step(sa, b->rest_blocks, true, b->stream);
+    }
+    if (e == cudaSuccess && b->nblocks > b->rest_blocks) {
+      lgx::BatchStepArgs sa{b->d_descs, b->d_block_lat, b->d_block_word0, b->d_base, k,
+                            b->rest_blocks};
+      e = lgx::launch_batch_step(sa, b->nblocks - b->rest_blocks, false, b->stream);
+    }
+  }
+  if (e == cudaSuccess && sample && b->field_blocks) {
+    lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, (uint32_t)b->lats.size(), b->field_blocks,
+                            b->d_base, len};
+    e = lgx::launch_batch_sample(sp, b->stream);
+  }
+  if (e == cudaSuccess) e = lgx::launch_batch_base(b->d_base, len, b->stream);
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+  if (e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return cuda_fail(e, "batch graph capture");
+  }
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  return LGX_OK;
+}
+
+int graph_for(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
+  for (auto& g : b->graphs)
+    if (g.len == len && g.sample == sample) {
+      *out = g.exec;
+      return LGX_OK;
+    }
+  cudaGraphExec_t ex = nullptr;
+  int rc = capture(b, len, sample, &ex);
+  if (rc) return rc;
+  b->graphs.push_back({len, sample, ex});
+  *out = ex;
+  return LGX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgx_batch_create(lgx_lattice* const* lats, size_t n, lgx_batch** out) {
+  if (!out || !lats || n == 0) {
+    lgx::set_error("lgx_batch_create: need at least one lattice");
+    return LGX_ERR_ARG;
+  }
+  *out = nullptr;
+  for (size_t i = 0; i < n; ++i)
+    if (!lats[i] || lats[i]->device != lats[0]->device) {
+      lgx::set_error("lgx_batch_create: null lattice, or lattices on different devices");
+      return LGX_ERR_ARG;
+    }
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j < i; ++j)
+      if (lats[i] == lats[j]) {
+        lgx::set_error("lgx_batch_create: a lattice appears twice");
+        return LGX_ERR_ARG;
+      }
+  lgx_batch* b = new (std::nothrow) lgx_batch();
+  if (!b) {
+    lgx::set_error("out of host memory");
+    return LGX_ERR_ALLOC;
+  }
+  b->device = lats[0]->device;
+  b->lats.assign(lats, lats + n);
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev[i]);
+  // block table: each lattice padded to whole 256-word blocks
+  std::vector<uint32_t> block_lat, block_word0, item0(n + 1, 0), blk0(n + 1, 0);
+  for (int pass = 0; pass < 2; ++pass)
+    for (size_t i = 0; i < n; ++i) {
+      if (lats[i]->rest != (pass == 0)) continue;
+      for (uint32_t w = 0; w < lats[i]->dm.total; w += 256) {
+        block_lat.push_back((uint32_t)i);
+        block_word0.push_back(w);
+      }
+      if (pass == 0) b->rest_blocks = (uint32_t)block_lat.size();
+    }
+  for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+    const lgx::Dims& dm = lats[i]->dm;
+    item0[i + 1] = item0[i] + dm.h * dm.iw;
+    blk0[i + 1] = blk0[i] + (lats[i]->has_field ? lats[i]->bw * lats[i]->bh : 0);
+  }
+  b->nblocks = (uint32_t)block_lat.size();
+  b->items_per_step = item0[n];
+  b->field_blocks = blk0[n];
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_descs, n * sizeof(lgx::LatDesc));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_block_lat, b->nblocks * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_block_word0, b->nblocks * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_item0, (n + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_blk0, (n + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_base, sizeof(uint64_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_block_lat, block_lat.data(), b->nblocks * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_block_word0, block_word0.data(), b->nblocks * 4, cudaMemcpyHostToDevice);
+  // The batched inlet kernel writes lattice i's draws for step s of the
+  // interval at item (item0[i] * len + s * h * iw ...); lay the prefix out
+  // for the longest interval and let each buffer hold kInletChunk steps.
+  b->inlet_bufs.assign(n, nullptr);
+  for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+    const lgx::Dims& dm = lats[i]->dm;
+    if (dm.iw)
+      e = cudaMalloc(&b->inlet_bufs[i], (size_t)lgx::kInletChunk * dm.h * dm.iw * 7 * 4);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_item0, item0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_blk0, blk0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    const int rc = (e == cudaErrorMemoryAllocation) ? LGX_ERR_ALLOC : LGX_ERR_CUDA;
+    lgx::set_error(std::string("lgx_batch_create: ") + cudaGetErrorString(e));
+    free_batch(b);
+    return rc;
+  }
+  *out = b;
+  return LGX_OK;
+}
+
+int lgx_batch_destroy(lgx_batch* b) {
+  if (b) free_batch(b);
+  return LGX_OK;
+}
+
+int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float alpha) {
+  if (!b) {
+    lgx::set_error("null batch handle");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaSetDevice(b->device));
+  // Field and block tables were laid out at creation; pending work on a
+  // member's own stream finishes first.
+  for (lgx_lattice* l : b->lats) LGX_CUDA(cudaStreamSynchronize(l->stream));
+  int rc = setup_descs(b, alpha);
+  if (rc) return rc;
+  // The inlet draws of an interval are laid out per lattice as [k][h][iw][7];
+  // the batched inlet kernel's item index runs lattice-major with each
+  // lattice's items for the whole interval contiguous, so the prefix is
+  // scaled by the interval length when the interval differs from one step.
+  uint64_t left = n, since = 0;
+  while (left > 0) {
+    uint64_t len = std::min<uint64_t>(left, lgx::kInletChunk);
+    if (every > 0) len = std::min<uint64_t>(len, every - since);
+    const bool sample = every > 0 && (since + len >= every || len == left);
+    if (b->items_per_step) {
+      // prefix for this interval length
+      std::vector<uint32_t> item0(b->lats.size() + 1, 0);
+      for (size_t i = 0; i < b->lats.size(); ++i)
+        item0[i + 1] = item0[i] + (uint32_t)len * b->lats[i]->dm.h * b->lats[i]->dm.iw;
+      LGX_CUDA(cudaMemcpyAsync(b->d_item0, item0.data(), item0.size() * 4,
+                               cudaMemcpyHostToDevice, b->stream));
+    }
+    cudaGraphExec_t ex = nullptr;
+    rc = graph_for(b, (uint32_t)len, sample, &ex);
+    if (rc) return rc;
+    LGX_CUDA(cudaGraphLaunch(ex, b->stream));
+    b->graph_launches += 1;
+    const uint64_t per_step = (b->rest_blocks ? 1 : 0) + (b->nblocks > b->rest_blocks ? 1 : 0);
+    b->launches += len * per_step + 1 + (sample ? 1 : 0) + (b->items_per_step ? 1 : 0);
+    left -= len;
+    since += len;
+    if (sample) since = 0;
+  }
+  LGX_CUDA(cudaStreamSynchronize(b->stream));
+  for (lgx_lattice* l : b->lats) {
+    l->steps += n;
+    l->cur ^= (int)(n & 1u);
+    l->inlet_valid = 0;  // the lattice's own inlet draws are for earlier steps
+  }
+  return LGX_OK;
+}
+
+int lgx_batch_advance(lgx_batch* b, uint64_t n) { return lgx_batch_advance_sampling(b, n, 0, 0.f); }
+
+int lgx_batch_launch_count(lgx_batch* b, uint64_t* kernels, uint64_t* graphs) {
+  if (!b) {
+    lgx::set_error("null batch handle");
+    return LGX_ERR_ARG;
+  }
+  if (kernels) *kernels = b->launches;
+  if (graphs) *graphs = b->graph_launches;
+  return LGX_OK;
+}
+
+int lgx_batch_timing_mark(lgx_batch* b, int slot) {
+  if (!b || slot < 0 || slot >= 8) {
+    lgx::set_error("lgx_batch_timing_mark: bad argument");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaEventRecord(b->ev[slot], b->stream));
+  return LGX_OK;
+}
+
+int lgx_batch_timing_elapsed(lgx_batch* b, int a, int c, float* ms) {
+  if (!b || a < 0 || a >= 8 || c < 0 || c >= 8 || !ms) {
+    lgx::set_error("lgx_batch_timing_elapsed: bad argument");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaEventSynchronize(b->ev[c]));
+  LGX_CUDA(cudaEventElapsedTime(ms, b->ev[a], b->ev[c]));
+  return LGX_OK;
+}
+
+}  // extern "C"

@@ -2,78 +2,19 @@
 // the exhaustive circuit check.
 //
 // Coarse-graining (lgca_sample, src/gpu.rs:324-377): one warp per block of the
-// field.  Lanes take rows of the block; each row contributes the masked
-// popcounts of the one to several words the block's columns straddle.  The
-// sums are exact 32-bit integers (mass, px2 = sum CX2 * count, py2, nsolid),
-// reduced across the warp, and only then turned into f32 velocity and blended
-// into the running average with round-to-nearest intrinsics, so no fused
-// multiply-add can change the last bit (Moments::velocity, src/moments.rs:91).
+// field (sample_block in lgx_step_impl.cuh).
 #include "lgx_device.cuh"
 #include "lgx_internal.hpp"
+#include "lgx_step_impl.cuh"
 
 namespace lgx {
 
 namespace {
 
-constexpr float kSqrt3_2 = 0.8660254f;  // src/hex.rs:25
-
 __global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p) {
-  const uint32_t lane = threadIdx.x & 31u;
   const uint32_t blk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (blk >= p.bw * p.bh) return;  // whole warp leaves together
-  const uint32_t jb = blk / p.bw, ib = blk - jb * p.bw;
-  const uint32_t x0 = ib * p.bx, x1 = x0 + p.bx;
-  const uint32_t w0 = x0 >> 5, w1 = (x1 - 1u) >> 5;
-  const size_t S = p.dm.total;
-  int mass = 0, px = 0, py = 0, nsolid = 0;
-  for (uint32_t r = lane; r < p.by; r += 32u) {
-    const size_t base = (size_t)(jb * p.by + r) * p.dm.wpr;
-    for (uint32_t wi = w0; wi <= w1; ++wi) {
-      const uint32_t lo = max(x0, wi << 5) - (wi << 5);
-      const uint32_t hi = min(x1, (wi + 1u) << 5) - (wi << 5);
-      const uint32_t m = (hi - lo >= 32u) ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << lo);
-      const uint32_t sm = __ldg(p.solid + base + wi) & m;
-      nsolid += __popc(sm);
-      const uint32_t fm = m & ~sm;
-      const int c0 = __popc(__ldg(p.a + 0 * S + base + wi) & fm);
-      const int c1 = __popc(__ldg(p.a + 1 * S + base + wi) & fm);
-      const int c2 = __popc(__ldg(p.a + 2 * S + base + wi) & fm);
-      const int c3 = __popc(__ldg(p.a + 3 * S + base + wi) & fm);
-      const int c4 = __popc(__ldg(p.a + 4 * S + base + wi) & fm);
-      const int c5 = __popc(__ldg(p.a + 5 * S + base + wi) & fm);
-      const int c6 = __popc(__ldg(p.a + 6 * S + base + wi) & fm);
-      mass += c0 + c1 + c2 + c3 + c4 + c5 + c6;
-      // CX2 = {2, 1, -1, -2, -1, 1}, CY2 = {0, 1, 1, 0, -1, -1}
-      px += 2 * (c0 - c3) + c1 - c2 - c4 + c5;
-      py += c1 + c2 - c4 - c5;
-    }
-  }
-  const unsigned FULL = 0xffffffffu;
-  mass = __reduce_add_sync(FULL, mass);
-  px = __reduce_add_sync(FULL, px);
-  py = __reduce_add_sync(FULL, py);
-  nsolid = __reduce_add_sync(FULL, nsolid);
-  if (lane != 0) return;
-  const uint32_t nb = p.bw * p.bh;
-  if (p.sums) {
-    p.sums[blk] = mass;
-    p.sums[nb + blk] = px;
-    p.sums[2 * nb + blk] = py;
-    p.sums[3 * nb + blk] = nsolid;
-  }
-  const float n = __uint2float_rn(p.bx * p.by);
-  const float m = __int2float_rn(mass);
-  float vx = 0.0f, vy = 0.0f;
-  if (mass > 0) {
-    vx = __fdiv_rn(__fmul_rn(__int2float_rn(px), 0.5f), m);
-    vy = __fdiv_rn(__fmul_rn(__int2float_rn(py), kSqrt3_2), m);
-  }
-  const float a = p.alpha;
-  const float u0 = p.ux[blk], v0 = p.uy[blk], r0 = p.rho[blk];
-  p.ux[blk] = __fadd_rn(u0, __fmul_rn(a, __fsub_rn(vx, u0)));
-  p.uy[blk] = __fadd_rn(v0, __fmul_rn(a, __fsub_rn(vy, v0)));
-  p.rho[blk] = __fadd_rn(r0, __fmul_rn(a, __fsub_rn(__fdiv_rn(m, n), r0)));
-  p.sol[blk] = __fdiv_rn(__int2float_rn(nsolid), n);
+  sample_block(p, blk);
 }
 
 // Particles on the lattice, obstacle sites included, tail-masked

@@ -1,0 +1,50 @@
+// lgx_handle.hpp -- the lattice handle behind the C ABI (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/lgx.h"
+#include "lgx_internal.hpp"
+
+namespace lgx {
+// Steps whose inlet draws are made in one launch, and the most steps one
+// persistent launch runs.
+constexpr uint32_t kInletChunk = 128;
+}  // namespace lgx
+
+// Mirrors GpuLattice (src/gpu.rs:453-476): the ping-pong planes, the solid
+// plane and its one-bit-per-word summary, the coarse-grained field, and the
+// stream everything of this lattice runs on.
+struct lgx_lattice {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  lgx::Dims dm{};
+  bool rest = true;
+  uint64_t seed = 0;
+  uint64_t steps = 0;
+  uint32_t thresh[7] = {0, 0, 0, 0, 0, 0, 0};
+  uint32_t* planes[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint32_t* solid = nullptr;
+  uint32_t* anysolid = nullptr;
+  uint8_t* cells = nullptr;  // staging for load/store, w*h bytes
+  unsigned long long* counter = nullptr;
+  // inlet draws for the current chunk of steps
+  uint32_t* inlet = nullptr;
+  uint32_t inlet_cap = 0;      // steps the buffer holds
+  size_t inlet_words = 0;      // its size in words
+  uint64_t inlet_first = 0;    // step index of slot 0
+  uint32_t inlet_valid = 0;    // slots filled
+  // field
+  bool has_field = false;
+  uint32_t bx = 0, by = 0, bw = 0, bh = 0;
+  float* field = nullptr;      // ux | uy | rho | sol, bw*bh each
+  int32_t* sums = nullptr;     // mass | px2 | py2 | nsolid
+  cudaEvent_t ev[8] = {};
+  uint64_t launches = 0;     // kernels this handle has launched
+  // persistent multi-step kernel
+  int step_mode = LGX_STEP_AUTO;
+  uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
+  uint32_t* done = nullptr;  // [wave_grid] published step per CTA
+  uint32_t* error = nullptr; // timeout flag
+};

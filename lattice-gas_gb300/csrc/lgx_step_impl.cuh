@@ -1,0 +1,193 @@
+// lgx_step_impl.cuh -- the per-word bitplane update and the per-block
+// coarse-graining, shared by the single-lattice and the batched kernels.
+#pragma once
+
+#include "lgx_device.cuh"
+#include "lgx_internal.hpp"
+
+namespace lgx {
+
+// Plane loads.  Within the persistent kernel the planes change between steps
+// and are written by other SMs, so they are read through L2 (ld.global.cg);
+// the single-step kernel may use the read-only path.
+template <bool COHERENT>
+__device__ __forceinline__ uint32_t ldp(const uint32_t* p) {
+  if (COHERENT) return __ldcg(p);
+  return __ldg(p);
+}
+
+// Word to the left of `j` in the same row, with the row's periodic wrap: for
+// j == 0 the bit that enters is bit `lastbit` of the last word, placed at 31.
+template <bool COHERENT>
+__device__ __forceinline__ uint32_t left_word(const uint32_t* row, uint32_t j, bool in_warp,
+                                              uint32_t shuffled, const Dims& dm) {
+  if (in_warp) return shuffled;
+  if (j > 0) return ldp<COHERENT>(row + j - 1);
+  return ldp<COHERENT>(row + dm.lastword) << (31u - dm.lastbit);
+}
+
+// Bits x+1 into x: (w >> 1) | (next << 31), and on the last word of the row
+// the bit at `lastbit` comes from bit 0 of word 0 (src/gpu.rs:248-254).
+template <bool COHERENT>
+__device__ __forceinline__ uint32_t shift_from_right(uint32_t w, const uint32_t* row, uint32_t j,
+                                                     bool in_warp, uint32_t shuffled,
+                                                     const Dims& dm) {
+  uint32_t hi = in_warp ? shuffled : ((j + 1u < dm.wpr) ? ldp<COHERENT>(row + j + 1u) : 0u);
+  uint32_t v = __funnelshift_r(w, hi, 1);
+  if (j == dm.lastword)
+    v = (v & ~(1u << dm.lastbit)) | ((ldp<COHERENT>(row) & 1u) << dm.lastbit);
+  return v;
+}
+
+// One step of lattice word g (g clamped into range for idle lanes, which
+// still take part in the shuffles; `live` lanes store).  All 32 lanes of the
+// warp call this together with consecutive g.
+template <bool REST, bool COHERENT>
+__device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
+                                          const uint32_t* __restrict__ solid,
+                                          const uint32_t* __restrict__ anysolid,
+                                          const uint32_t* __restrict__ inlet, const Dims& dm,
+                                          const Draws& s, uint32_t g, bool live) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t y = g / dm.wpr;
+  const uint32_t j = g - y * dm.wpr;
+  const bool odd = y & 1u;
+  const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
+  const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
+  const size_t S = dm.total;
+
+  const uint32_t* r0 = a + 0 * S + (size_t)y * dm.wpr;
+  const uint32_t* r1 = a + 1 * S + (size_t)ym * dm.wpr;
+  const uint32_t* r2 = a + 2 * S + (size_t)ym * dm.wpr;
+  const uint32_t* r3 = a + 3 * S + (size_t)y * dm.wpr;
+  const uint32_t* r4 = a + 4 * S + (size_t)yp * dm.wpr;
+  const uint32_t* r5 = a + 5 * S + (size_t)yp * dm.wpr;
+
+  const uint32_t w0 = ldp<COHERENT>(r0 + j), w1 = ldp<COHERENT>(r1 + j);
+  const uint32_t w2 = ldp<COHERENT>(r2 + j), w3 = ldp<COHERENT>(r3 + j);
+  const uint32_t w4 = ldp<COHERENT>(r4 + j), w5 = ldp<COHERENT>(r5 + j);
+  const uint32_t w6 = ldp<COHERENT>(a + 6 * S + g);
+
+  // Partner lanes hold the neighbouring word of the same plane and row
+  // exactly when they sit in the same row.
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t l0 = __shfl_up_sync(FULL, w0, 1), l1 = __shfl_up_sync(FULL, w1, 1);
+  const uint32_t l5 = __shfl_up_sync(FULL, w5, 1);
+  const uint32_t q2 = __shfl_down_sync(FULL, w2, 1), q3 = __shfl_down_sync(FULL, w3, 1);
+  const uint32_t q4 = __shfl_down_sync(FULL, w4, 1);
+  const bool lok = lane > 0u && j > 0u;
+  const bool rok = lane < 31u && j + 1u < dm.wpr;
+
+  // Gather (src/gpu.rs:237-265).  Direction d takes from the neighbour in the
+  // opposite direction; the column offset depends on the row's parity:
+  //   d0: x-1        d3: x+1
+  //   d1: even x-1, odd x      d2: even x, odd x+1     (row y-1)
+  //   d4: even x, odd x+1      d5: even x-1, odd x     (row y+1)
+  uint32_t n[7];
+  n[0] = __funnelshift_l(left_word<COHERENT>(r0, j, lok, l0, dm), w0, 1);
+  n[3] = shift_from_right<COHERENT>(w3, r3, j, rok, q3, dm);
+  if (odd) {
+    n[1] = w1;
+    n[2] = shift_from_right<COHERENT>(w2, r2, j, rok, q2, dm);
+    n[4] = shift_from_right<COHERENT>(w4, r4, j, rok, q4, dm);
+    n[5] = w5;
+  } else {
+    n[1] = __funnelshift_l(left_word<COHERENT>(r1, j, lok, l1, dm), w1, 1);
+    n[2] = w2;
+    n[4] = w4;
+    n[5] = __funnelshift_l(left_word<COHERENT>(r5, j, lok, l5, dm), w5, 1);
+  }
+  n[6] = w6;
+
+  uint32_t o[7];
+  collide<REST>(n, s, o);
+
+  uint32_t sm = 0u;
+  if ((__ldg(anysolid + (g >> 5)) >> (g & 31u)) & 1u) sm = __ldg(solid + g);
+  uint32_t res[7];
+  walls(n, o, sm, res);
+
+  if (j < dm.iw) {  // inflow re-seed of the leftmost columns (src/gpu.rs:296-306)
+    const uint32_t span = min(dm.inlet_cols - j * 32u, 32u);
+    const uint32_t imask = (span >= 32u) ? 0xffffffffu : ((1u << span) - 1u);
+    const uint32_t apply = imask & ~sm;
+    const uint32_t* bern = inlet + ((size_t)y * dm.iw + j) * 7u;
+#pragma unroll
+    for (int d = 0; d < 7; ++d) res[d] = (res[d] & ~apply) | (__ldg(bern + d) & apply);
+  }
+
+  const uint32_t mask = (j == dm.lastword) ? dm.tail : 0xffffffffu;
+  if (live) {
+#pragma unroll
+    for (int d = 0; d < 7; ++d) b[d * S + g] = res[d] & mask;
+  }
+}
+
+
+// Coarse-graining of field block `blk` of one lattice by one whole warp
+// (lgca_sample, src/gpu.rs:324-377).  Lanes take rows of the block; each row
+// contributes the masked popcounts of the one to several words the block's
+// columns straddle.  The sums are exact 32-bit integers (mass, px2 = sum
+// CX2 * count, py2, nsolid), reduced across the warp, and only then turned
+// into f32 velocity and blended into the running average with
+// round-to-nearest intrinsics, so no fused multiply-add can change the last
+// bit (Moments::velocity, src/moments.rs:91).
+__device__ __forceinline__ void sample_block(const SampleArgs& p, uint32_t blk) {
+  constexpr float kSqrt3_2 = 0.8660254f;  // src/hex.rs:25
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t jb = blk / p.bw, ib = blk - jb * p.bw;
+  const uint32_t x0 = ib * p.bx, x1 = x0 + p.bx;
+  const uint32_t w0 = x0 >> 5, w1 = (x1 - 1u) >> 5;
+  const size_t S = p.dm.total;
+  int mass = 0, px = 0, py = 0, nsolid = 0;
+  for (uint32_t r = lane; r < p.by; r += 32u) {
+    const size_t base = (size_t)(jb * p.by + r) * p.dm.wpr;
+    for (uint32_t wi = w0; wi <= w1; ++wi) {
+      const uint32_t lo = max(x0, wi << 5) - (wi << 5);
+      const uint32_t hi = min(x1, (wi + 1u) << 5) - (wi << 5);
+      const uint32_t m = (hi - lo >= 32u) ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << lo);
+      const uint32_t sm = __ldg(p.solid + base + wi) & m;
+      nsolid += __popc(sm);
+      const uint32_t fm = m & ~sm;
+      const int c0 = __popc(__ldcg(p.a + 0 * S + base + wi) & fm);
+      const int c1 = __popc(__ldcg(p.a + 1 * S + base + wi) & fm);
+      const int c2 = __popc(__ldcg(p.a + 2 * S + base + wi) & fm);
+      const int c3 = __popc(__ldcg(p.a + 3 * S + base + wi) & fm);
+      const int c4 = __popc(__ldcg(p.a + 4 * S + base + wi) & fm);
+      const int c5 = __popc(__ldcg(p.a + 5 * S + base + wi) & fm);
+      const int c6 = __popc(__ldcg(p.a + 6 * S + base + wi) & fm);
+      mass += c0 + c1 + c2 + c3 + c4 + c5 + c6;
+      // CX2 = {2, 1, -1, -2, -1, 1}, CY2 = {0, 1, 1, 0, -1, -1}
+      px += 2 * (c0 - c3) + c1 - c2 - c4 + c5;
+      py += c1 + c2 - c4 - c5;
+    }
+  }
+  const unsigned FULL = 0xffffffffu;
+  mass = __reduce_add_sync(FULL, mass);
+  px = __reduce_add_sync(FULL, px);
+  py = __reduce_add_sync(FULL, py);
+  nsolid = __reduce_add_sync(FULL, nsolid);
+  if (lane != 0) return;
+  const uint32_t nb = p.bw * p.bh;
+  if (p.sums) {
+    p.sums[blk] = mass;
+    p.sums[nb + blk] = px;
+    p.sums[2 * nb + blk] = py;
+    p.sums[3 * nb + blk] = nsolid;
+  }
+  const float n = __uint2float_rn(p.bx * p.by);
+  const float m = __int2float_rn(mass);
+  float vx = 0.0f, vy = 0.0f;
+  if (mass > 0) {
+    vx = __fdiv_rn(__fmul_rn(__int2float_rn(px), 0.5f), m);
+    vy = __fdiv_rn(__fmul_rn(__int2float_rn(py), kSqrt3_2), m);
+  }
+  const float a = p.alpha;
+  const float u0 = p.ux[blk], v0 = p.uy[blk], r0 = p.rho[blk];
+  p.ux[blk] = __fadd_rn(u0, __fmul_rn(a, __fsub_rn(vx, u0)));
+  p.uy[blk] = __fadd_rn(v0, __fmul_rn(a, __fsub_rn(vy, v0)));
+  p.rho[blk] = __fadd_rn(r0, __fmul_rn(a, __fsub_rn(__fdiv_rn(m, n), r0)));
+  p.sol[blk] = __fdiv_rn(__int2float_rn(nsolid), n);
+}
+
+}  // namespace lgx

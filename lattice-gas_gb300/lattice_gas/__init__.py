@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblgx.so")
 
-__all__ = ["GpuLattice", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
+__all__ = ["GpuLattice", "Batch", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
            "add_box", "add_circle", "shear_wave", "verify_circuit", "SQRT3_2"]
 
 SQRT3_2 = np.float32(0.8660254)
@@ -87,6 +87,13 @@ def lib():
         _sig(L, "lgx_timing_elapsed", vp, C.c_int, C.c_int, C.POINTER(C.c_float))
         _sig(L, "lgx_verify_circuit", C.c_int, u32p, sz)
         _sig(L, "lgx_select_device", C.c_int)
+        _sig(L, "lgx_batch_create", C.POINTER(vp), sz, C.POINTER(vp))
+        _sig(L, "lgx_batch_destroy", vp)
+        _sig(L, "lgx_batch_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
+        _sig(L, "lgx_batch_advance", vp, C.c_uint64)
+        _sig(L, "lgx_batch_launch_count", vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64))
+        _sig(L, "lgx_batch_timing_mark", vp, C.c_int)
+        _sig(L, "lgx_batch_timing_elapsed", vp, C.c_int, C.c_int, C.POINTER(C.c_float))
         _sig(L, "lgx_probe_int_rate", C.c_int, C.POINTER(C.c_double))
         _sig(L, "lgx_host_alloc", sz, C.POINTER(vp))
         _sig(L, "lgx_host_free", vp)
@@ -244,6 +251,50 @@ class GpuLattice:
     def timing_elapsed(self, a, b) -> float:
         ms = C.c_float()
         _check(lib().lgx_timing_elapsed(self._h, int(a), int(b), C.byref(ms)))
+        return float(ms.value)
+
+
+class Batch:
+    """Many lattices advanced together: one launch per step for all of them,
+    each sampling interval a replayed CUDA graph.  The lattices stay owned by
+    the caller; advance them only through the batch while it is alive."""
+
+    def __init__(self, lattices):
+        self.lattices = list(lattices)
+        arr = (vp * len(self.lattices))(*[l.handle.value for l in self.lattices])
+        self._h = vp()
+        _check(lib().lgx_batch_create(arr, len(self.lattices), C.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().lgx_batch_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def advance(self, n):
+        _check(lib().lgx_batch_advance(self._h, int(n)))
+
+    def advance_sampling(self, n, sample_every, alpha):
+        _check(lib().lgx_batch_advance_sampling(self._h, int(n), int(sample_every),
+                                                float(alpha)))
+
+    @property
+    def launches(self):
+        k, g = C.c_uint64(), C.c_uint64()
+        _check(lib().lgx_batch_launch_count(self._h, C.byref(k), C.byref(g)))
+        return int(k.value), int(g.value)
+
+    def timing_mark(self, slot):
+        _check(lib().lgx_batch_timing_mark(self._h, int(slot)))
+
+    def timing_elapsed(self, a, b) -> float:
+        ms = C.c_float()
+        _check(lib().lgx_batch_timing_elapsed(self._h, int(a), int(b), C.byref(ms)))
         return float(ms.value)
 
 

@@ -1,0 +1,138 @@
+"""Batches: many uneven lattices advanced together must give, lattice by
+lattice, exactly what advancing each alone gives (and what the oracle gives).
+Every test here needs a GPU."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make(LG, specs):
+    """specs: (w, h, rest, inlet_cols, obstacle, block, seed)"""
+    out = []
+    for w, h, rest, inlet, obstacle, block, seed in specs:
+        cells = np.zeros(w * h, np.uint8)
+        if obstacle:
+            LG.add_circle(cells, w, h, w / 3.0, h * 0.43, min(w, h) / 6.0)
+        LG.init_equilibrium(cells, 0.3, 0.15, 0.0, rest, seed)
+        out.append((w, h, rest, inlet, block, seed, cells))
+    return out
+
+
+def build(LG, spec):
+    w, h, rest, inlet, block, seed, cells = spec
+    g = LG.GpuLattice(w, h, rest, seed)
+    if inlet:
+        g.set_inlet(inlet, 0.3, (0.15, 0.0), rest)
+    if block:
+        g.attach_field(block, block)
+    g.load(cells)
+    return g
+
+
+def snapshot(g):
+    out = [g.store(), g.steps, g.total_particles()]
+    if g._field is not None:
+        out += g.read_block_sums()
+        f = g.read_field()
+        out += [f.ux.copy(), f.uy.copy(), f.rho.copy(), f.solid.copy()]
+    return out
+
+
+def same(a, b):
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        if isinstance(x, np.ndarray):
+            assert np.array_equal(x.view(np.uint8), y.view(np.uint8))
+        else:
+            assert x == y
+
+
+SPECS = [
+    (256, 256, True, 0, False, 16, 11),
+    (100, 34, True, 40, True, 8, 12),     # ragged, two-word inlet, obstacle
+    (33, 20, True, 8, False, 0, 13),      # one-bit tail, no field
+    (1000, 64, True, 8, True, 32, 14),
+    (64, 18, False, 0, False, 8, 15),     # six-direction rule in the same batch
+    (129, 40, False, 70, True, 16, 16),
+    (2048, 1024, True, 0, False, 16, 17),
+]
+
+
+@pytest.mark.parametrize("n,every", [(1, 0), (37, 0), (300, 50), (257, 100), (400, 500)])
+def test_batch_equals_each_lattice_alone(LG, n, every):
+    specs = make(LG, SPECS)
+    alone = [build(LG, s) for s in specs]
+    for g in alone:
+        g.advance_sampling(n, every, 0.4)
+    together = [build(LG, s) for s in specs]
+    b = LG.Batch(together)
+    b.advance_sampling(n, every, 0.4)
+    for x, y in zip(alone, together):
+        same(snapshot(x), snapshot(y))
+    b.close()
+
+
+def test_batch_replays_and_continues(LG):
+    """Several calls (graph replays, mixed lengths), then a plain advance after
+    the batch: still identical to the lattices run alone throughout."""
+    specs = make(LG, SPECS[:4])
+    alone = [build(LG, s) for s in specs]
+    together = [build(LG, s) for s in specs]
+    b = LG.Batch(together)
+    for n, every in ((100, 50), (100, 50), (33, 0), (150, 50)):
+        for g in alone:
+            g.advance_sampling(n, every, 1.0)
+        b.advance_sampling(n, every, 1.0)
+    b.close()
+    for g in alone + together:
+        g.advance(10)
+    for x, y in zip(alone, together):
+        same(snapshot(x), snapshot(y))
+
+
+def test_batch_matches_oracle(LG, O):
+    specs = make(LG, SPECS[:5])
+    together = [build(LG, s) for s in specs]
+    b = LG.Batch(together)
+    b.advance_sampling(120, 40, 0.5)
+    for (w, h, rest, inlet, block, seed, cells), g in zip(specs, together):
+        o = O.BitplaneLattice(w, h, rest, seed, 4)
+        if inlet:
+            o.set_inlet(inlet, 0.3, (0.15, 0.0), rest)
+        if block:
+            o.attach_field(block, block)
+        o.load(cells)
+        o.advance_sampling(120, 40, 0.5)
+        assert np.array_equal(g.store(), o.store())
+        if block:
+            for x, y in zip(g.read_block_sums(), o.read_block_sums()):
+                assert np.array_equal(x, y)
+
+
+def test_transport_sweep_batch_equals_alone(LG):
+    """The 64-lattice transport sweep (shear-wave starts, 16x16 blocks every 50
+    steps), 200 steps: batch == each alone."""
+    from lattice_gas import workloads as W
+    wls = W.transport_sweep()
+    def mk(wl):
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.attach_field(wl.block, wl.block)
+        g.load(wl.cells)
+        return g
+    alone = [mk(wl) for wl in wls]
+    for g in alone:
+        g.advance_sampling(200, 50, 1.0)
+    together = [mk(wl) for wl in wls]
+    b = LG.Batch(together)
+    b.advance_sampling(200, 50, 1.0)
+    for x, y in zip(alone, together):
+        same(snapshot(x), snapshot(y))
+
+
+def test_batch_rejects_bad_arguments(LG):
+    g = LG.GpuLattice(64, 64, True, 1)
+    with pytest.raises(LG.LgxError):
+        LG.Batch([g, g])
+    with pytest.raises(LG.LgxError):
+        LG.Batch([])
