@@ -28,6 +28,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "lattice-gas_gb300"))
 
@@ -210,6 +212,120 @@ def run_reference(args, world, rank):
     return 0
 
 
+def bench_batched(LG, W, steps: int):
+    """The transport sweep: 64 periodic shear-wave lattices, 256..2048 x 256..1024,
+    16x16 blocks every 50 steps; once one lattice per launch (each lattice's
+    run in turn), once as one batch (a replayed CUDA graph per interval)."""
+    wls = W.transport_sweep(steps=steps)
+    sites = sum(w.sites for w in wls)
+
+    def mk(wl, mode):
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.set_step_mode(mode)
+        g.attach_field(wl.block, wl.block)
+        g.load(wl.cells)
+        return g
+
+    plain = [mk(wl, 1) for wl in wls]
+    for g in plain:
+        g.advance_sampling(100, 50, 1.0)
+    t0 = time.perf_counter()
+    for g in plain:
+        g.advance_sampling(steps, 50, 1.0)
+    t_plain = time.perf_counter() - t0
+    together = [mk(wl, 0) for wl in wls]
+    b = LG.Batch(together)
+    b.advance_sampling(100, 50, 1.0)
+    k0, g0 = b.launches
+    b.timing_mark(0)
+    b.advance_sampling(steps, 50, 1.0)
+    b.timing_mark(1)
+    t_batch = b.timing_elapsed(0, 1) / 1e3
+    k1, g1 = b.launches
+    same = all(np.array_equal(x.store(), y.store()) for x, y in zip(plain, together))
+    out = {"workload": "transport sweep: 64 shear-wave lattices 256..2048 x 256..1024, "
+                       "%d steps, 16x16 blocks every 50" % steps,
+           "sites": sites, "value": round(sites * steps / t_batch / 1e9, 2),
+           "plain_value": round(sites * steps / t_plain / 1e9, 2),
+           "speedup_vs_plain": round(t_plain / t_batch, 2), "unit": UNIT,
+           "batched_s": round(t_batch, 4), "plain_s": round(t_plain, 4),
+           "kernel_launches": k1 - k0, "graph_launches": g1 - g0,
+           "bit_exact_vs_plain": bool(same)}
+    b.close()
+    for g in plain + together:
+        g.close()
+    return out
+
+
+def bench_served(LG, W, n: int, budget: int):
+    """The request stream: Poisson arrivals at 200/s, sizes 128x128..4096x2048,
+    1k..50k steps, sampling every 50..500 steps with 8..32 blocks, obstacle none
+    / plate / circle.  Served with continuous batching, and as the plain
+    baseline each request alone on the plain kernel, first come first served."""
+    import threading
+    reqs = W.request_stream(n=n)
+    work = sum(r.work.sites * r.work.steps for r in reqs)
+    srv = LG.Server(budget_bytes=budget, max_active=512)
+    ids = [None] * len(reqs)
+    t0 = time.perf_counter()
+
+    def feed():
+        for i, r in enumerate(reqs):
+            d = r.arrival - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            ids[i] = srv.submit_workload(r.work)
+
+    th = threading.Thread(target=feed)
+    th.start()
+    th.join()
+    lat = []
+    for rid in ids:
+        if srv.wait(rid, 600.0) != LG.REQ_DONE:
+            raise RuntimeError("a served request did not complete")
+        lat.append(srv.result(rid)["latency"])
+    t_served = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    # plain: each request alone, one lattice per launch, in arrival order
+    clock = 0.0
+    plain_lat = []
+    busy = 0.0
+    for r in reqs:
+        wl = r.work
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.set_step_mode(1)
+        if wl.inlet_cols:
+            g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)
+        g.attach_field(wl.block, wl.block)
+        t1 = time.perf_counter()
+        g.load(wl.cells)
+        g.advance_sampling(wl.steps, wl.sample_every, wl.alpha)
+        g.read_field()
+        g.read_block_sums()
+        svc = time.perf_counter() - t1
+        g.close()
+        busy += svc
+        clock = max(clock, r.arrival) + svc
+        plain_lat.append(clock - r.arrival)
+    lat.sort()
+    plain_lat.sort()
+    pct = lambda a, q: a[min(len(a) - 1, int(q * len(a)))]
+    return {"workload": "request stream: %d requests, Poisson 200/s, 128x128..4096x2048, "
+                        "1k..50k steps, sampling 50..500, blocks 8..32; budget %d MiB"
+                        % (n, budget >> 20),
+            "site_updates": work, "value": round(work / t_served / 1e9, 2),
+            "plain_value": round(work / clock / 1e9, 2),
+            "speedup_vs_plain": round(clock / t_served, 2), "unit": UNIT,
+            "p50_latency_s": round(pct(lat, 0.5), 4), "p99_latency_s": round(pct(lat, 0.99), 4),
+            "plain_p50_latency_s": round(pct(plain_lat, 0.5), 4),
+            "plain_p99_latency_s": round(pct(plain_lat, 0.99), 4),
+            "served_s": round(t_served, 3), "plain_s": round(clock, 3),
+            "ticks": st["ticks"], "kernel_launches": st["kernel_launches"],
+            "latency_note": "includes queueing; the stream offers more work than the GPU "
+                            "serves, so the queue grows while it arrives"}
+
+
 def run_gb300(args, world, rank, local):
     import numpy as np
     import lattice_gas as LG
@@ -293,6 +409,11 @@ def run_gb300(args, world, rank, local):
                          "Lattice::step restated in C (oracle/), %d threads"
                          % (nsteps, dt, threads)}
 
+    batched = served = None
+    if not args.no_patterns:
+        batched = bench_batched(LG, W, args.sweep_steps)
+        served = bench_served(LG, W, args.requests, args.budget_mib << 20)
+
     if rank != 0:
         return 0
     line = {
@@ -316,9 +437,11 @@ def run_gb300(args, world, rank, local):
                      "note": "integer-ALU bound; see int_pipe"},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": wl.sites,
                 "d2h_bytes_per_step": 8 * nb * 4},
-        "gpu_launches": launches // max(args.steps, 1) * args.steps,
+        "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "batched": batched,
+        "served": served,
         "device": g.device_name(),
     }
     print(json.dumps(line), flush=True)
@@ -334,6 +457,11 @@ def main():
     ap.add_argument("--lattice-steps", type=int, default=20000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-patterns", action="store_true",
+                    help="skip the batched and served measurements")
+    ap.add_argument("--sweep-steps", type=int, default=5000)
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--budget-mib", type=int, default=4096)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -140,6 +140,72 @@ int lgx_batch_launch_count(lgx_batch *b, uint64_t *kernels, uint64_t *graphs);
 int lgx_batch_timing_mark(lgx_batch *b, int slot);
 int lgx_batch_timing_elapsed(lgx_batch *b, int a, int c, float *ms);
 
+/* ---- serving: a request loop with continuous batching ---------------------- */
+
+/* One simulation request: a lattice's cells (copied at submit), its rule and
+ * seed, the inflow (inlet_cols == 0: none), the run length, and the field to
+ * sample (every sample_every steps and after the last, blocks of bx x by,
+ * running average weight alpha).  The result is exactly what
+ * lgx_attach_field + lgx_advance_sampling give on a fresh lattice. */
+typedef struct {
+  size_t w, h;
+  int rest_particles;
+  uint64_t seed;
+  const uint8_t *cells;
+  float density, ux, uy;
+  size_t inlet_cols;
+  uint64_t steps;
+  uint64_t sample_every;
+  float alpha;
+  size_t bx, by;
+} lgx_request;
+
+enum {
+  LGX_REQ_QUEUED = 0,
+  LGX_REQ_RUNNING = 1,
+  LGX_REQ_DONE = 2,
+  LGX_REQ_CANCELLED = 3,
+  LGX_REQ_FAILED = 4
+};
+
+typedef struct {
+  uint64_t completed, failed, cancelled, active, queued;
+  uint64_t ticks, kernel_launches, site_updates;
+  uint64_t bytes_in_use, peak_bytes, peak_active;
+} lgx_server_stats;
+
+typedef struct lgx_server lgx_server;
+/* A server thread on the current device.  Requests are admitted, first fit in
+ * arrival order, while their device memory fits `budget_bytes` and at most
+ * `max_active` are resident; resident lattices advance together (one batched
+ * launch per step) and finished ones make room for waiting ones.  No
+ * counterpart in the reference beyond running one lattice per request. */
+int lgx_server_create(size_t budget_bytes, size_t max_active, lgx_server **out);
+/* Cancels what is still queued or running, then stops the thread. */
+int lgx_server_destroy(lgx_server *s);
+/* LGX_ERR_BUSY if the lattice alone exceeds the budget. */
+int lgx_server_submit(lgx_server *s, const lgx_request *req, uint64_t *id);
+int lgx_server_poll(lgx_server *s, uint64_t id, int *state);
+/* Waits until the request leaves the queued/running states (timeout_s < 0:
+ * forever); LGX_ERR_BUSY on timeout. */
+int lgx_server_wait(lgx_server *s, uint64_t id, double timeout_s, int *state);
+/* The final field, exact block sums and particle count of a finished request,
+ * and its latency (completion minus submission, seconds).  Null outputs are
+ * skipped; n_blocks must be (w/bx)*(h/by). */
+int lgx_server_result(lgx_server *s, uint64_t id, float *ux, float *uy, float *rho, float *sol,
+                      int32_t *mass, int32_t *px2, int32_t *py2, int32_t *nsolid,
+                      size_t n_blocks, uint64_t *particles, double *latency_s);
+int lgx_server_cancel(lgx_server *s, uint64_t id);
+/* Frees a finished request's result buffers. */
+int lgx_server_release(lgx_server *s, uint64_t id);
+int lgx_server_get_stats(lgx_server *s, lgx_server_stats *out);
+/* Device memory one request occupies while resident (what admission counts
+ * against the budget). */
+int lgx_request_device_bytes(const lgx_request *req, size_t *out);
+/* Test hook: the next `count` admissions fail as if device allocation had
+ * failed; those requests end LGX_REQ_FAILED and serving continues. */
+int lgx_server_inject_alloc_failure(lgx_server *s, int count);
+
 /* ---- host-side lattice setup (src/lattice.rs, src/hex.rs) ---------------- */
 
 /* Equilibrium::new(..).thresholds() (src/lattice.rs:72-92): 24-bit thresholds,

@@ -5,8 +5,9 @@
 // Metal queue (src/transport.rs:299-313).  Small lattices cannot fill a GPU,
 // so here one launch steps every lattice of a batch: blocks of 256 threads
 // are laid over the concatenated word ranges (each lattice padded to whole
-// blocks), a per-block table names the lattice, and each block runs the
-// same per-word update as the single-lattice kernel.  The step kernels are
+// blocks), a block finds its lattice by binary search over the per-lattice
+// block prefix, and runs the same per-word update as the single-lattice
+// kernel.  The step kernels are
 // chained with programmatic dependent launch, a batched coarse-graining
 // kernel samples every lattice's field, and a sampling interval's launches
 // are captured once into a CUDA graph that is replayed for every interval:
@@ -36,11 +37,23 @@ __device__ __forceinline__ void batch_word(const LatDesc& d, uint64_t local, uin
 // One step of every lattice of one rule in the batch (blocks first_block ..
 // first_block + gridDim.x - 1 of the block table).  `k` is the step's index
 // within the captured interval; the batch step is *base + k.
+// Largest i < n with prefix[i] <= x (prefix[0] == 0, non-decreasing): the
+// entry that owns item x when entry i owns prefix[i] .. prefix[i+1] - 1.
+__device__ __forceinline__ uint32_t owner_of(const uint32_t* prefix, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(prefix + mid) <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 template <bool REST>
 __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
-  const LatDesc& d = p.descs[p.block_lat[blk]];
-  uint32_t g = p.block_word0[blk] + threadIdx.x;
+  const uint32_t li = owner_of(p.block0, p.nlat, blk);
+  const LatDesc& d = p.descs[li];
+  uint32_t g = (blk - __ldg(p.block0 + li)) * (uint32_t)kThreads + threadIdx.x;
   const bool live = g < d.dm.total;
   if (!live) g = d.dm.total - 1u;
   const uint64_t local = *p.base + p.k;
@@ -55,12 +68,7 @@ __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepAr
 __global__ void __launch_bounds__(128) lgx_batch_inlet_kernel(BatchInletArgs p) {
   const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= p.total_items) return;
-  // lattice by binary search over the item prefix
-  uint32_t lo = 0, hi = p.nlat;
-  while (hi - lo > 1u) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (p.item0[mid] <= idx) lo = mid; else hi = mid;
-  }
+  const uint32_t lo = owner_of(p.item0, p.nlat, idx);
   const LatDesc& d = p.descs[lo];
   const uint32_t per_step = d.dm.h * d.dm.iw;
   const uint32_t rel = idx - p.item0[lo];
@@ -82,11 +90,7 @@ __global__ void __launch_bounds__(128) lgx_batch_inlet_kernel(BatchInletArgs p) 
 __global__ void __launch_bounds__(256) lgx_batch_sample_kernel(BatchSampleArgs p) {
   const uint32_t task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (task >= p.total_blocks) return;
-  uint32_t lo = 0, hi = p.nlat;
-  while (hi - lo > 1u) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (p.blk0[mid] <= task) lo = mid; else hi = mid;
-  }
+  const uint32_t lo = owner_of(p.blk0, p.nlat, task);
   const LatDesc& d = p.descs[lo];
   const uint64_t local = *p.base + p.k_after;
   const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;

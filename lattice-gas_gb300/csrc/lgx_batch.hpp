@@ -26,11 +26,11 @@ struct LatDesc {
 
 struct BatchStepArgs {
   const LatDesc* descs;
-  const uint32_t* block_lat;    // lattice of each 256-thread block
-  const uint32_t* block_word0;  // its first lattice word
-  const uint64_t* base;         // batch steps completed before this interval
-  uint32_t k;                   // step index within the interval
-  uint32_t first_block;         // this launch's first entry of the block table
+  const uint32_t* block0;  // prefix of per-lattice 256-word blocks, nlat + 1 entries
+  uint32_t nlat;
+  const uint64_t* base;    // batch steps completed before this interval
+  uint32_t k;              // step index within the interval
+  uint32_t first_block;    // this launch's first block (rest lattices come first)
 };
 
 struct BatchInletArgs {

@@ -45,13 +45,12 @@ struct lgx_batch {
   std::vector<lgx_lattice*> lats;
   std::vector<lgx::LatDesc> descs;
   lgx::LatDesc* d_descs = nullptr;
-  uint32_t* d_block_lat = nullptr;
-  uint32_t* d_block_word0 = nullptr;
+  uint32_t* d_block0 = nullptr;
   uint32_t* d_item0 = nullptr;
   uint32_t* d_blk0 = nullptr;
   uint64_t* d_base = nullptr;
   uint32_t nblocks = 0;
-  uint32_t rest_blocks = 0;     // leading block-table entries of rest-particle lattices
+  uint32_t rest_blocks = 0;     // leading blocks, those of rest-particle lattices
   uint32_t items_per_step = 0;  // inlet draw items of one step, all lattices
   uint32_t field_blocks = 0;
   std::vector<uint32_t*> inlet_bufs;
@@ -69,8 +68,7 @@ void free_batch(lgx_batch* b) {
   for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
   for (auto* p : b->inlet_bufs) cudaFree(p);
   cudaFree(b->d_descs);
-  cudaFree(b->d_block_lat);
-  cudaFree(b->d_block_word0);
+  cudaFree(b->d_block0);
   cudaFree(b->d_item0);
   cudaFree(b->d_blk0);
   cudaFree(b->d_base);
@@ -125,13 +123,13 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
   }
   for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
     // rest-particle lattices' blocks first, then the six-direction ones
+    const uint32_t nl = (uint32_t)b->lats.size();
     if (b->rest_blocks) {
-      lgx::BatchStepArgs sa{b->d_descs, b->d_block_lat, b->d_block_word0, b->d_base, k, 0};
+      lgx::BatchStepArgs sa{b->d_descs, b->d_block0, nl, b->d_base, k, 0};
       e = lgx::launch_batch_step(sa, b->rest_blocks, true, b->stream);
     }
     if (e == cudaSuccess && b->nblocks > b->rest_blocks) {
-      lgx::BatchStepArgs sa{b->d_descs, b->d_block_lat, b->d_block_word0, b->d_base, k,
-                            b->rest_blocks};
+      lgx::BatchStepArgs sa{b->d_descs, b->d_block0, nl, b->d_base, k, b->rest_blocks};
       e = lgx::launch_batch_step(sa, b->nblocks - b->rest_blocks, false, b->stream);
     }
   }
@@ -194,39 +192,33 @@ int lgx_batch_create(lgx_lattice* const* lats, size_t n, lgx_batch** out) {
     return LGX_ERR_ALLOC;
   }
   b->device = lats[0]->device;
-  b->lats.assign(lats, lats + n);
+  // rest-particle lattices first, so each rule's blocks are one contiguous run
+  for (int pass = 0; pass < 2; ++pass)
+    for (size_t i = 0; i < n; ++i)
+      if (lats[i]->rest == (pass == 0)) b->lats.push_back(lats[i]);
+  lats = b->lats.data();
   cudaError_t e = cudaSetDevice(b->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev[i]);
   // block table: each lattice padded to whole 256-word blocks
-  std::vector<uint32_t> block_lat, block_word0, item0(n + 1, 0), blk0(n + 1, 0);
-  for (int pass = 0; pass < 2; ++pass)
-    for (size_t i = 0; i < n; ++i) {
-      if (lats[i]->rest != (pass == 0)) continue;
-      for (uint32_t w = 0; w < lats[i]->dm.total; w += 256) {
-        block_lat.push_back((uint32_t)i);
-        block_word0.push_back(w);
-      }
-      if (pass == 0) b->rest_blocks = (uint32_t)block_lat.size();
-    }
+  std::vector<uint32_t> block0(n + 1, 0), item0(n + 1, 0), blk0(n + 1, 0);
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
     const lgx::Dims& dm = lats[i]->dm;
+    block0[i + 1] = block0[i] + (dm.total + 255) / 256;
+    if (lats[i]->rest) b->rest_blocks = block0[i + 1];
     item0[i + 1] = item0[i] + dm.h * dm.iw;
     blk0[i + 1] = blk0[i] + (lats[i]->has_field ? lats[i]->bw * lats[i]->bh : 0);
   }
-  b->nblocks = (uint32_t)block_lat.size();
+  b->nblocks = block0[n];
   b->items_per_step = item0[n];
   b->field_blocks = blk0[n];
   if (e == cudaSuccess) e = cudaMalloc(&b->d_descs, n * sizeof(lgx::LatDesc));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_block_lat, b->nblocks * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_block_word0, b->nblocks * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_block0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_item0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_blk0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_base, sizeof(uint64_t));
   if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_block_lat, block_lat.data(), b->nblocks * 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_block_word0, block_word0.data(), b->nblocks * 4, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(b->d_block0, block0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
   // The batched inlet kernel writes lattice i's draws for step s of the
   // interval at item (item0[i] * len + s * h * iw ...); lay the prefix out
   // for the longest interval and let each buffer hold kInletChunk steps.

@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblgx.so")
 
-__all__ = ["GpuLattice", "Batch", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
+__all__ = ["GpuLattice", "Batch", "Server", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
            "add_box", "add_circle", "shear_wave", "verify_circuit", "SQRT3_2"]
 
 SQRT3_2 = np.float32(0.8660254)
@@ -38,6 +38,24 @@ i32p = C.POINTER(C.c_int32)
 f32p = C.POINTER(C.c_float)
 sz = C.c_size_t
 vp = C.c_void_p
+
+
+class Request(C.Structure):
+    """lgx_request (include/lgx.h)."""
+    _fields_ = [("w", C.c_size_t), ("h", C.c_size_t), ("rest_particles", C.c_int),
+                ("seed", C.c_uint64), ("cells", C.POINTER(C.c_uint8)), ("density", C.c_float),
+                ("ux", C.c_float), ("uy", C.c_float), ("inlet_cols", C.c_size_t),
+                ("steps", C.c_uint64), ("sample_every", C.c_uint64), ("alpha", C.c_float),
+                ("bx", C.c_size_t), ("by", C.c_size_t)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "cancelled", "active", "queued",
+                                          "ticks", "kernel_launches", "site_updates",
+                                          "bytes_in_use", "peak_bytes", "peak_active")]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 
 class LgxError(RuntimeError):
@@ -87,6 +105,18 @@ def lib():
         _sig(L, "lgx_timing_elapsed", vp, C.c_int, C.c_int, C.POINTER(C.c_float))
         _sig(L, "lgx_verify_circuit", C.c_int, u32p, sz)
         _sig(L, "lgx_select_device", C.c_int)
+        _sig(L, "lgx_server_create", sz, sz, C.POINTER(vp))
+        _sig(L, "lgx_server_destroy", vp)
+        _sig(L, "lgx_server_submit", vp, C.POINTER(Request), C.POINTER(C.c_uint64))
+        _sig(L, "lgx_server_poll", vp, C.c_uint64, C.POINTER(C.c_int))
+        _sig(L, "lgx_server_wait", vp, C.c_uint64, C.c_double, C.POINTER(C.c_int))
+        _sig(L, "lgx_server_result", vp, C.c_uint64, f32p, f32p, f32p, f32p, i32p, i32p, i32p,
+             i32p, sz, C.POINTER(C.c_uint64), C.POINTER(C.c_double))
+        _sig(L, "lgx_server_cancel", vp, C.c_uint64)
+        _sig(L, "lgx_server_release", vp, C.c_uint64)
+        _sig(L, "lgx_server_get_stats", vp, C.POINTER(ServerStats))
+        _sig(L, "lgx_server_inject_alloc_failure", vp, C.c_int)
+        _sig(L, "lgx_request_device_bytes", C.POINTER(Request), C.POINTER(C.c_size_t))
         _sig(L, "lgx_batch_create", C.POINTER(vp), sz, C.POINTER(vp))
         _sig(L, "lgx_batch_destroy", vp)
         _sig(L, "lgx_batch_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
@@ -296,6 +326,89 @@ class Batch:
         ms = C.c_float()
         _check(lib().lgx_batch_timing_elapsed(self._h, int(a), int(b), C.byref(ms)))
         return float(ms.value)
+
+
+class Server:
+    """A request loop with continuous batching (lgx_server_*).  Requests are
+    admitted against a device-memory budget, resident lattices advance
+    together, and only the moments come back."""
+
+    def __init__(self, budget_bytes: int, max_active: int = 256):
+        self._h = vp()
+        _check(lib().lgx_server_create(int(budget_bytes), int(max_active), C.byref(self._h)))
+        self._shape = {}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().lgx_server_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, cells, w, h, rest, seed, density, inflow, inlet_cols, steps, sample_every,
+               alpha, bx, by) -> int:
+        c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+        q = Request(w, h, int(bool(rest)), _u64(seed), _p(c, C.c_uint8), float(density),
+                    float(inflow[0]), float(inflow[1]), int(inlet_cols), int(steps),
+                    int(sample_every), float(alpha), int(bx), int(by))
+        rid = C.c_uint64()
+        _check(lib().lgx_server_submit(self._h, C.byref(q), C.byref(rid)))
+        self._shape[int(rid.value)] = (w // bx) * (h // by)
+        return int(rid.value)
+
+    def submit_workload(self, wl) -> int:
+        return self.submit(wl.cells, wl.w, wl.h, wl.rest, wl.seed, wl.density, wl.inflow,
+                           wl.inlet_cols, wl.steps, wl.sample_every, wl.alpha, wl.block, wl.block)
+
+    def poll(self, rid) -> int:
+        st = C.c_int()
+        _check(lib().lgx_server_poll(self._h, int(rid), C.byref(st)))
+        return st.value
+
+    def wait(self, rid, timeout=-1.0) -> int:
+        st = C.c_int()
+        _check(lib().lgx_server_wait(self._h, int(rid), float(timeout), C.byref(st)))
+        return st.value
+
+    def result(self, rid) -> dict:
+        nb = self._shape[int(rid)]
+        f = [np.zeros(nb, np.float32) for _ in range(4)]
+        m = [np.zeros(nb, np.int32) for _ in range(4)]
+        part = C.c_uint64()
+        lat = C.c_double()
+        _check(lib().lgx_server_result(self._h, int(rid), *[_p(a, C.c_float) for a in f],
+                                       *[_p(a, C.c_int32) for a in m], nb, C.byref(part),
+                                       C.byref(lat)))
+        return dict(ux=f[0], uy=f[1], rho=f[2], solid=f[3], mass=m[0], px2=m[1], py2=m[2],
+                    nsolid=m[3], particles=int(part.value), latency=float(lat.value))
+
+    def cancel(self, rid):
+        _check(lib().lgx_server_cancel(self._h, int(rid)))
+
+    def release(self, rid):
+        _check(lib().lgx_server_release(self._h, int(rid)))
+        self._shape.pop(int(rid), None)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().lgx_server_get_stats(self._h, C.byref(st)))
+        return {n: int(getattr(st, n)) for n, _ in ServerStats._fields_}
+
+    @staticmethod
+    def request_bytes(wl) -> int:
+        """Device memory the workload occupies while resident."""
+        q = Request(wl.w, wl.h, int(bool(wl.rest)), 0, None, 0.0, 0.0, 0.0, int(wl.inlet_cols),
+                    int(wl.steps), int(wl.sample_every), 1.0, int(wl.block), int(wl.block))
+        out = C.c_size_t()
+        _check(lib().lgx_request_device_bytes(C.byref(q), C.byref(out)))
+        return int(out.value)
+
+    def inject_alloc_failure(self, count: int):
+        _check(lib().lgx_server_inject_alloc_failure(self._h, int(count)))
 
 
 # ---- host-side setup (src/lattice.rs, src/hex.rs, src/transport.rs) --------
