@@ -119,6 +119,37 @@ int lgx_verify_circuit(int rest_particles, uint32_t *out, size_t n);
  * 2 = funnel shift, 3 = add, 4 = high-half multiply.  The denominators of the step's integer roofline. */
 int lgx_probe_int_rate(int op, double *ops_per_s);
 
+/* ---- one step with no allocation ------------------------------------------ */
+
+/* No counterpart in the reference.  One step of a lattice whose buffers the
+ * caller owns, for callers that cannot let a library allocate device memory:
+ * hosts that hand out every buffer from their own arena, work being recorded
+ * into a CUDA graph (where cudaMalloc is not allowed), and loops that cannot
+ * afford the synchronisation cudaMalloc/cudaFree imply.  Buffers, all device
+ * memory: planes_in / planes_out hold 7 planes of ceil(w/32)*h words each,
+ * plane-major, bit k of word y*ceil(w/32)+j being column 32j+k (planes_out
+ * receives the step; it must not alias planes_in); solid has one plane of the
+ * same shape, anysolid one bit per word of it (bit g%32 of word g/32 set when
+ * solid word g is non-zero).  thresh are the inflow's seven 24-bit thresholds
+ * (lgx_equilibrium_thresholds), read only when inlet_cols > 0; seed and steps
+ * (steps taken before this one) key the draws as lgx_advance does.  The work
+ * is enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the
+ * call returns without waiting.
+ *
+ * The inflow's per-step draws, h * ceil(inlet_cols/32) * 7 words, go to one
+ * scratch array of 262144 words (1 MiB) compiled into the library and held
+ * by every device that loads it; larger inflows are refused with
+ * LGX_ERR_ARG.  Every call shares that array and overwrites it completely
+ * before reading it, so calls whose work overlaps on the GPU (on different
+ * streams, or on different host threads) race and must be ordered by the
+ * caller.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture. */
+int lgx_step_planes_noalloc(const uint32_t *planes_in, uint32_t *planes_out,
+                            const uint32_t *solid, const uint32_t *anysolid, size_t w, size_t h,
+                            int rest_particles, size_t inlet_cols, const uint32_t thresh[7],
+                            uint64_t seed, uint64_t steps, void *stream);
+
 /* ---- batches: many lattices advanced together ---------------------------- */
 
 /* A batch borrows lattices made with lgx_create (planes, fields, inlets) and

@@ -1,0 +1,123 @@
+// lgx_noalloc.cu -- one lattice step that allocates no memory.
+//
+// Some callers cannot let a library call cudaMalloc behind their back: a host
+// engine that carves every device buffer out of one arena it sized at start-up
+// (and treats any other allocation as a bug), code that is recording work into
+// a CUDA graph, where allocation calls are not allowed, and loops that cannot
+// afford the implicit device synchronisation cudaMalloc and cudaFree bring.
+// For them lgx_step_planes_noalloc advances a lattice whose buffers the caller
+// owns, and keeps the one piece of scratch the step needs -- the inflow's
+// Bernoulli words for the step, h x ceil(inlet_cols / 32) x 7 words -- in a
+// fixed array compiled into this library instead of a per-call allocation.
+//
+// The array is a file-scope __device__ variable, so every GPU that loads the
+// library holds it (kScratchWords words, 1 MiB) until the process exits.  Host
+// code cannot use the array's name as a device address; the first call on each
+// device looks the address up with cudaGetSymbolAddress while that device is
+// current, and later calls reuse it.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/lgx.h"
+#include "lgx_internal.hpp"
+
+namespace {
+
+// Scratch capacity in 32-bit words: h * ceil(inlet_cols / 32) * 7 must fit.
+constexpr size_t kScratchWords = 262144;  // 1 MiB
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kScratchWords];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once).
+int scratch_address(int dev, uint32_t** out) {
+  std::lock_guard<std::mutex> g(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      lgx::set_error(std::string("lgx_step_planes_noalloc: cudaGetSymbolAddress: ") +
+                     cudaGetErrorString(e));
+      return LGX_ERR_CUDA;
+    }
+    g_scratch_addr[dev] = p;
+  }
+  *out = (uint32_t*)g_scratch_addr[dev];
+  return LGX_OK;
+}
+
+}  // namespace
+
+extern "C" int lgx_step_planes_noalloc(const uint32_t* planes_in, uint32_t* planes_out,
+                                       const uint32_t* solid, const uint32_t* anysolid,
+                                       size_t w, size_t h, int rest_particles,
+                                       size_t inlet_cols, const uint32_t thresh[7],
+                                       uint64_t seed, uint64_t steps, void* stream) {
+  if (!planes_in || !planes_out || !solid || !anysolid || planes_in == planes_out) {
+    lgx::set_error("lgx_step_planes_noalloc: null or aliased buffers");
+    return LGX_ERR_ARG;
+  }
+  if (h % 2 != 0 || w <= 4 || h <= 4 || ((w + 31) / 32) * h * 7 >= (1ull << 32)) {
+    lgx::set_error("lgx_step_planes_noalloc: h must be even, w > 4, h > 4, and the lattice "
+                   "within 32-bit word indices");
+    return LGX_ERR_ARG;
+  }
+  const lgx::Dims dm = lgx::make_dims((uint32_t)w, (uint32_t)h, (uint32_t)inlet_cols);
+  const size_t need = (size_t)dm.h * dm.iw * 7;
+  if (need > kScratchWords) {
+    lgx::set_error("lgx_step_planes_noalloc: the inflow needs " + std::to_string(need) +
+                   " scratch words (h * ceil(inlet_cols / 32) * 7), more than the " +
+                   std::to_string(kScratchWords) + " this entry point holds");
+    return LGX_ERR_ARG;
+  }
+  if (dm.iw && !thresh) {
+    lgx::set_error("lgx_step_planes_noalloc: an inflow needs its seven thresholds");
+    return LGX_ERR_ARG;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    lgx::set_error("lgx_step_planes_noalloc: no usable current device");
+    return LGX_ERR_NO_DEVICE;
+  }
+  uint32_t* scratch = nullptr;
+  const int rc = scratch_address(dev, &scratch);  // first call on this device: the lookup
+  if (rc) return rc;
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (dm.iw) {
+    // Every word the step reads is written here first; nothing needs zeroing.
+    lgx::InletArgs ia;
+    ia.out = scratch;
+    ia.dm = dm;
+    ia.seed = seed;
+    ia.steps = steps;
+    ia.nsteps = 1;
+    for (int d = 0; d < 7; ++d) ia.thresh[d] = thresh[d];
+    e = lgx::launch_inlet(ia, st);
+    if (e != cudaSuccess) {
+      lgx::set_error(std::string("lgx_step_planes_noalloc: ") + cudaGetErrorString(e));
+      return LGX_ERR_CUDA;
+    }
+  }
+  lgx::StepArgs sa;
+  sa.a = planes_in;
+  sa.b = planes_out;
+  sa.solid = solid;
+  sa.anysolid = anysolid;
+  sa.inlet = dm.iw ? scratch : nullptr;
+  sa.dm = dm;
+  sa.seed = seed;
+  sa.steps = steps;
+  e = lgx::launch_step(sa, rest_particles != 0, st);
+  if (e != cudaSuccess) {
+    lgx::set_error(std::string("lgx_step_planes_noalloc: ") + cudaGetErrorString(e));
+    return LGX_ERR_CUDA;
+  }
+  return LGX_OK;
+}

@@ -117,6 +117,8 @@ def lib():
         _sig(L, "lgx_server_get_stats", vp, C.POINTER(ServerStats))
         _sig(L, "lgx_server_inject_alloc_failure", vp, C.c_int)
         _sig(L, "lgx_request_device_bytes", C.POINTER(Request), C.POINTER(C.c_size_t))
+        _sig(L, "lgx_step_planes_noalloc", vp, vp, vp, vp, sz, sz, C.c_int, sz, u32p,
+             C.c_uint64, C.c_uint64, vp)
         _sig(L, "lgx_batch_create", C.POINTER(vp), sz, C.POINTER(vp))
         _sig(L, "lgx_batch_destroy", vp)
         _sig(L, "lgx_batch_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
