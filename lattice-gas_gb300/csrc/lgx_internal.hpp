@@ -20,6 +20,9 @@ struct Dims {
   uint32_t tail;      // valid-bit mask of the last word of a row
   uint32_t iw;        // words of a row the inlet touches, ceil(inlet_cols / 32)
   uint32_t inlet_cols;
+  // g / wpr == (t + ((g - t) >> div_s1)) >> div_s2 with t = mulhi(g, div_m), for
+  // every 32-bit g (the round-up multiply-shift method for unsigned division)
+  uint32_t div_m, div_s1, div_s2;
 };
 
 Dims make_dims(uint32_t w, uint32_t h, uint32_t inlet_cols);

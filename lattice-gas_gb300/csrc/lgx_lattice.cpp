@@ -36,6 +36,11 @@ Dims make_dims(uint32_t w, uint32_t h, uint32_t inlet_cols) {
   d.tail = (d.lastbit == 31u) ? 0xffffffffu : ((1u << (d.lastbit + 1u)) - 1u);
   d.inlet_cols = std::min(inlet_cols, w);
   d.iw = (d.inlet_cols + 31u) / 32u;
+  uint32_t l = 0;  // ceil(log2(wpr))
+  while ((1ull << l) < d.wpr) ++l;
+  d.div_m = (uint32_t)(((1ull << 32) * ((1ull << l) - d.wpr)) / d.wpr + 1u);
+  d.div_s1 = l < 1u ? l : 1u;
+  d.div_s2 = l > 1u ? l - 1u : 0u;
   return d;
 }
 

@@ -49,7 +49,8 @@ __device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
                                           const uint32_t* __restrict__ inlet, const Dims& dm,
                                           const Draws& s, uint32_t g, bool live) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t y = g / dm.wpr;
+  const uint32_t t = __umulhi(g, dm.div_m);
+  const uint32_t y = (t + ((g - t) >> dm.div_s1)) >> dm.div_s2;  // g / wpr
   const uint32_t j = g - y * dm.wpr;
   const bool odd = y & 1u;
   const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
@@ -102,10 +103,19 @@ __device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
   uint32_t o[7];
   collide<REST>(n, s, o);
 
+  // Obstacle words are rare.  A warp covers the 32 words g & ~31 .. g | 31, whose
+  // summary bits are one anysolid word, so the whole warp skips the solid
+  // load and the bounce-back select together when that word is zero.
+  const uint32_t any = __ldg(anysolid + (g >> 5));
   uint32_t sm = 0u;
-  if ((__ldg(anysolid + (g >> 5)) >> (g & 31u)) & 1u) sm = __ldg(solid + g);
   uint32_t res[7];
-  walls(n, o, sm, res);
+  if (any != 0u) {
+    if ((any >> (g & 31u)) & 1u) sm = __ldg(solid + g);
+    walls(n, o, sm, res);
+  } else {
+#pragma unroll
+    for (int d = 0; d < 7; ++d) res[d] = o[d];
+  }
 
   if (j < dm.iw) {  // inflow re-seed of the leftmost columns (src/gpu.rs:296-306)
     const uint32_t span = min(dm.inlet_cols - j * 32u, 32u);
@@ -116,10 +126,13 @@ __device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
     for (int d = 0; d < 7; ++d) res[d] = (res[d] & ~apply) | (__ldg(bern + d) & apply);
   }
 
-  const uint32_t mask = (j == dm.lastword) ? dm.tail : 0xffffffffu;
+  if (dm.tail != 0xffffffffu && j == dm.lastword) {  // clear the bits past the row's end
+#pragma unroll
+    for (int d = 0; d < 7; ++d) res[d] &= dm.tail;
+  }
   if (live) {
 #pragma unroll
-    for (int d = 0; d < 7; ++d) b[d * S + g] = res[d] & mask;
+    for (int d = 0; d < 7; ++d) b[d * S + g] = res[d];
   }
 }
 
