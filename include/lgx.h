@@ -237,6 +237,36 @@ int lgx_request_device_bytes(const lgx_request *req, size_t *out);
  * failed; those requests end LGX_REQ_FAILED and serving continues. */
 int lgx_server_inject_alloc_failure(lgx_server *s, int count);
 
+/* ---- the reference's byte-per-cell update, on the device ------------------- */
+
+/* The reference's CPU lattice (src/lattice.rs): one byte per cell, collisions
+ * from the padded lookup table with one xorshift64* generator per band of
+ * ceil(h / threads) rows, the inflow re-seeded from one serial generator each
+ * step.  The same random stream as the reference's CPU path, so its golden
+ * checksums (tests/golden.rs) reproduce bit for bit; the bitplane lattice
+ * above draws a different (counter-based) stream, as the reference's GPU path
+ * does.  `threads` only fixes the band structure of the stream. */
+typedef struct lgx_byte_lattice lgx_byte_lattice;
+/* Lattice::new (src/lattice.rs:127-152). */
+int lgx_byte_create(size_t w, size_t h, float density, float ux, float uy, size_t inlet_cols,
+                    int rest_particles, size_t threads, uint64_t seed, lgx_byte_lattice **out);
+int lgx_byte_destroy(lgx_byte_lattice *lat);
+/* Cells (with SOLID_BIT on obstacles); n must be w*h. */
+int lgx_byte_load(lgx_byte_lattice *lat, const uint8_t *cells, size_t n);
+/* Lattice::restart (src/lattice.rs:188-193). */
+int lgx_byte_restart(lgx_byte_lattice *lat, const uint8_t *cells, size_t n, uint64_t seed);
+int lgx_byte_store(lgx_byte_lattice *lat, uint8_t *cells, size_t n);
+/* Lattice::advance (src/lattice.rs:222-264, with apply_inlet 270-285). */
+int lgx_byte_advance(lgx_byte_lattice *lat, uint64_t n);
+/* Field::new / Field::sample (src/render.rs:35-120) on the device, and the copy out. */
+int lgx_byte_attach_field(lgx_byte_lattice *lat, size_t bx, size_t by);
+int lgx_byte_sample_field(lgx_byte_lattice *lat, float alpha);
+int lgx_byte_read_field(lgx_byte_lattice *lat, float *ux, float *uy, float *rho, float *sol,
+                        size_t n_blocks);
+/* Lattice::total_particles (src/lattice.rs:299-312). */
+int lgx_byte_total_particles(lgx_byte_lattice *lat, uint64_t *out);
+int lgx_byte_steps(lgx_byte_lattice *lat, uint64_t *out);
+
 /* ---- host-side lattice setup (src/lattice.rs, src/hex.rs) ---------------- */
 
 /* Equilibrium::new(..).thresholds() (src/lattice.rs:72-92): 24-bit thresholds,

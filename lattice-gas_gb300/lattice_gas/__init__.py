@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblgx.so")
 
-__all__ = ["GpuLattice", "Batch", "Server", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
+__all__ = ["GpuLattice", "Lattice", "Batch", "Server", "Field", "LgxError", "lib", "thresholds", "init_equilibrium",
            "add_box", "add_circle", "shear_wave", "verify_circuit", "SQRT3_2"]
 
 SQRT3_2 = np.float32(0.8660254)
@@ -119,6 +119,18 @@ def lib():
         _sig(L, "lgx_request_device_bytes", C.POINTER(Request), C.POINTER(C.c_size_t))
         _sig(L, "lgx_step_planes_noalloc", vp, vp, vp, vp, sz, sz, C.c_int, sz, u32p,
              C.c_uint64, C.c_uint64, vp)
+        _sig(L, "lgx_byte_create", sz, sz, C.c_float, C.c_float, C.c_float, sz, C.c_int, sz,
+             C.c_uint64, C.POINTER(vp))
+        _sig(L, "lgx_byte_destroy", vp)
+        _sig(L, "lgx_byte_load", vp, u8p, sz)
+        _sig(L, "lgx_byte_restart", vp, u8p, sz, C.c_uint64)
+        _sig(L, "lgx_byte_store", vp, u8p, sz)
+        _sig(L, "lgx_byte_advance", vp, C.c_uint64)
+        _sig(L, "lgx_byte_attach_field", vp, sz, sz)
+        _sig(L, "lgx_byte_sample_field", vp, C.c_float)
+        _sig(L, "lgx_byte_read_field", vp, f32p, f32p, f32p, f32p, sz)
+        _sig(L, "lgx_byte_total_particles", vp, C.POINTER(C.c_uint64))
+        _sig(L, "lgx_byte_steps", vp, C.POINTER(C.c_uint64))
         _sig(L, "lgx_batch_create", C.POINTER(vp), sz, C.POINTER(vp))
         _sig(L, "lgx_batch_destroy", vp)
         _sig(L, "lgx_batch_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
@@ -284,6 +296,71 @@ class GpuLattice:
         ms = C.c_float()
         _check(lib().lgx_timing_elapsed(self._h, int(a), int(b), C.byref(ms)))
         return float(ms.value)
+
+
+class Lattice:
+    """The reference's byte-per-cell lattice (src/lattice.rs), on the device:
+    the CPU path's own random stream, bands of ceil(h / threads) rows."""
+
+    def __init__(self, w, h, density, inflow, inlet_cols, rest_particles, threads, seed):
+        self.w, self.h = int(w), int(h)
+        self._h = vp()
+        _check(lib().lgx_byte_create(self.w, self.h, float(density), float(inflow[0]),
+                                     float(inflow[1]), int(inlet_cols), int(bool(rest_particles)),
+                                     int(threads), _u64(seed), C.byref(self._h)))
+        self._field = None
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().lgx_byte_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, cells):
+        c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+        _check(lib().lgx_byte_load(self._h, _p(c, C.c_uint8), c.size))
+
+    def restart(self, cells, seed):
+        c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+        _check(lib().lgx_byte_restart(self._h, _p(c, C.c_uint8), c.size, _u64(seed)))
+
+    def store(self) -> np.ndarray:
+        out = np.zeros(self.w * self.h, np.uint8)
+        _check(lib().lgx_byte_store(self._h, _p(out, C.c_uint8), out.size))
+        return out
+
+    def advance(self, n):
+        _check(lib().lgx_byte_advance(self._h, int(n)))
+
+    def attach_field(self, bx, by):
+        _check(lib().lgx_byte_attach_field(self._h, int(bx), int(by)))
+        self._field = (int(bx), int(by), self.w // int(bx), self.h // int(by))
+
+    def sample_field(self, alpha):
+        _check(lib().lgx_byte_sample_field(self._h, float(alpha)))
+
+    def read_field(self) -> Field:
+        bx, by, bw, bh = self._field
+        f = Field(self.w, self.h, bx, by)
+        _check(lib().lgx_byte_read_field(self._h, _p(f.ux, C.c_float), _p(f.uy, C.c_float),
+                                         _p(f.rho, C.c_float), _p(f.solid, C.c_float), bw * bh))
+        return f
+
+    def total_particles(self) -> int:
+        v = C.c_uint64()
+        _check(lib().lgx_byte_total_particles(self._h, C.byref(v)))
+        return int(v.value)
+
+    @property
+    def steps(self) -> int:
+        v = C.c_uint64()
+        _check(lib().lgx_byte_steps(self._h, C.byref(v)))
+        return int(v.value)
 
 
 class Batch:

@@ -1,0 +1,90 @@
+"""The reference's byte-per-cell update on the device (lgx_byte_*): its golden
+tests (tests/golden.rs) through the engine, bit for bit, and agreement with the
+oracle's Lattice::step on other sizes, thread bands, obstacles and inflows.
+Needs a GPU."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden_byte.json")))
+DENSITY = np.float32(float(GOLD["constants"]["DENSITY"]))
+SPEED = np.float32(float(GOLD["constants"]["SPEED"]))
+SEED = int(GOLD["constants"]["SEED"], 16)
+BLOCK = int(GOLD["constants"]["BLOCK"])
+
+
+def golden_cells(LG, c):
+    """tests/golden.rs:76-86 with the engine's own host setup."""
+    w, h = c["w"], c["h"]
+    cells = np.zeros(w * h, np.uint8)
+    if c["plate"]:
+        yc = np.float32(h) * LG.SQRT3_2 / np.float32(2.0)
+        x0 = np.float32(w) / np.float32(5.0)
+        LG.add_box(cells, w, h, x0, x0 + np.float32(3.0), yc - np.float32(12.0),
+                   yc + np.float32(12.0))
+    LG.init_equilibrium(cells, DENSITY, SPEED, 0.0, c["rest"], SEED)
+    return cells
+
+
+@pytest.mark.parametrize("case", GOLD["cases"], ids=[c["name"] for c in GOLD["cases"]])
+def test_golden_output_on_the_device(LG, O, case):
+    g = GOLD["golden"][case["name"]]
+    lat = LG.Lattice(case["w"], case["h"], DENSITY, (SPEED, 0.0), case["inlet"], case["rest"],
+                     case["threads"], SEED)
+    lat.load(golden_cells(LG, case))
+    lat.advance(case["steps"])
+    cells = lat.store()
+    assert O.fnv1a(cells) == int(g["cells"], 16)
+    lat.attach_field(BLOCK, BLOCK)
+    lat.sample_field(1.0)
+    f = lat.read_field()
+    fb = b"".join(a.astype("<f4").tobytes() for a in (f.ux, f.uy, f.rho, f.solid))
+    assert O.fnv1a(fb) == int(g["field"], 16)
+    assert O.invariants(cells) == (g["mass"], g["px"], g["py"])
+    assert lat.total_particles() == g["mass"]
+    assert lat.steps == case["steps"]
+
+
+@pytest.mark.parametrize("w,h,threads,inlet,rest", [
+    (300, 64, 3, 40, True),     # partial last segment, two-word inlet
+    (129, 18, 5, 8, True),      # odd width, bands of 4 rows with a short last band
+    (64, 64, 8, 0, False),      # six-direction rule
+    (1000, 40, 1, 70, True),    # one band, many segments per row
+    (48, 48, 48, 0, True),      # a band per row
+])
+def test_device_byte_path_matches_the_oracle(LG, O, w, h, threads, inlet, rest):
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, w / 3.0, h * 0.4, min(w, h) / 6.0)
+    LG.init_equilibrium(cells, 0.3, 0.15, 0.0, rest, 99 + w)
+    seed = 0xFEEDFACE + w
+    lat = LG.Lattice(w, h, 0.3, (0.15, 0.0), inlet, rest, threads, seed)
+    lat.load(cells)
+    ref = O.Lattice(w, h, 0.3, (0.15, 0.0), inlet, rest, threads, seed)
+    ref.set_cells(cells)
+    for n in (1, 13, 60):
+        lat.advance(n)
+        ref.advance(n)
+        got = lat.store()
+        assert np.array_equal(got, ref.cells), "differs in %d cells" % int((got != ref.cells).sum())
+
+
+def test_restart_and_thread_invariance_of_conserved_quantities(LG, O):
+    """tests/golden.rs:262-297 on the device: closed box, 1/2/3/5/8 bands."""
+    for rest in (False, True):
+        expected = None
+        cells = np.zeros(64 * 64, np.uint8)
+        LG.init_equilibrium(cells, DENSITY, SPEED, 0.0, rest, SEED)
+        before = O.invariants(cells)
+        for threads in (1, 2, 3, 5, 8):
+            lat = LG.Lattice(64, 64, DENSITY, (SPEED, 0.0), 0, rest, threads, SEED)
+            lat.restart(cells, SEED)
+            lat.advance(100)
+            after = O.invariants(lat.store())
+            assert after == before
+            if expected is None:
+                expected = after
+            assert after == expected
