@@ -81,8 +81,12 @@ int lgx_advance_sampling(lgx_lattice *lat, uint64_t n, uint64_t sample_every, fl
  * persistent kernel (each block owns a fixed range of words and waits, with a
  * bounded spin, only for the blocks owning the rows next to its own).
  * Results are identical in every mode. */
-enum { LGX_STEP_AUTO = 0, LGX_STEP_SINGLE = 1, LGX_STEP_WAVE = 2 };
+enum { LGX_STEP_AUTO = 0, LGX_STEP_SINGLE = 1, LGX_STEP_WAVE = 2, LGX_STEP_TEMPORAL = 3 };
 int lgx_set_step_mode(lgx_lattice *lat, int mode);
+/* TEMPORAL: runs of k steps (k = 4 or 8, lgx_set_temporal_depth) in one pass
+ * over HBM, the intermediate steps kept in registers (lattices at least 64
+ * words wide; other runs, and steps up to a sampling point, go one at a time). */
+int lgx_set_temporal_depth(lgx_lattice *lat, int k);
 /* GpuLattice::sample_field (src/gpu.rs:710-721). */
 int lgx_sample_field(lgx_lattice *lat, float alpha);
 /* GpuLattice::read_field (src/gpu.rs:725-736): n_blocks must be bw*bh. */

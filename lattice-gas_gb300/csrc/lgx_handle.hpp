@@ -44,6 +44,7 @@ struct lgx_lattice {
   uint64_t launches = 0;     // kernels this handle has launched
   // persistent multi-step kernel
   int step_mode = LGX_STEP_AUTO;
+  uint32_t temporal_depth = 4;  // steps per pass in LGX_STEP_TEMPORAL
   uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
   uint32_t* done = nullptr;  // [wave_grid] published step per CTA
   uint32_t* error = nullptr; // timeout flag

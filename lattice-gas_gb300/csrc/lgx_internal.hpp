@@ -55,6 +55,19 @@ struct WaveArgs {
   uint32_t* error;
 };
 
+// K steps in one pass over HBM (temporal blocking): a -> b after K steps.
+struct TemporalArgs {
+  const uint32_t* a;
+  uint32_t* b;
+  const uint32_t* solid;
+  const uint32_t* anysolid;
+  const uint32_t* inlet;  // [K][h][iw][7] draws of the K steps; null when iw == 0
+  Dims dm;
+  uint64_t seed;
+  uint64_t steps;  // steps taken before the first of the K
+  uint32_t nstrips, nbands, band_rows;
+};
+
 // Inlet Bernoulli words for `nsteps` consecutive steps starting at `steps`,
 // written to out[s][y][jw][d].
 struct InletArgs {
@@ -86,6 +99,10 @@ cudaError_t launch_inlet(const InletArgs& s, cudaStream_t st);
 // one per 32-word chunk).
 cudaError_t wave_grid(bool rest, uint32_t total, uint32_t* grid);
 cudaError_t launch_wave(const WaveArgs& w, bool rest, uint32_t grid, cudaStream_t st);
+// Temporal blocking: supported depths and widths, the tiling, the launch.
+bool temporal_supported(const Dims& dm, uint32_t k);
+void temporal_tiling(const Dims& dm, uint32_t band_rows, TemporalArgs* t);
+cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaStream_t st);
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
                          cudaStream_t st);

@@ -183,6 +183,28 @@ int enqueue_wave(lgx_lattice* lat, uint32_t k) {
   return LGX_OK;
 }
 
+// K steps in one pass (temporal blocking); the caller checked the inlet
+// chunk covers them.
+int enqueue_temporal(lgx_lattice* lat, uint32_t k) {
+  lgx::TemporalArgs ta;
+  ta.a = lat->planes[lat->cur];
+  ta.b = lat->planes[lat->cur ^ 1];
+  ta.solid = lat->solid;
+  ta.anysolid = lat->anysolid;
+  ta.inlet = lat->dm.iw ? lat->inlet + (size_t)(lat->steps - lat->inlet_first) * lat->dm.h *
+                                           lat->dm.iw * 7
+                        : nullptr;
+  ta.dm = lat->dm;
+  ta.seed = lat->seed;
+  ta.steps = lat->steps;
+  lgx::temporal_tiling(lat->dm, 128, &ta);
+  LGX_CUDA(lgx::launch_temporal(ta, lat->rest, k, lat->stream));
+  lat->launches += 1;
+  lat->cur ^= 1;
+  lat->steps += k;
+  return LGX_OK;
+}
+
 int enqueue_single(lgx_lattice* lat) {
   lgx::StepArgs sa;
   sa.a = lat->planes[lat->cur];
@@ -208,11 +230,19 @@ int enqueue_single(lgx_lattice* lat) {
 int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
   uint64_t left = n, since = 0;
   const bool wave = lat->step_mode == LGX_STEP_WAVE;
+  const uint32_t tk = lat->temporal_depth;
+  const bool temporal =
+      lat->step_mode == LGX_STEP_TEMPORAL && lgx::temporal_supported(lat->dm, tk);
   while (left > 0) {
     int rc = ensure_inlet(lat, left);
     if (rc) return rc;
     uint64_t k = 1;
-    if (wave) {
+    const bool fits = left >= tk && (every == 0 || every - since >= tk) &&
+                      (lat->dm.iw == 0 || lat->inlet_first + lat->inlet_valid - lat->steps >= tk);
+    if (temporal && fits) {
+      k = tk;
+      rc = enqueue_temporal(lat, tk);
+    } else if (wave) {
       k = std::min<uint64_t>(left, lgx::kInletChunk);
       if (every > 0) k = std::min<uint64_t>(k, every - since);
       if (lat->dm.iw) k = std::min<uint64_t>(k, lat->inlet_first + lat->inlet_valid - lat->steps);
@@ -413,11 +443,21 @@ int lgx_advance_sampling(lgx_lattice* lat, uint64_t n, uint64_t every, float alp
 }
 
 int lgx_set_step_mode(lgx_lattice* lat, int mode) {
-  if (!lat || (mode != LGX_STEP_AUTO && mode != LGX_STEP_SINGLE && mode != LGX_STEP_WAVE)) {
+  if (!lat || (mode != LGX_STEP_AUTO && mode != LGX_STEP_SINGLE && mode != LGX_STEP_WAVE &&
+               mode != LGX_STEP_TEMPORAL)) {
     lgx::set_error("lgx_set_step_mode: bad handle or mode");
     return LGX_ERR_ARG;
   }
   lat->step_mode = mode;
+  return LGX_OK;
+}
+
+int lgx_set_temporal_depth(lgx_lattice* lat, int k) {
+  if (!lat || (k != 4 && k != 8)) {
+    lgx::set_error("lgx_set_temporal_depth: depth must be 4 or 8");
+    return LGX_ERR_ARG;
+  }
+  lat->temporal_depth = (uint32_t)k;
   return LGX_OK;
 }
 

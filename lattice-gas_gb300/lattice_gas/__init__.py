@@ -95,6 +95,7 @@ def lib():
         _sig(L, "lgx_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
         _sig(L, "lgx_sample_field", vp, C.c_float)
         _sig(L, "lgx_set_step_mode", vp, C.c_int)
+        _sig(L, "lgx_set_temporal_depth", vp, C.c_int)
         _sig(L, "lgx_read_field", vp, f32p, f32p, f32p, f32p, sz)
         _sig(L, "lgx_read_block_sums", vp, i32p, i32p, i32p, i32p, sz)
         _sig(L, "lgx_total_particles", vp, C.POINTER(C.c_uint64))
@@ -237,10 +238,13 @@ class GpuLattice:
     def advance_sampling(self, n, sample_every, alpha):
         _check(lib().lgx_advance_sampling(self._h, int(n), int(sample_every), float(alpha)))
 
-    STEP_AUTO, STEP_SINGLE, STEP_WAVE = 0, 1, 2
+    STEP_AUTO, STEP_SINGLE, STEP_WAVE, STEP_TEMPORAL = 0, 1, 2, 3
 
     def set_step_mode(self, mode: int):
         _check(lib().lgx_set_step_mode(self._h, int(mode)))
+
+    def set_temporal_depth(self, k: int):
+        _check(lib().lgx_set_temporal_depth(self._h, int(k)))
 
     def sample_field(self, alpha):
         _check(lib().lgx_sample_field(self._h, float(alpha)))
