@@ -1,0 +1,54 @@
+"""A fixed run of one workload, for profilers (ncu) to attach to.
+
+    python lattice-gas_gb300/lattice_gas/profile_run.py --case wake --steps 60
+    python lattice-gas_gb300/lattice_gas/profile_run.py --case big --steps 20 --mode 1
+
+Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
+16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
+`sweep` (the 64-lattice transport sweep as one batch).  --mode picks the step
+launch mode (1 one launch per step, 2 persistent waves, 3 temporal blocking).
+"""
+import argparse
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+import lattice_gas as LG  # noqa: E402
+from lattice_gas import workloads as W  # noqa: E402
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="wake", choices=["wake", "big", "sweep"])
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--mode", type=int, default=1)
+    ap.add_argument("--depth", type=int, default=4)
+    a = ap.parse_args()
+    if a.case == "sweep":
+        wls = W.transport_sweep(steps=a.steps)
+        lats = []
+        for wl in wls:
+            g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+            g.attach_field(wl.block, wl.block)
+            g.load(wl.cells)
+            lats.append(g)
+        b = LG.Batch(lats)
+        b.advance_sampling(a.steps, 50, 1.0)
+        print("sweep: %d lattices, %d steps" % (len(lats), a.steps))
+        return
+    wl = W.wake_run() if a.case == "wake" else W.roofline_case(w=16384, h=8192, n_circles=50)
+    g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+    g.set_step_mode(a.mode)
+    if a.mode == 3:
+        g.set_temporal_depth(a.depth)
+    g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)
+    g.attach_field(wl.block, wl.block)
+    g.load(wl.cells)
+    g.advance_sampling(a.steps, wl.sample_every, wl.alpha)
+    print("%s: %d x %d, %d steps, %d particles" % (a.case, wl.w, wl.h, a.steps,
+                                                     g.total_particles()))
+
+
+if __name__ == "__main__":
+    main()
