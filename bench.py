@@ -46,9 +46,17 @@ def peaks():
     return 6800.0, "fallback"
 
 
-# Per-launch DRAM traffic of the step kernel on the wake run, from the ncu
-# capture summarised in profiles/step_wake_run.md (read + write bytes).
-STEP_TRAFFIC_BYTES = None
+# From the ncu capture summarised in profiles/step_wake_run_pipes.md (the wake
+# run's lgx_step_kernel, one launch = one step): DRAM bytes read + written per
+# launch (cold cache under ncu; the 18 MB of planes stay in L2 between steps of
+# a timed run), and the ALU-pipe warp instructions per launch, which do not
+# depend on timing.
+STEP_TRAFFIC_BYTES = 8409344 + 0
+STEP_ALU_WARP_INSTR = 3400515
+# Roofline-case DRAM bytes per site-update, from the 16384 x 8192 capture of the
+# same kernel (118.8 MB read + 73.4 MB written for 134.2 M sites); the full
+# 32768 x 16384 case scales with its sites.
+BIG_DRAM_BYTES_PER_SITE = (118771712 + 73354496) / (16384 * 8192)
 
 
 class ClockSampler:
@@ -257,6 +265,39 @@ def bench_batched(LG, W, steps: int):
     return out
 
 
+def bench_roofline_case(LG, W, steps: int):
+    """The 32768 x 16384 roofline case (200 circles, inflow): one launch per
+    step, and temporal blocking of 4 and 8 steps per pass over HBM."""
+    wl = W.roofline_case()
+    out = {"workload": "roofline case: 32768x16384, 200 circles r 16..64, 8-column inflow, "
+                       "density 0.2; %d steps timed per mode" % steps, "sites": wl.sites}
+    states = {}
+    for mode, k, name in ((1, 0, "single"), (3, 4, "temporal4"), (3, 8, "temporal8")):
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.set_step_mode(mode)
+        if k:
+            g.set_temporal_depth(k)
+        g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)
+        g.load(wl.cells)
+        g.advance(16)
+        g.timing_mark(0)
+        g.advance(steps)
+        g.timing_mark(1)
+        ms = g.timing_elapsed(0, 1) / steps
+        states[name] = g.store()
+        out[name] = {"ms_per_step": round(ms, 4),
+                     "value": round(wl.sites / (ms * 1e-3) / 1e9, 1),
+                     "algorithmic_GBps": round(wl.sites * ALGO_BYTES_PER_SITE / (ms * 1e-3) / 1e9, 1)}
+        g.close()
+    out["single"]["dram_GBps_from_ncu"] = round(
+        wl.sites * BIG_DRAM_BYTES_PER_SITE / (out["single"]["ms_per_step"] * 1e-3) / 1e9, 1)
+    out["bit_exact_temporal_vs_single"] = bool(
+        np.array_equal(states["single"], states["temporal4"]) and
+        np.array_equal(states["single"], states["temporal8"]))
+    out["unit"] = UNIT
+    return out
+
+
 def bench_served(LG, W, n: int, budget: int):
     """The request stream: Poisson arrivals at 200/s, sizes 128x128..4096x2048,
     1k..50k steps, sampling every 50..500 steps with 8..32 blocks, obstacle none
@@ -409,10 +450,13 @@ def run_gb300(args, world, rank, local):
                          "Lattice::step restated in C (oracle/), %d threads"
                          % (nsteps, dt, threads)}
 
-    batched = served = None
+    batched = served = big = None
     if not args.no_patterns:
         batched = bench_batched(LG, W, args.sweep_steps)
         served = bench_served(LG, W, args.requests, args.budget_mib << 20)
+        big = bench_roofline_case(LG, W, args.big_steps)
+    lop3_peak = LG.probe_int_rate(0)
+    alu_achieved = STEP_ALU_WARP_INSTR * 32 / (step_ms * 1e-3)
 
     if rank != 0:
         return 0
@@ -434,7 +478,12 @@ def run_gb300(args, world, rank, local):
                      "traffic": STEP_TRAFFIC_BYTES, "peak_kind": peak_kind,
                      "kernel": "lgx_step_kernel", "step_kernel_us": round(step_ms * 1e3, 3),
                      "algorithmic_bytes_per_launch": wl.sites * ALGO_BYTES_PER_SITE,
-                     "note": "integer-ALU bound; see int_pipe"},
+                     "note": "the step is integer-ALU bound, not HBM bound: see int_pipe",
+                     "int_pipe": {"achieved": round(alu_achieved / 1e12, 2),
+                                  "peak": round(lop3_peak / 1e12, 2), "unit": "Tlane-op/s",
+                                  "frac": round(alu_achieved / lop3_peak, 4),
+                                  "alu_warp_instr_per_launch": STEP_ALU_WARP_INSTR,
+                                  "peak_kind": "measured (lgx_probe_int_rate, lop3)"}},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": wl.sites,
                 "d2h_bytes_per_step": 8 * nb * 4},
         "gpu_launches": launches,
@@ -442,6 +491,7 @@ def run_gb300(args, world, rank, local):
         "cpu_baseline": cpu,
         "batched": batched,
         "served": served,
+        "roofline_case": big,
         "device": g.device_name(),
     }
     print(json.dumps(line), flush=True)
@@ -462,6 +512,7 @@ def main():
     ap.add_argument("--sweep-steps", type=int, default=5000)
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--budget-mib", type=int, default=4096)
+    ap.add_argument("--big-steps", type=int, default=96)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
