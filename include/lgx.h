@@ -66,6 +66,13 @@ int lgx_attach_field(lgx_lattice *lat, size_t bx, size_t by);
 int lgx_load(lgx_lattice *lat, const uint8_t *cells, size_t n);
 /* GpuLattice::restart (src/gpu.rs:616-620): load, then seed = seed, steps = 0. */
 int lgx_restart(lgx_lattice *lat, const uint8_t *cells, size_t n, uint64_t seed);
+/* Lattice::init_equilibrium (src/lattice.rs:197-208) applied to the lattice on the
+ * device, for callers that today run it on the host and then GpuLattice::load:
+ * every fluid cell gets an equilibrium sample for (density, ux, uy) from
+ * Rng::new(seed ^ 0xA5A51234), in row-major cell order; obstacles keep no
+ * particles.  The result equals init_equilibrium on the stored cells followed by
+ * lgx_load.  seed is the host Lattice's seed; steps are unchanged. */
+int lgx_init_equilibrium(lgx_lattice *lat, float density, float ux, float uy, uint64_t seed);
 /* GpuLattice::store (src/gpu.rs:630-652): n must be w*h. */
 int lgx_store(lgx_lattice *lat, uint8_t *cells, size_t n);
 /* GpuLattice::advance (src/gpu.rs:657-659). */
@@ -259,6 +266,9 @@ int lgx_byte_destroy(lgx_byte_lattice *lat);
 int lgx_byte_load(lgx_byte_lattice *lat, const uint8_t *cells, size_t n);
 /* Lattice::restart (src/lattice.rs:188-193). */
 int lgx_byte_restart(lgx_byte_lattice *lat, const uint8_t *cells, size_t n, uint64_t seed);
+/* Lattice::init_equilibrium (src/lattice.rs:197-208) on the device, with the
+ * lattice's own density, inflow and seed. */
+int lgx_byte_init_equilibrium(lgx_byte_lattice *lat);
 int lgx_byte_store(lgx_byte_lattice *lat, uint8_t *cells, size_t n);
 /* Lattice::advance (src/lattice.rs:222-264, with apply_inlet 270-285). */
 int lgx_byte_advance(lgx_byte_lattice *lat, uint64_t n);

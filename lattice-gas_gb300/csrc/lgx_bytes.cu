@@ -28,43 +28,18 @@
 
 #include "../../include/lgx.h"
 #include "lgx_internal.hpp"
+#include "lgx_rng.cuh"
 
 namespace {
 
+using lgx::jump_ahead;
+using lgx::rng_seed;
+using lgx::xorshift;
+
 constexpr uint32_t kSeg = 128;     // cells per thread segment
-constexpr int kJumps = 32;         // M^(2^i), i < 32: offsets below 2^32
+constexpr int kJumps = 32;         // the first 32 jump matrices: offsets below 2^32
 constexpr uint8_t kSolid = 0x80, kRest = 0x40;
-constexpr uint64_t kMul = 0x2545F4914F6CDD1Dull;
-
-__host__ __device__ __forceinline__ uint64_t rng_seed(uint64_t seed) {
-  uint64_t s = seed ^ 0x9E3779B97F4A7C15ull;
-  s = (s ^ (s >> 30)) * 0xBF58476D1CE4E5B9ull;
-  s = (s ^ (s >> 27)) * 0x94D049BB133111EBull;
-  return (s ^ (s >> 31)) | 1ull;
-}
-
-__host__ __device__ __forceinline__ uint64_t xorshift(uint64_t x) {
-  x ^= x << 13;
-  x ^= x >> 7;
-  x ^= x << 17;
-  return x;
-}
-
-// x <- M^k x, with jump[i * 64 + j] the j-th column of M^(2^i).
-__device__ __forceinline__ uint64_t jump_ahead(uint64_t x, uint32_t k, const uint64_t* jump) {
-  for (int i = 0; k; ++i, k >>= 1) {
-    if (!(k & 1u)) continue;
-    const uint64_t* col = jump + i * 64;
-    uint64_t r = 0, v = x;
-    while (v) {
-      const int j = __ffsll((long long)v) - 1;
-      r ^= col[j];
-      v &= v - 1;
-    }
-    x = r;
-  }
-  return x;
-}
+constexpr uint64_t kMul = lgx::kRngMul;
 
 struct ByteStepArgs {
   const uint8_t* old;
@@ -160,18 +135,7 @@ __global__ void __launch_bounds__(128) lgx_byte_inlet_kernel(const ByteInletArgs
   uint8_t* row = p.cells + (size_t)y * p.w;
   for (uint32_t x = 0; x < p.cols; ++x) {
     if (row[x] & kSolid) continue;
-    uint8_t s = 0;
-    for (int d = 0; d < 6; d += 2) {
-      st = xorshift(st);
-      const uint64_t v = st * kMul;
-      s |= (uint8_t)(((uint32_t)(v >> 40) < p.t[d]) << d);
-      s |= (uint8_t)(((((uint32_t)(v >> 16)) & 0xFFFFFFu) < p.t[d + 1]) << (d + 1));
-    }
-    if (p.rest) {
-      st = xorshift(st);
-      if ((uint32_t)((st * kMul) >> 40) < p.t[6]) s |= kRest;
-    }
-    row[x] = s;
+    row[x] = lgx::equilibrium_sample(p.t, p.rest != 0, st);
   }
 }
 
@@ -215,21 +179,6 @@ void build_table(bool rest, std::vector<uint8_t>* data, uint32_t* stride) {
     for (uint32_t k = 0; k < st; ++k) (*data)[(size_t)s * st + k] = g[k % g.size()];
   }
   *stride = st;
-}
-
-// Host: columns of M^(2^i) for the xorshift64 state update.
-std::vector<uint64_t> build_jumps() {
-  auto apply = [](const uint64_t* cols, uint64_t v) {
-    uint64_t r = 0;
-    for (int j = 0; j < 64; ++j)
-      if (v >> j & 1) r ^= cols[j];
-    return r;
-  };
-  std::vector<uint64_t> J((size_t)kJumps * 64);
-  for (int j = 0; j < 64; ++j) J[j] = xorshift(1ull << j);
-  for (int i = 1; i < kJumps; ++i)
-    for (int j = 0; j < 64; ++j) J[(size_t)i * 64 + j] = apply(&J[(size_t)(i - 1) * 64], J[(size_t)(i - 1) * 64 + j]);
-  return J;
 }
 
 int cuda_fail(cudaError_t e, const char* what) {
@@ -363,7 +312,8 @@ int lgx_byte_create(size_t w, size_t h, float density, float ux, float uy, size_
   L->dm = lgx::make_dims(L->w, L->h, 0);
   std::vector<uint8_t> table;
   build_table(L->rest, &table, &L->stride);
-  const std::vector<uint64_t> jumps = build_jumps();
+  std::vector<uint64_t> jumps = lgx::build_jumps();
+  jumps.resize((size_t)kJumps * 64);
   const size_t cells = w * h, total = L->dm.total;
   cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&L->cells[0], cells);
@@ -419,6 +369,25 @@ int lgx_byte_restart(lgx_byte_lattice* L, const uint8_t* cells, size_t n, uint64
   if (rc) return rc;
   L->seed = seed;
   L->steps = 0;
+  return LGX_OK;
+}
+
+// Lattice::init_equilibrium (src/lattice.rs:197-208), on the device.  The
+// obstacles stay where they are, so the draw offsets need no update.
+int lgx_byte_init_equilibrium(lgx_byte_lattice* L) {
+  if (!L) {
+    lgx::set_error("null lattice");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaSetDevice(L->device));
+  lgx::EqFill f{};
+  f.cells = L->cells[L->cur];
+  f.n = (size_t)L->w * L->h;
+  f.seed = L->seed ^ 0xA5A51234ull;
+  f.rest = L->rest;
+  memcpy(f.thresh, L->thresh, sizeof(f.thresh));
+  LGX_CUDA(lgx::launch_equilibrium_fill(f, L->stream));
+  LGX_CUDA(cudaStreamSynchronize(L->stream));
   return LGX_OK;
 }
 

@@ -116,6 +116,23 @@ cudaError_t launch_verify(uint32_t* out, uint32_t n, bool rest, cudaStream_t st)
 
 // Host-side equilibrium thresholds (src/lattice.rs:59-92), f32 without fusion.
 void equilibrium_thresholds(float density, float ux, float uy, bool rest, uint32_t out[7]);
+// The equilibrium fill of Lattice::init_equilibrium (src/lattice.rs:197-208)
+// on the device: every fluid cell (not solid) gets an equilibrium sample from
+// Rng::new(seed), cell order row-major; solid cells get no particles (bytes:
+// exactly the solid bit).  Target: the seven planes of a bitplane lattice, or
+// n byte cells (16-byte aligned) when `planes` is null.
+struct EqFill {
+  uint32_t* planes;
+  const uint32_t* solid;
+  Dims dm;
+  uint8_t* cells;
+  size_t n;
+  uint64_t seed;
+  uint32_t thresh[7];
+  bool rest;
+};
+cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st);
+
 
 void set_error(const std::string& msg);
 

@@ -416,6 +416,22 @@ int lgx_restart(lgx_lattice* lat, const uint8_t* cells, size_t n, uint64_t seed)
   return LGX_OK;
 }
 
+int lgx_init_equilibrium(lgx_lattice* lat, float density, float ux, float uy, uint64_t seed) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  lgx::EqFill f{};
+  f.planes = lat->planes[lat->cur];
+  f.solid = lat->solid;
+  f.dm = lat->dm;
+  f.seed = seed ^ 0xA5A51234ull;  // src/lattice.rs:198
+  f.rest = lat->rest;
+  lgx::equilibrium_thresholds(density, ux, uy, lat->rest, f.thresh);
+  LGX_CUDA(lgx::launch_equilibrium_fill(f, lat->stream));
+  lat->launches += 2;
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
 int lgx_store(lgx_lattice* lat, uint8_t* cells, size_t n) {
   int rc = check_lat(lat);
   if (rc) return rc;

@@ -91,6 +91,7 @@ def lib():
         _sig(L, "lgx_load", vp, u8p, sz)
         _sig(L, "lgx_restart", vp, u8p, sz, C.c_uint64)
         _sig(L, "lgx_store", vp, u8p, sz)
+        _sig(L, "lgx_init_equilibrium", vp, C.c_float, C.c_float, C.c_float, C.c_uint64)
         _sig(L, "lgx_advance", vp, C.c_uint64)
         _sig(L, "lgx_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
         _sig(L, "lgx_sample_field", vp, C.c_float)
@@ -126,6 +127,7 @@ def lib():
         _sig(L, "lgx_byte_load", vp, u8p, sz)
         _sig(L, "lgx_byte_restart", vp, u8p, sz, C.c_uint64)
         _sig(L, "lgx_byte_store", vp, u8p, sz)
+        _sig(L, "lgx_byte_init_equilibrium", vp)
         _sig(L, "lgx_byte_advance", vp, C.c_uint64)
         _sig(L, "lgx_byte_attach_field", vp, sz, sz)
         _sig(L, "lgx_byte_sample_field", vp, C.c_float)
@@ -232,6 +234,12 @@ class GpuLattice:
         _check(lib().lgx_store(self._h, _p(out, C.c_uint8), out.size))
         return out
 
+    def init_equilibrium(self, density, inflow, seed):
+        """Lattice::init_equilibrium (src/lattice.rs:197-208) on the device: fluid cells
+        get equilibrium samples from Rng::new(seed ^ 0xA5A51234), obstacles stay."""
+        _check(lib().lgx_init_equilibrium(self._h, float(density), float(inflow[0]),
+                                          float(inflow[1]), _u64(seed)))
+
     def advance(self, n):
         _check(lib().lgx_advance(self._h, int(n)))
 
@@ -337,6 +345,10 @@ class Lattice:
         out = np.zeros(self.w * self.h, np.uint8)
         _check(lib().lgx_byte_store(self._h, _p(out, C.c_uint8), out.size))
         return out
+
+    def init_equilibrium(self):
+        """Lattice::init_equilibrium (src/lattice.rs:197-208), on the device."""
+        _check(lib().lgx_byte_init_equilibrium(self._h))
 
     def advance(self, n):
         _check(lib().lgx_byte_advance(self._h, int(n)))
