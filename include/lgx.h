@@ -104,6 +104,18 @@ int lgx_read_field(lgx_lattice *lat, float *ux, float *uy, float *rho, float *so
  * the count of obstacle cells.  n_blocks must be bw*bh. */
 int lgx_read_block_sums(lgx_lattice *lat, int32_t *mass, int32_t *px2, int32_t *py2,
                         int32_t *nsolid, size_t n_blocks);
+/* transport::row_ux (src/transport.rs:87-91) of the lattice as it stands: the mean
+ * x-velocity of each row, WITH_WALLS moments (src/moments.rs:37-74), formed on the
+ * device; the reference stores the whole lattice to the host for it (Sim::cells,
+ * src/sim.rs:100-114).  n must be h. */
+int lgx_row_ux(lgx_lattice *lat, float *ux, size_t n);
+/* transport::column_uy (src/transport.rs:51-84): the mean y-velocity of each
+ * column, 0 for a column without particles.  n must be w. */
+int lgx_column_uy(lgx_lattice *lat, float *uy, size_t n);
+/* New: the exact integer WITH_WALLS moments behind those profiles: rows gets
+ * mass[h] | px2[h] | py2[h] (n_rows = 3h), cols mass[w] | px2[w] | py2[w]
+ * (n_cols = 3w); either may be null. */
+int lgx_line_sums(lgx_lattice *lat, int32_t *rows, size_t n_rows, int32_t *cols, size_t n_cols);
 /* GpuLattice::total_particles (src/gpu.rs:740-754), counted in 64 bits. */
 int lgx_total_particles(lgx_lattice *lat, uint64_t *out);
 /* GpuLattice::steps (pub field, src/gpu.rs:471). */
@@ -181,6 +193,27 @@ int lgx_batch_advance(lgx_batch *b, uint64_t n);
 int lgx_batch_launch_count(lgx_batch *b, uint64_t *kernels, uint64_t *graphs);
 int lgx_batch_timing_mark(lgx_batch *b, int slot);
 int lgx_batch_timing_elapsed(lgx_batch *b, int a, int c, float *ms);
+
+/* ---- transport coefficients (src/transport.rs) ---------------------------- */
+#define LGX_TRANSPORT_SAMPLES 20
+/* transport::Transport (src/transport.rs:31-37) and what its fits were made from. */
+typedef struct lgx_transport {
+  float nu;                 /* kinematic viscosity, lattice units */
+  float g;                  /* advection factor */
+  uint64_t window_nu;       /* decay windows, steps (decay_window, transport.rs:131-150) */
+  uint64_t window_g;
+  float u_actual;           /* realised mean speed of the advection start */
+  double mode_nu[2 * LGX_TRANSPORT_SAMPLES];  /* averaged mode (a, b) per sample */
+  double mode_g[2 * LGX_TRANSPORT_SAMPLES];
+} lgx_transport;
+/* transport::measure(density, rest, threads, seed, size, gpu = true) (src/transport.rs:
+ * 291-319) for each of n densities, out[i] for densities[i]; n = 1 is measure, a range
+ * of densities is main.rs's density scan (src/main.rs:549-560).  All realisations of
+ * all measurements run as one batch on the current device, with the mode's profiles
+ * formed on the device; nu and g are those the reference computes on the bitplane
+ * path (its `threads` only shapes the CPU path).  size: the box side, even, 8..16384. */
+int lgx_transport_measure(const float *densities, size_t n, int rest, uint64_t seed,
+                          size_t size, lgx_transport *out);
 
 /* ---- serving: a request loop with continuous batching ---------------------- */
 

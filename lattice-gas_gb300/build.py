@@ -26,6 +26,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 SOURCES = ["lgx_step.cu", "lgx_temporal.cu", "lgx_field.cu", "lgx_batch.cu", "lgx_bytes.cu",
            "lgx_noalloc.cu",
     "lgx_init.cu",
+    "lgx_profile.cu",
+    "lgx_transport.cpp",
            "lgx_probe.cu",
            "lgx_lattice.cpp",
            "lgx_batch_host.cpp", "lgx_server.cpp", "lgx_setup.cpp"]

@@ -1,6 +1,7 @@
 // lgx_batch.hpp -- device-side descriptors of a batch of lattices.
 #pragma once
 
+#include "../../include/lgx.h"
 #include "lgx_internal.hpp"
 
 namespace lgx {
@@ -55,5 +56,13 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, bool res
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st);
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st);
 cudaError_t launch_batch_base(uint64_t* base, uint32_t n, cudaStream_t st);
+
+// Work enqueued after every batch step, inside the captured graphs: called
+// with the batch's stream, its device step counter for the interval and the
+// step's index within the interval plus one (the state after batch step
+// *base + k_after).  Setting a hook drops the graphs captured without it.
+typedef cudaError_t (*BatchStepHook)(void* ctx, cudaStream_t st, const uint64_t* base,
+                                     uint32_t k_after);
+int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx);
 
 }  // namespace lgx

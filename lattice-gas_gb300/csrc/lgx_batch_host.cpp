@@ -58,6 +58,8 @@ struct lgx_batch {
   uint64_t launches = 0;
   uint64_t graph_launches = 0;
   cudaEvent_t ev[8] = {};
+  lgx::BatchStepHook hook = nullptr;
+  void* hook_ctx = nullptr;
 };
 
 namespace {
@@ -132,6 +134,7 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
       lgx::BatchStepArgs sa{b->d_descs, b->d_block0, nl, b->d_base, k, b->rest_blocks};
       e = lgx::launch_batch_step(sa, b->nblocks - b->rest_blocks, false, b->stream);
     }
+    if (e == cudaSuccess && b->hook) e = b->hook(b->hook_ctx, b->stream, b->d_base, k + 1);
   }
   if (e == cudaSuccess && sample && b->field_blocks) {
     lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, (uint32_t)b->lats.size(), b->field_blocks,
@@ -166,6 +169,24 @@ int graph_for(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
 }
 
 }  // namespace
+
+namespace lgx {
+
+int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx) {
+  if (!b) {
+    lgx::set_error("null batch handle");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaSetDevice(b->device));
+  LGX_CUDA(cudaStreamSynchronize(b->stream));
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  b->graphs.clear();
+  b->hook = fn;
+  b->hook_ctx = ctx;
+  return LGX_OK;
+}
+
+}  // namespace lgx
 
 extern "C" {
 
@@ -279,7 +300,8 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
     LGX_CUDA(cudaGraphLaunch(ex, b->stream));
     b->graph_launches += 1;
     const uint64_t per_step = (b->rest_blocks ? 1 : 0) + (b->nblocks > b->rest_blocks ? 1 : 0);
-    b->launches += len * per_step + 1 + (sample ? 1 : 0) + (b->items_per_step ? 1 : 0);
+    b->launches += len * (per_step + (b->hook ? 1 : 0)) + 1 + (sample ? 1 : 0) +
+                   (b->items_per_step ? 1 : 0);
     left -= len;
     since += len;
     if (sample) since = 0;

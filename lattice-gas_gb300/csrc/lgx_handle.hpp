@@ -48,4 +48,7 @@ struct lgx_lattice {
   uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
   uint32_t* done = nullptr;  // [wave_grid] published step per CTA
   uint32_t* error = nullptr; // timeout flag
+  // row and column profiles: scratch, row_ux[h], column_uy[w], column sums
+  // [3][w] and the device copy of the profile descriptor, one allocation
+  void* prof = nullptr;
 };

@@ -149,12 +149,34 @@ __global__ void __launch_bounds__(kThreads) lgx_fill_sample_kernel(const FillArg
         uint32_t m = fluid_mask(p, wd);
         if (p.f.planes) {
           uint32_t o[7] = {0, 0, 0, 0, 0, 0, 0};
-          while (m) {
-            const uint32_t b = __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t s = equilibrium_sample(p.f.thresh, p.f.rest, st);
+          if (p.f.thresh_rows || p.f.thresh_cols) {
+            // thresholds by row, or by column (32 j + b)
+            const uint32_t y = (uint32_t)(wd / p.f.dm.wpr), j = (uint32_t)(wd % p.f.dm.wpr);
+            uint32_t t[7];
+            if (p.f.thresh_rows) {
 #pragma unroll
-            for (int d = 0; d < 7; ++d) o[d] |= ((s >> d) & 1u) << b;
+              for (int d = 0; d < 7; ++d) t[d] = __ldg(p.f.thresh_rows + (size_t)y * 7 + d);
+            }
+            while (m) {
+              const uint32_t b = __ffs(m) - 1;
+              m &= m - 1;
+              if (p.f.thresh_cols) {
+#pragma unroll
+                for (int d = 0; d < 7; ++d)
+                  t[d] = __ldg(p.f.thresh_cols + (size_t)(j * 32u + b) * 7 + d);
+              }
+              const uint32_t s = equilibrium_sample(t, p.f.rest, st);
+#pragma unroll
+              for (int d = 0; d < 7; ++d) o[d] |= ((s >> d) & 1u) << b;
+            }
+          } else {
+            while (m) {
+              const uint32_t b = __ffs(m) - 1;
+              m &= m - 1;
+              const uint32_t s = equilibrium_sample(p.f.thresh, p.f.rest, st);
+#pragma unroll
+              for (int d = 0; d < 7; ++d) o[d] |= ((s >> d) & 1u) << b;
+            }
           }
 #pragma unroll
           for (int d = 0; d < 7; ++d) p.f.planes[(size_t)d * p.f.dm.total + wd] = o[d];
@@ -200,6 +222,8 @@ cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st) {
   const uint64_t cells = p.nwords * 32u;
   if ((cells * 4u) >> kFillJumps) return cudaErrorInvalidValue;  // draw index range
   if (!f.planes && (reinterpret_cast<uintptr_t>(f.cells) & 15u)) return cudaErrorInvalidValue;
+  if ((f.thresh_rows || f.thresh_cols) && (!f.planes || (f.thresh_rows && f.thresh_cols)))
+    return cudaErrorInvalidValue;
   p.nseg = (p.nwords + kSegWords - 1) / kSegWords;
   // a few blocks per SM, each over a contiguous range of whole tiles
   const uint64_t tiles = (p.nseg + kThreads - 1) / kThreads;

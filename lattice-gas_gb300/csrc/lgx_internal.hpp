@@ -130,6 +130,11 @@ struct EqFill {
   uint64_t seed;
   uint32_t thresh[7];
   bool rest;
+  // Planes target only: thresholds per row ([h][7], the shear-wave start of
+  // src/transport.rs:188-200) or per column ([w][7], transport.rs:240-252)
+  // in device memory, in place of `thresh`; at most one is set.
+  const uint32_t* thresh_rows;
+  const uint32_t* thresh_cols;
 };
 cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st);
 

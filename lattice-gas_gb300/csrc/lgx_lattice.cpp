@@ -15,6 +15,7 @@
 
 #include "../../include/lgx.h"
 #include "lgx_handle.hpp"
+#include "lgx_profile.hpp"
 #include "lgx_internal.hpp"
 
 namespace lgx {
@@ -88,6 +89,7 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->inlet);
   cudaFree(lat->field);
   cudaFree(lat->sums);
+  cudaFree(lat->prof);
   cudaFree(lat->done);
   cudaFree(lat->error);
   for (auto& e : lat->ev)
@@ -273,6 +275,48 @@ int check_wave_error(lgx_lattice* lat) {
                    "the lattice state is undefined");
     return LGX_ERR_CUDA;
   }
+  return LGX_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Profiles of the current state into the lattice's profile buffers; returns
+// the device addresses of row_ux, column_uy and the column sums.
+int run_profile(lgx_lattice* lat, float** row_u, float** col_u, int32_t** col_sums) {
+  const lgx::Dims& dm = lat->dm;
+  const size_t scratch = lgx::profile_scratch_words(dm.w, dm.h) * 4;
+  const size_t off_row = (scratch + 255) & ~(size_t)255;
+  const size_t off_col = off_row + (((size_t)dm.h * 4 + 255) & ~(size_t)255);
+  const size_t off_sum = off_col + (((size_t)dm.w * 4 + 255) & ~(size_t)255);
+  const size_t off_desc = off_sum + (((size_t)dm.w * 12 + 255) & ~(size_t)255);
+  char* base = (char*)lat->prof;
+  if (!base) {
+    LGX_CUDA(cudaMalloc(&lat->prof, off_desc + sizeof(lgx::ProfDesc)));
+    base = (char*)lat->prof;
+    LGX_CUDA(cudaMemsetAsync(base, 0, scratch, lat->stream));  // column sums, counter
+  }
+  lgx::ProfDesc d{};
+  d.planes[0] = d.planes[1] = lat->planes[lat->cur];
+  d.dm = dm;
+  d.rows = (int32_t*)base;
+  d.cols = d.rows + 3 * (size_t)dm.h;
+  d.done = (uint32_t*)(d.cols + 3 * (size_t)dm.w);
+  d.row_u = (float*)(base + off_row);
+  d.col_u = (float*)(base + off_col);
+  d.col_sums = (int32_t*)(base + off_sum);
+  d.first = 0;
+  d.every = 0;
+  d.count = 1;
+  lgx::ProfDesc* dd = (lgx::ProfDesc*)(base + off_desc);
+  LGX_CUDA(cudaMemcpyAsync(dd, &d, sizeof(d), cudaMemcpyHostToDevice, lat->stream));
+  lgx::ProfArgs pa{dd, 1, nullptr, 0};
+  LGX_CUDA(lgx::launch_profile(pa, dm.h, lat->stream));
+  lat->launches += 1;
+  *row_u = d.row_u;
+  *col_u = d.col_u;
+  *col_sums = d.col_sums;
   return LGX_OK;
 }
 
@@ -526,6 +570,56 @@ int lgx_read_block_sums(lgx_lattice* lat, int32_t* mass, int32_t* px2, int32_t* 
     if (dst[i] && nb)
       LGX_CUDA(cudaMemcpyAsync(dst[i], lat->sums + i * nb, nb * sizeof(int32_t),
                                cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_row_ux(lgx_lattice* lat, float* ux, size_t n) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!ux || n != lat->dm.h) {
+    lgx::set_error("lgx_row_ux: need one value per row");
+    return LGX_ERR_ARG;
+  }
+  float *ru, *cu;
+  int32_t* cs;
+  rc = run_profile(lat, &ru, &cu, &cs);
+  if (rc) return rc;
+  LGX_CUDA(cudaMemcpyAsync(ux, ru, n * 4, cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_column_uy(lgx_lattice* lat, float* uy, size_t n) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!uy || n != lat->dm.w) {
+    lgx::set_error("lgx_column_uy: need one value per column");
+    return LGX_ERR_ARG;
+  }
+  float *ru, *cu;
+  int32_t* cs;
+  rc = run_profile(lat, &ru, &cu, &cs);
+  if (rc) return rc;
+  LGX_CUDA(cudaMemcpyAsync(uy, cu, n * 4, cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_line_sums(lgx_lattice* lat, int32_t* rows, size_t n_rows, int32_t* cols, size_t n_cols) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if ((rows && n_rows != 3ull * lat->dm.h) || (cols && n_cols != 3ull * lat->dm.w)) {
+    lgx::set_error("lgx_line_sums: rows holds 3 x h values, cols 3 x w");
+    return LGX_ERR_ARG;
+  }
+  float *ru, *cu;
+  int32_t* cs;
+  rc = run_profile(lat, &ru, &cu, &cs);
+  if (rc) return rc;
+  if (rows)
+    LGX_CUDA(cudaMemcpyAsync(rows, lat->prof, n_rows * 4, cudaMemcpyDeviceToHost, lat->stream));
+  if (cols) LGX_CUDA(cudaMemcpyAsync(cols, cs, n_cols * 4, cudaMemcpyDeviceToHost, lat->stream));
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
   return LGX_OK;
 }

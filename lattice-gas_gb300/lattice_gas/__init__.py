@@ -58,6 +58,17 @@ class ServerStats(C.Structure):
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 
+TRANSPORT_SAMPLES = 20
+
+
+class Transport(C.Structure):
+    """lgx_transport: transport::Transport (src/transport.rs:31-37) and its fit inputs."""
+    _fields_ = [("nu", C.c_float), ("g", C.c_float), ("window_nu", C.c_uint64),
+                ("window_g", C.c_uint64), ("u_actual", C.c_float),
+                ("mode_nu", C.c_double * (2 * TRANSPORT_SAMPLES)),
+                ("mode_g", C.c_double * (2 * TRANSPORT_SAMPLES))]
+
+
 class LgxError(RuntimeError):
     """A C-ABI call returned a non-zero lgx_status."""
 
@@ -100,6 +111,9 @@ def lib():
         _sig(L, "lgx_read_field", vp, f32p, f32p, f32p, f32p, sz)
         _sig(L, "lgx_read_block_sums", vp, i32p, i32p, i32p, i32p, sz)
         _sig(L, "lgx_total_particles", vp, C.POINTER(C.c_uint64))
+        _sig(L, "lgx_row_ux", vp, f32p, sz)
+        _sig(L, "lgx_column_uy", vp, f32p, sz)
+        _sig(L, "lgx_line_sums", vp, i32p, sz, i32p, sz)
         _sig(L, "lgx_steps", vp, C.POINTER(C.c_uint64))
         _sig(L, "lgx_stream", vp, C.POINTER(vp))
         _sig(L, "lgx_launch_count", vp, C.POINTER(C.c_uint64))
@@ -142,6 +156,8 @@ def lib():
         _sig(L, "lgx_batch_timing_mark", vp, C.c_int)
         _sig(L, "lgx_batch_timing_elapsed", vp, C.c_int, C.c_int, C.POINTER(C.c_float))
         _sig(L, "lgx_probe_int_rate", C.c_int, C.POINTER(C.c_double))
+        _sig(L, "lgx_transport_measure", f32p, sz, C.c_int, C.c_uint64, sz,
+             C.POINTER(Transport))
         _sig(L, "lgx_host_alloc", sz, C.POINTER(vp))
         _sig(L, "lgx_host_free", vp)
         _sig(L, "lgx_equilibrium_thresholds", C.c_float, C.c_float, C.c_float, C.c_int, u32p)
@@ -233,6 +249,26 @@ class GpuLattice:
             out = np.zeros(self.w * self.h, np.uint8)
         _check(lib().lgx_store(self._h, _p(out, C.c_uint8), out.size))
         return out
+
+    def row_ux(self) -> np.ndarray:
+        """transport::row_ux (src/transport.rs:87-91), reduced on the device."""
+        out = np.zeros(self.h, np.float32)
+        _check(lib().lgx_row_ux(self._h, _p(out, C.c_float), out.size))
+        return out
+
+    def column_uy(self) -> np.ndarray:
+        """transport::column_uy (src/transport.rs:51-84), reduced on the device."""
+        out = np.zeros(self.w, np.float32)
+        _check(lib().lgx_column_uy(self._h, _p(out, C.c_float), out.size))
+        return out
+
+    def line_sums(self):
+        """Exact WITH_WALLS (mass, px2, py2) of every row ([3, h]) and column ([3, w])."""
+        rows = np.zeros(3 * self.h, np.int32)
+        cols = np.zeros(3 * self.w, np.int32)
+        _check(lib().lgx_line_sums(self._h, _p(rows, C.c_int32), rows.size, _p(cols, C.c_int32),
+                                   cols.size))
+        return rows.reshape(3, self.h), cols.reshape(3, self.w)
 
     def init_equilibrium(self, density, inflow, seed):
         """Lattice::init_equilibrium (src/lattice.rs:197-208) on the device: fluid cells
@@ -581,3 +617,13 @@ def verify_circuit(rest) -> np.ndarray:
     out = np.zeros(n, np.uint32)
     _check(lib().lgx_verify_circuit(int(bool(rest)), _p(out, C.c_uint32), n))
     return out
+
+
+def transport_measure(densities, rest=True, seed=0x5EED, size=256):
+    """transport::measure on the device for each density (src/transport.rs:291-319).
+    Returns a list of Transport records (nu, g, windows, averaged modes)."""
+    d = np.ascontiguousarray(np.atleast_1d(densities), dtype=np.float32)
+    out = (Transport * d.size)()
+    _check(lib().lgx_transport_measure(_p(d, C.c_float), d.size, int(bool(rest)), _u64(seed),
+                                       int(size), out))
+    return list(out)

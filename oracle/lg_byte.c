@@ -287,6 +287,16 @@ void lgo_cells_shear_wave(uint8_t *cells, size_t w, size_t h, float density,
     }
 }
 
+void lgo_cells_column_wave(uint8_t *cells, size_t w, size_t h, float density, float u0,
+                           const float *uy_col, int rest, uint64_t rng_seed) {
+    equilibrium_t *cols = (equilibrium_t *)malloc(w * sizeof(equilibrium_t));
+    for (size_t x = 0; x < w; ++x) eq_new(&cols[x], density, u0, uy_col[x], rest);
+    uint64_t st = lgo_rng_seed(rng_seed);
+    for (size_t y = 0; y < h; ++y)
+        for (size_t x = 0; x < w; ++x) cells[y * w + x] = eq_sample(&cols[x], &st);
+    free(cols);
+}
+
 void lgo_add_box(uint8_t *cells, size_t w, size_t h, float x0, float x1, float y0, float y1,
                  int strict) {
     for (size_t y = 0; y < h; ++y)

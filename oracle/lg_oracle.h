@@ -78,6 +78,12 @@ void lgo_cells_init_equilibrium(uint8_t *cells, size_t n, float density, float u
 void lgo_cells_shear_wave(uint8_t *cells, size_t w, size_t h, float density,
                           const float *ux_row, int rest, uint64_t rng_seed);
 
+/* Transverse-wave start (src/transport.rs:237-251): column x drawn from
+ * Equilibrium(density, u0, uy_col[x]), cells in row-major order, one generator
+ * Rng::new(rng_seed). */
+void lgo_cells_column_wave(uint8_t *cells, size_t w, size_t h, float density, float u0,
+                           const float *uy_col, int rest, uint64_t rng_seed);
+
 /* ---- moments and coarse-graining (src/moments.rs, src/render.rs:61-120) --- */
 /* Exact (mass, px2, py2, solid) of a byte slice through the FLUID (walls=0) or
  * WITH_WALLS (walls=1) table. */
@@ -122,6 +128,23 @@ uint64_t lgo_bp_total_particles(const lgo_bp *g);
 uint64_t lgo_bp_steps(const lgo_bp *g);
 /* Raw planes (7 * wpr * h words, plane-major) for word-level comparisons. */
 const uint32_t *lgo_bp_planes(const lgo_bp *g);
+
+/* ---- transport.rs ------------------------------------------------------- */
+/* row_ux / column_uy (transport.rs:51-91) of byte cells. */
+void lgo_row_ux(const uint8_t *cells, size_t w, size_t h, float *out);
+void lgo_column_uy(const uint8_t *cells, size_t w, size_t h, float *out);
+#define LGO_TRANSPORT_SAMPLES 20
+typedef struct lgo_transport {
+    float nu, g;
+    uint64_t window_nu, window_g;
+    float u_actual;
+    double mode_nu[2 * LGO_TRANSPORT_SAMPLES];
+    double mode_g[2 * LGO_TRANSPORT_SAMPLES];
+} lgo_transport;
+/* transport::measure (transport.rs:291-319) on the CPU byte path (gpu = 0, whose
+ * random stream depends on threads) or on the bitplane path (gpu = 1). */
+void lgo_transport_measure(float density, int rest, size_t threads, uint64_t seed, size_t size,
+                           int gpu, lgo_transport *out);
 
 #ifdef __cplusplus
 }

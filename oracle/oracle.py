@@ -39,6 +39,13 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
+class TransportResult(C.Structure):
+    """lgo_transport: transport::Transport and the inputs of its fits."""
+    _fields_ = [("nu", C.c_float), ("g", C.c_float), ("window_nu", C.c_uint64),
+                ("window_g", C.c_uint64), ("u_actual", C.c_float),
+                ("mode_nu", C.c_double * 40), ("mode_g", C.c_double * 40)]
+
+
 def _sig(lib, name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -79,6 +86,12 @@ def lib():
         _sig(L, "lgo_cells_init_equilibrium", None, u8p, sz, C.c_float, C.c_float, C.c_float,
              C.c_int, C.c_uint64)
         _sig(L, "lgo_cells_shear_wave", None, u8p, sz, sz, C.c_float, f32p, C.c_int, C.c_uint64)
+        _sig(L, "lgo_cells_column_wave", None, u8p, sz, sz, C.c_float, C.c_float, f32p, C.c_int,
+             C.c_uint64)
+        _sig(L, "lgo_row_ux", None, u8p, sz, sz, f32p)
+        _sig(L, "lgo_column_uy", None, u8p, sz, sz, f32p)
+        _sig(L, "lgo_transport_measure", None, C.c_float, C.c_int, sz, C.c_uint64, sz, C.c_int,
+             C.POINTER(TransportResult))
         _sig(L, "lgo_moments_sum", None, u8p, sz, C.c_int, i64p)
         _sig(L, "lgo_invariants", None, u8p, sz, i64p)
         _sig(L, "lgo_field_sample", None, u8p, sz, sz, sz, sz, C.c_float, f32p, f32p, f32p, f32p)
@@ -331,3 +344,37 @@ class BitplaneLattice:
         wpr = (self.w + 31) // 32
         p = lib().lgo_bp_planes(self._p)
         return np.ctypeslib.as_array(p, shape=(7 * wpr * self.h,)).copy()
+
+
+def column_wave_cells(w, h, density, u0, uy_col, rest, rng_seed):
+    """Transverse-wave start (src/transport.rs:237-251)."""
+    c = np.zeros(w * h, np.uint8)
+    u = np.ascontiguousarray(uy_col, dtype=np.float32)
+    lib().lgo_cells_column_wave(ptr(c, C.c_uint8), w, h, density, u0, ptr(u, C.c_float),
+                                int(rest), rng_seed & (2**64 - 1))
+    return c
+
+
+def row_ux(cells, w, h):
+    """transport::row_ux (src/transport.rs:87-91)."""
+    c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+    out = np.zeros(h, np.float32)
+    lib().lgo_row_ux(ptr(c, C.c_uint8), w, h, ptr(out, C.c_float))
+    return out
+
+
+def column_uy(cells, w, h):
+    """transport::column_uy (src/transport.rs:51-84)."""
+    c = np.ascontiguousarray(cells, dtype=np.uint8).reshape(-1)
+    out = np.zeros(w, np.float32)
+    lib().lgo_column_uy(ptr(c, C.c_uint8), w, h, ptr(out, C.c_float))
+    return out
+
+
+def transport_measure(density, rest, threads, seed, size, gpu):
+    """transport::measure (src/transport.rs:291-319) on the byte path (gpu=False) or the
+    bitplane path (gpu=True)."""
+    r = TransportResult()
+    lib().lgo_transport_measure(float(density), int(bool(rest)), int(threads),
+                                seed & (2**64 - 1), int(size), int(bool(gpu)), C.byref(r))
+    return r
