@@ -298,6 +298,43 @@ def bench_roofline_case(LG, W, steps: int):
     return out
 
 
+def bench_transport(LG, cpu: bool):
+    """transport::measure (src/transport.rs:291-319), the caller that synchronises
+    most: one measurement at the reference's sizes (its own bench times 64 and 256,
+    benches/speed.rs:676-683) and main.rs's 22-density scan as one batch.  The CPU
+    reference is the oracle's byte-path measure, the reference's CPU path."""
+    import time
+    out = {"unit": "s per call", "density": 0.22, "rest": True}
+    for size in (64, 256):
+        best = None
+        for _ in range(3):
+            t = time.perf_counter()
+            r = LG.transport_measure([0.22], rest=True, seed=0x5EED, size=size)[0]
+            dt = time.perf_counter() - t
+            best = dt if best is None else min(best, dt)
+        out["measure_%d" % size] = {"engine_s": round(best, 4), "nu": round(r.nu, 5),
+                                    "g": round(r.g, 5), "window_nu": r.window_nu,
+                                    "window_g": r.window_g}
+    ds = [0.04 + 0.02 * i for i in range(22)]
+    t = time.perf_counter()
+    LG.transport_measure(ds, rest=True, seed=0x5EED, size=256)
+    out["scan_22_densities_256"] = {"engine_s": round(time.perf_counter() - t, 4),
+                                    "densities": "0.04..0.46 step 0.02 (src/main.rs:549-560)"}
+    if cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        t = time.perf_counter()
+        c = O.transport_measure(0.22, True, threads, 0x5EED, 64, gpu=False)
+        dt = time.perf_counter() - t
+        out["measure_64"]["cpu_reference_s"] = round(dt, 4)
+        out["measure_64"]["cpu"] = {"kind": "port", "cores": threads, "nu": round(c.nu, 5),
+                                    "g": round(c.g, 5),
+                                    "sample": "transport::measure(0.22, rest, %d threads, "
+                                              "0x5EED, 64, cpu) restated in C" % threads}
+        out["measure_64"]["speedup_vs_cpu"] = round(dt / out["measure_64"]["engine_s"], 1)
+    return out
+
+
 def bench_served(LG, W, n: int, budget: int):
     """The request stream: Poisson arrivals at 200/s, sizes 128x128..4096x2048,
     1k..50k steps, sampling every 50..500 steps with 8..32 blocks, obstacle none
@@ -450,11 +487,12 @@ def run_gb300(args, world, rank, local):
                          "Lattice::step restated in C (oracle/), %d threads"
                          % (nsteps, dt, threads)}
 
-    batched = served = big = None
+    batched = served = big = transport = None
     if not args.no_patterns:
         batched = bench_batched(LG, W, args.sweep_steps)
         served = bench_served(LG, W, args.requests, args.budget_mib << 20)
         big = bench_roofline_case(LG, W, args.big_steps)
+        transport = bench_transport(LG, rank == 0 and world == 1 and not args.no_cpu)
     lop3_peak = LG.probe_int_rate(0)
     alu_achieved = STEP_ALU_WARP_INSTR * 32 / (step_ms * 1e-3)
 
@@ -492,6 +530,7 @@ def run_gb300(args, world, rank, local):
         "batched": batched,
         "served": served,
         "roofline_case": big,
+        "transport": transport,
         "device": g.device_name(),
     }
     print(json.dumps(line), flush=True)
