@@ -321,7 +321,8 @@ def bench_transport(LG, cpu: bool):
     out["scan_22_densities_256"] = {"engine_s": round(time.perf_counter() - t, 4),
                                     "densities": "0.04..0.46 step 0.02 (src/main.rs:549-560)"}
     if cpu:
-        from oracle import oracle as O
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
         threads = os.cpu_count() or 1
         t = time.perf_counter()
         c = O.transport_measure(0.22, True, threads, 0x5EED, 64, gpu=False)
