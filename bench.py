@@ -258,7 +258,11 @@ def bench_batched(LG, W, steps: int):
            "speedup_vs_plain": round(t_plain / t_batch, 2), "unit": UNIT,
            "batched_s": round(t_batch, 4), "plain_s": round(t_plain, 4),
            "kernel_launches": k1 - k0, "graph_launches": g1 - g0,
-           "bit_exact_vs_plain": bool(same)}
+           "bit_exact_vs_plain": bool(same),
+           "size_classes": [{k: (round(v, 2) if isinstance(v, float) else v)
+                             for k, v in c.items()} for c in b.plan],
+           "size_class_note": "the tuner's per-step times, one launch per step vs the "
+                              "resident kernel, for each class of small lattices"}
     b.close()
     for g in plain + together:
         g.close()
@@ -401,6 +405,7 @@ def bench_served(LG, W, n: int, budget: int):
             "plain_p99_latency_s": round(pct(plain_lat, 0.99), 4),
             "served_s": round(t_served, 3), "plain_s": round(clock, 3),
             "ticks": st["ticks"], "kernel_launches": st["kernel_launches"],
+            "device_busy_s": round(st["gpu_busy_ns"] / 1e9, 4),
             "latency_note": "includes queueing; the stream offers more work than the GPU "
                             "serves, so the queue grows while it arrives"}
 

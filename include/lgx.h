@@ -183,6 +183,32 @@ int lgx_step_planes_noalloc(const uint32_t *planes_in, uint32_t *planes_out,
  * batch, advance it only through the batch. */
 typedef struct lgx_batch lgx_batch;
 int lgx_batch_create(lgx_lattice *const *lats, size_t n, lgx_batch **out);
+/* How a batch steps its lattices.  AUTO: lattices of up to 32768 words are grouped
+ * into size classes (words rounded up to a power of two, and the rule), and a
+ * tuner times each class both ways on synthetic lattices of its size and count --
+ * one batched launch per step, or the resident kernel (a thread-block cluster per
+ * lattice, every step of an interval in one launch) over its cluster shapes -- and
+ * the faster is used; larger lattices always take one launch per step.  PER_STEP:
+ * every lattice one launch per step.  RESIDENT: every class that has a usable
+ * cluster shape on the resident kernel.  Results are identical under all three. */
+#define LGX_BATCH_AUTO 0
+#define LGX_BATCH_PER_STEP 1
+#define LGX_BATCH_RESIDENT 2
+int lgx_batch_create_ex(lgx_lattice *const *lats, size_t n, int policy, lgx_batch **out);
+/* One size class of a batch and the tuner's finding for it. */
+typedef struct lgx_batch_class {
+  uint32_t words;       /* words per plane per lattice, rounded up to a power of two */
+  uint32_t lattices;    /* members of the batch in the class */
+  int rest;             /* the class's rule: 1 with rest particles */
+  int resident;         /* 1: resident kernel, 0: one batched launch per step */
+  uint32_t cluster;     /* the resident kernel's best cluster shape: CTAs per lattice */
+  uint32_t threads;     /* and threads per CTA */
+  float step_us;        /* tuner's time per step of the class, one launch per step */
+  float resident_us;    /* and on the resident kernel (0: no usable shape) */
+} lgx_batch_class;
+/* The classes of small lattices (larger ones are not listed): *n is their number,
+ * the first min(cap, *n) are written. */
+int lgx_batch_plan(lgx_batch *b, lgx_batch_class *out, size_t cap, size_t *n);
 int lgx_batch_destroy(lgx_batch *b);
 /* Every lattice advances n steps, sampling into its own attached field every
  * sample_every steps and after the last (as lgx_advance_sampling). */
@@ -247,6 +273,7 @@ typedef struct {
   uint64_t completed, failed, cancelled, active, queued;
   uint64_t ticks, kernel_launches, site_updates;
   uint64_t bytes_in_use, peak_bytes, peak_active;
+  uint64_t gpu_busy_ns;  /* device time of the ticks run so far (start to end of each) */
 } lgx_server_stats;
 
 typedef struct lgx_server lgx_server;

@@ -28,6 +28,8 @@ SOURCES = ["lgx_step.cu", "lgx_temporal.cu", "lgx_field.cu", "lgx_batch.cu", "lg
     "lgx_init.cu",
     "lgx_profile.cu",
     "lgx_transport.cpp",
+    "lgx_resident.cu",
+    "lgx_tune.cpp",
            "lgx_probe.cu",
            "lgx_lattice.cpp",
            "lgx_batch_host.cpp", "lgx_server.cpp", "lgx_setup.cpp"]

@@ -63,6 +63,26 @@ __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepAr
   batch_word<REST>(d, local, p.k, g, live, s);
 }
 
+// Both rules in one launch: a block belongs to one lattice, so the rule is
+// uniform across it.  Used when a batch mixes rest-particle and six-direction
+// lattices, to keep one launch per step.
+__global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_mixed_kernel(BatchStepArgs p) {
+  const uint32_t blk = p.first_block + blockIdx.x;
+  const uint32_t li = owner_of(p.block0, p.nlat, blk);
+  const LatDesc& d = p.descs[li];
+  uint32_t g = (blk - __ldg(p.block0 + li)) * (uint32_t)kThreads + threadIdx.x;
+  const bool live = g < d.dm.total;
+  if (!live) g = d.dm.total - 1u;
+  const uint64_t local = *p.base + p.k;
+  const Draws s = draws(g ^ step_seed32(d.seed, d.steps0 + local));
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (d.rest)
+    batch_word<true>(d, local, p.k, g, live, s);
+  else
+    batch_word<false>(d, local, p.k, g, live, s);
+}
+
 // Inlet draws for steps base .. base + nsteps - 1 of every lattice with an
 // inlet: one thread per (lattice, step, row, inlet word).
 __global__ void __launch_bounds__(128) lgx_batch_inlet_kernel(BatchInletArgs p) {
@@ -116,7 +136,7 @@ __global__ void lgx_batch_base_kernel(uint64_t* base, uint32_t n) { *base += n; 
 
 }  // namespace
 
-cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, bool rest,
+cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule,
                               cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
@@ -127,7 +147,8 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, bool res
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (rest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<true>, a);
+  if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_step_mixed_kernel, a);
+  if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<true>, a);
   return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<false>, a);
 }
 

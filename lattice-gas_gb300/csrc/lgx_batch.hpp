@@ -51,7 +51,31 @@ struct BatchSampleArgs {
   uint32_t k_after;      // sample the state after batch step *base + k_after
 };
 
-cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, bool rest,
+// Sampling schedule of a lattice within one resident launch: it is
+// coarse-grained after step t (1-based) when since + t is a multiple of
+// every, or t == left (its last step); every == 0: never.
+struct ResSched {
+  uint32_t every, since, left;
+};
+
+// `len` steps of lattices first_lat .. first_lat + nlat - 1 (of descs and
+// sched), one thread-block cluster each, in one launch.  The batch step
+// before the first of them is *base (null: 0); after local step t the state of
+// a lattice is in planes[(cur0 + t) & 1].  Inlet draws as for the batched step.
+struct ResidentArgs {
+  const LatDesc* descs;
+  const ResSched* sched;
+  uint32_t first_lat;
+  const uint64_t* base;
+  uint32_t len;
+};
+bool resident_config_valid(uint32_t csize, uint32_t threads);
+cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
+                            uint32_t threads, cudaStream_t st);
+
+// The rule of the blocks a batched step launch covers.
+constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;
+cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule,
                               cudaStream_t st);
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st);
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st);

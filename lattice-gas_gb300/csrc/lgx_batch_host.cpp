@@ -1,10 +1,15 @@
-// lgx_batch_host.cpp -- the batch handle: many lattices, one launch per step.
+// lgx_batch_host.cpp -- the batch handle: many lattices advanced together.
 //
 // A batch borrows lattices created with lgx_create (their planes, fields and
-// inlet settings) and advances all of them together.  For each sampling
-// interval it replays a CUDA graph captured on first use:
-//   [batched inlet draws] -> L x batched step (programmatic dependent launch)
-//   -> [batched coarse-graining] -> batch step counter += L
+// inlet settings) and advances all of them together.  Lattices are grouped
+// into size classes; the tuner (lgx_tune.cpp) decides for each class of small
+// lattices whether it runs on the resident kernel (a cluster per lattice, all
+// steps of an interval in one launch) or with the rest, one batched launch
+// per step.  For each sampling interval the batch replays a CUDA graph
+// captured on first use:
+//   [batched inlet draws] -+-> L x batched step (programmatic dependent launch)
+//                          |   -> [batched coarse-graining]            -+-> counter += L
+//                          +-> one resident launch per class (own sampling) -+
 // The graph holds only device pointers to the descriptor table and the step
 // counter, so one capture serves every interval of the same length.
 #include <cuda_runtime.h>
@@ -17,6 +22,7 @@
 #include "../../include/lgx.h"
 #include "lgx_batch.hpp"
 #include "lgx_handle.hpp"
+#include "lgx_tune.hpp"
 
 namespace {
 
@@ -24,6 +30,13 @@ struct GraphEntry {
   uint32_t len;
   bool sample;
   cudaGraphExec_t exec;
+  lgx::ResSched* sched;  // resident lattices' schedule for this interval shape
+};
+
+// A size class on the resident kernel: lattices [first, first + count).
+struct ResClass {
+  uint32_t first, count;
+  lgx::ClassPlan plan;
 };
 
 int cuda_fail(cudaError_t e, const char* what) {
@@ -60,6 +73,12 @@ struct lgx_batch {
   cudaEvent_t ev[8] = {};
   lgx::BatchStepHook hook = nullptr;
   void* hook_ctx = nullptr;
+  int policy = LGX_BATCH_AUTO;
+  uint32_t nstep = 0;                 // leading lattices stepped one launch per step
+  std::vector<ResClass> classes;      // then the resident classes
+  std::vector<lgx_batch_class> plan;  // every class, as reported
+  cudaStream_t side = nullptr;        // resident launches' branch of the graph
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -67,8 +86,14 @@ namespace {
 void free_batch(lgx_batch* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
-  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto& g : b->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaFree(g.sched);
+  }
   for (auto* p : b->inlet_bufs) cudaFree(p);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   cudaFree(b->d_descs);
   cudaFree(b->d_block0);
   cudaFree(b->d_item0);
@@ -112,7 +137,25 @@ int setup_descs(lgx_batch* b, float alpha) {
   return LGX_OK;
 }
 
-int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
+// One launch per step: the specialised kernel when every lattice has the same
+// rule, the mixed one otherwise (rest-particle lattices' blocks come first).
+int step_rule(uint32_t rest_blocks, uint32_t nblocks) {
+  if (rest_blocks == nblocks) return lgx::kRuleRest;
+  if (rest_blocks == 0) return lgx::kRuleNoRest;
+  return lgx::kRuleMixed;
+}
+
+int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
+            lgx::ResSched** sched_out) {
+  // the resident lattices sample at the end of the interval, when it samples
+  const size_t n = b->lats.size();
+  lgx::ResSched* sched = nullptr;
+  if (!b->classes.empty()) {
+    std::vector<lgx::ResSched> h(n, lgx::ResSched{sample ? len : 0u, 0u, len});
+    LGX_CUDA(cudaMalloc(&sched, n * sizeof(lgx::ResSched)));
+    *sched_out = sched;
+    LGX_CUDA(cudaMemcpy(sched, h.data(), n * sizeof(lgx::ResSched), cudaMemcpyHostToDevice));
+  }
   cudaGraph_t graph = nullptr;
   LGX_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
@@ -123,23 +166,31 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
     // the item prefix scales with the interval length
     e = lgx::launch_batch_inlet(ia, b->stream);
   }
-  for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
+  // the resident classes on their own branch, when there is a per-step chain
+  cudaStream_t rs = b->nstep ? b->side : b->stream;
+  if (e == cudaSuccess && !b->classes.empty() && b->nstep) {
+    e = cudaEventRecord(b->fork, b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork, 0);
+  }
+  for (const ResClass& c : b->classes) {
+    if (e != cudaSuccess) break;
+    lgx::ResidentArgs ra{b->d_descs, sched, c.first, b->d_base, len};
+    e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, rs);
+  }
+  for (uint32_t k = 0; k < len && e == cudaSuccess && b->nstep; ++k) {
     // rest-particle lattices' blocks first, then the six-direction ones
-    const uint32_t nl = (uint32_t)b->lats.size();
-    if (b->rest_blocks) {
-      lgx::BatchStepArgs sa{b->d_descs, b->d_block0, nl, b->d_base, k, 0};
-      e = lgx::launch_batch_step(sa, b->rest_blocks, true, b->stream);
-    }
-    if (e == cudaSuccess && b->nblocks > b->rest_blocks) {
-      lgx::BatchStepArgs sa{b->d_descs, b->d_block0, nl, b->d_base, k, b->rest_blocks};
-      e = lgx::launch_batch_step(sa, b->nblocks - b->rest_blocks, false, b->stream);
-    }
+    lgx::BatchStepArgs sa{b->d_descs, b->d_block0, b->nstep, b->d_base, k, 0};
+    e = lgx::launch_batch_step(sa, b->nblocks, step_rule(b->rest_blocks, b->nblocks),
+                               b->stream);
     if (e == cudaSuccess && b->hook) e = b->hook(b->hook_ctx, b->stream, b->d_base, k + 1);
   }
   if (e == cudaSuccess && sample && b->field_blocks) {
-    lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, (uint32_t)b->lats.size(), b->field_blocks,
-                            b->d_base, len};
+    lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, b->nstep, b->field_blocks, b->d_base, len};
     e = lgx::launch_batch_sample(sp, b->stream);
+  }
+  if (e == cudaSuccess && !b->classes.empty() && b->nstep) {
+    e = cudaEventRecord(b->join, b->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->join, 0);
   }
   if (e == cudaSuccess) e = lgx::launch_batch_base(b->d_base, len, b->stream);
   cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
@@ -161,9 +212,13 @@ int graph_for(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
       return LGX_OK;
     }
   cudaGraphExec_t ex = nullptr;
-  int rc = capture(b, len, sample, &ex);
-  if (rc) return rc;
-  b->graphs.push_back({len, sample, ex});
+  lgx::ResSched* sched = nullptr;
+  int rc = capture(b, len, sample, &ex, &sched);
+  if (rc) {
+    cudaFree(sched);
+    return rc;
+  }
+  b->graphs.push_back({len, sample, ex, sched});
   *out = ex;
   return LGX_OK;
 }
@@ -177,9 +232,16 @@ int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx) {
     lgx::set_error("null batch handle");
     return LGX_ERR_ARG;
   }
+  if (fn && !b->classes.empty()) {
+    lgx::set_error("a per-step hook needs every lattice stepped one launch per step");
+    return LGX_ERR_STATE;
+  }
   LGX_CUDA(cudaSetDevice(b->device));
   LGX_CUDA(cudaStreamSynchronize(b->stream));
-  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto& g : b->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaFree(g.sched);
+  }
   b->graphs.clear();
   b->hook = fn;
   b->hook_ctx = ctx;
@@ -191,6 +253,14 @@ int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx) {
 extern "C" {
 
 int lgx_batch_create(lgx_lattice* const* lats, size_t n, lgx_batch** out) {
+  return lgx_batch_create_ex(lats, n, LGX_BATCH_AUTO, out);
+}
+
+int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batch** out) {
+  if (policy != LGX_BATCH_AUTO && policy != LGX_BATCH_PER_STEP && policy != LGX_BATCH_RESIDENT) {
+    lgx::set_error("lgx_batch_create_ex: unknown policy");
+    return LGX_ERR_ARG;
+  }
   if (!out || !lats || n == 0) {
     lgx::set_error("lgx_batch_create: need at least one lattice");
     return LGX_ERR_ARG;
@@ -213,22 +283,83 @@ int lgx_batch_create(lgx_lattice* const* lats, size_t n, lgx_batch** out) {
     return LGX_ERR_ALLOC;
   }
   b->device = lats[0]->device;
-  // rest-particle lattices first, so each rule's blocks are one contiguous run
+  b->policy = policy;
+  cudaError_t e = cudaSetDevice(b->device);
+  // size classes of the small lattices (words rounded up to a power of two,
+  // and the rule), each planned by the tuner
+  std::vector<int> cls(n, -1);
+  struct Key {
+    uint32_t words;
+    bool rest;
+    uint32_t count;
+    lgx::ClassPlan plan;
+  };
+  std::vector<Key> keys;
+  for (size_t i = 0; i < n && policy != LGX_BATCH_PER_STEP; ++i) {
+    if (lats[i]->dm.total > lgx::kResidentMaxWords) continue;
+    const uint32_t wb = lgx::class_bucket(lats[i]->dm.total);
+    size_t k = 0;
+    while (k < keys.size() && !(keys[k].words == wb && keys[k].rest == lats[i]->rest)) ++k;
+    if (k == keys.size()) keys.push_back({wb, lats[i]->rest, 0, {}});
+    keys[k].count += 1;
+    cls[i] = (int)k;
+  }
+  std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& c) {
+    return a.words != c.words ? a.words < c.words : a.rest > c.rest;
+  });
+  for (size_t i = 0; i < n; ++i) {  // class index after the sort
+    if (cls[i] < 0) continue;
+    const uint32_t wb = lgx::class_bucket(lats[i]->dm.total);
+    size_t k = 0;
+    while (!(keys[k].words == wb && keys[k].rest == lats[i]->rest)) ++k;
+    cls[i] = (int)k;
+  }
+  std::vector<bool> res_class(keys.size(), false);
+  for (size_t k = 0; k < keys.size() && e == cudaSuccess; ++k) {
+    e = lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, &keys[k].plan);
+    const lgx::ClassPlan& p = keys[k].plan;
+    res_class[k] = policy == LGX_BATCH_RESIDENT ? p.csize != 0 : p.resident;
+    lgx_batch_class c{};
+    c.words = keys[k].words;
+    c.lattices = keys[k].count;
+    c.rest = keys[k].rest ? 1 : 0;
+    c.resident = res_class[k] ? 1 : 0;
+    c.cluster = p.csize;
+    c.threads = p.threads;
+    c.step_us = p.step_us;
+    c.resident_us = p.resident_us;
+    b->plan.push_back(c);
+  }
+  // order: per-step lattices (rest-particle ones first, so each rule's blocks
+  // are one contiguous run), then each resident class
   for (int pass = 0; pass < 2; ++pass)
     for (size_t i = 0; i < n; ++i)
-      if (lats[i]->rest == (pass == 0)) b->lats.push_back(lats[i]);
+      if ((cls[i] < 0 || !res_class[cls[i]]) && lats[i]->rest == (pass == 0))
+        b->lats.push_back(lats[i]);
+  b->nstep = (uint32_t)b->lats.size();
+  for (size_t k = 0; k < keys.size(); ++k) {
+    if (!res_class[k]) continue;
+    ResClass rc{(uint32_t)b->lats.size(), 0, keys[k].plan};
+    for (size_t i = 0; i < n; ++i)
+      if (cls[i] == (int)k) b->lats.push_back(lats[i]);
+    rc.count = (uint32_t)b->lats.size() - rc.first;
+    b->classes.push_back(rc);
+  }
   lats = b->lats.data();
-  cudaError_t e = cudaSetDevice(b->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
   for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev[i]);
-  // block table: each lattice padded to whole 256-word blocks
+  // block table of the per-step lattices: each padded to whole 256-word blocks
   std::vector<uint32_t> block0(n + 1, 0), item0(n + 1, 0), blk0(n + 1, 0);
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
     const lgx::Dims& dm = lats[i]->dm;
-    block0[i + 1] = block0[i] + (dm.total + 255) / 256;
-    if (lats[i]->rest) b->rest_blocks = block0[i + 1];
+    const bool step = i < b->nstep;
+    block0[i + 1] = block0[i] + (step ? (dm.total + 255) / 256 : 0);
+    if (step && lats[i]->rest) b->rest_blocks = block0[i + 1];
     item0[i + 1] = item0[i] + dm.h * dm.iw;
-    blk0[i + 1] = blk0[i] + (lats[i]->has_field ? lats[i]->bw * lats[i]->bh : 0);
+    blk0[i + 1] = blk0[i] + (step && lats[i]->has_field ? lats[i]->bw * lats[i]->bh : 0);
   }
   b->nblocks = block0[n];
   b->items_per_step = item0[n];
@@ -299,9 +430,10 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
     if (rc) return rc;
     LGX_CUDA(cudaGraphLaunch(ex, b->stream));
     b->graph_launches += 1;
-    const uint64_t per_step = (b->rest_blocks ? 1 : 0) + (b->nblocks > b->rest_blocks ? 1 : 0);
-    b->launches += len * (per_step + (b->hook ? 1 : 0)) + 1 + (sample ? 1 : 0) +
-                   (b->items_per_step ? 1 : 0);
+    const uint64_t per_step = b->nstep ? 1 : 0;
+    b->launches += len * (per_step + (b->hook ? 1 : 0)) + 1 +
+                   (sample && b->field_blocks ? 1 : 0) + (b->items_per_step ? 1 : 0) +
+                   b->classes.size();
     left -= len;
     since += len;
     if (sample) since = 0;
@@ -316,6 +448,16 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
 }
 
 int lgx_batch_advance(lgx_batch* b, uint64_t n) { return lgx_batch_advance_sampling(b, n, 0, 0.f); }
+
+int lgx_batch_plan(lgx_batch* b, lgx_batch_class* out, size_t cap, size_t* n) {
+  if (!b || !n || (cap && !out)) {
+    lgx::set_error("lgx_batch_plan: bad argument");
+    return LGX_ERR_ARG;
+  }
+  *n = b->plan.size();
+  for (size_t i = 0; i < b->plan.size() && i < cap; ++i) out[i] = b->plan[i];
+  return LGX_OK;
+}
 
 int lgx_batch_launch_count(lgx_batch* b, uint64_t* kernels, uint64_t* graphs) {
   if (!b) {

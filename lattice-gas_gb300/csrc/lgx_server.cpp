@@ -4,10 +4,11 @@
 // inflow) are submitted from any thread.  One server thread admits them
 // against a fixed device-memory budget, keeps every admitted lattice's planes
 // resident on the device, and advances all of them together in ticks: a tick
-// is as many steps as every resident lattice can take before one of them
-// reaches a sampling point or its end, run as one batched launch per step
-// (programmatic dependent launch), then one batched coarse-graining of the
-// lattices that are due.  A finished lattice's field, exact block sums and
+// is as many steps (up to 128) as every resident lattice can take before one
+// of them reaches its end, run as one batched launch per step (programmatic
+// dependent launch, both collision rules in one launch), with one batched
+// coarse-graining of exactly the lattices that reach a sampling point after
+// the steps where any do.  A finished lattice's field, exact block sums and
 // particle count are copied back (only the moments ever leave the device),
 // its memory returns to the pool, and waiting requests take its place the
 // next tick -- so requests arriving while others run join them on the GPU.
@@ -42,6 +43,7 @@
 namespace {
 
 constexpr int kRing = 4;
+constexpr size_t kMaxSamplePoints = 16;  // batched coarse-grainings per tick
 
 double now_s() {
   using namespace std::chrono;
@@ -105,9 +107,10 @@ struct lgx_server {
   std::vector<Req*> retiring;
   // tick ring
   struct Slot {
-    void* host = nullptr;   // pinned: descs | block0 | item0 | blk0
+    void* host = nullptr;   // pinned: descs | block0 | item0 | blk tables
     void* dev = nullptr;
-    cudaEvent_t ev = nullptr;
+    cudaEvent_t ev = nullptr;   // the tick's end
+    cudaEvent_t ev0 = nullptr;  // and its start, for the device time of ticks
     bool used = false;
   } ring[kRing];
   size_t slot_bytes = 0;
@@ -117,6 +120,7 @@ struct lgx_server {
   std::atomic<uint64_t> ticks{0}, launches{0}, site_updates{0};
   std::atomic<size_t> in_use_now{0};
   std::atomic<size_t> peak_bytes{0}, peak_active{0};
+  std::atomic<uint64_t> gpu_busy_ns{0};  // device time of finished ticks
   int fault_alloc = 0;  // test hook: fail the next N admissions' allocation
   std::string fatal;
 };
@@ -232,22 +236,61 @@ void retire(lgx_server* s, Req* r) {
   s->retiring.push_back(r);
 }
 
-// One tick: every active lattice advances `len` steps; those that reach a
-// sampling point or their end are sampled.
+// Wait for a ring slot's tick and add its device time to the statistics.
+cudaError_t settle(lgx_server* s, lgx_server::Slot& slot) {
+  cudaError_t e = cudaEventSynchronize(slot.ev);
+  float ms = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, slot.ev0, slot.ev);
+  if (e == cudaSuccess) s->gpu_busy_ns += (uint64_t)(ms * 1e6);
+  slot.used = false;
+  return e;
+}
+
+// Sampling points a lattice reaches during a tick of `len` steps: k in
+// 1..len with since + k a multiple of its period, and its last step.
+template <typename F>
+void due_points(const Req* r, uint64_t len, F&& mark) {
+  const uint64_t every = r->spec.sample_every;
+  if (every == 0) return;
+  for (uint64_t k = every - r->since; k <= len; k += every) mark(k);
+  const uint64_t left = r->spec.steps - r->steps_done;
+  if (left <= len && (r->since + left) % every != 0) mark(left);  // once, if not a multiple
+}
+
+// One tick: every active lattice advances `len` steps (fewer if the tick would
+// hold more than kMaxSamplePoints sampling points); after each step at which
+// some lattices reach a sampling point, one batched coarse-graining of exactly
+// those lattices.
 cudaError_t tick(lgx_server* s, uint64_t len) {
   auto& slot = s->ring[s->next_slot];
   s->next_slot = (s->next_slot + 1) % kRing;
   if (slot.used) {
-    cudaError_t e = cudaEventSynchronize(slot.ev);
+    cudaError_t e = settle(s, slot);
     if (e != cudaSuccess) return e;
   }
   slot.used = true;
   const size_t n = s->active.size();
+  // the steps after which someone samples, at most kMaxSamplePoints of them
+  std::vector<char> mark(len + 1, 0);
+  for (Req* r : s->active) due_points(r, len, [&](uint64_t k) { mark[k] = 1; });
+  std::vector<uint32_t> pts;
+  for (uint64_t k = 1; k <= len; ++k) {
+    if (!mark[k]) continue;
+    if (pts.size() == kMaxSamplePoints) {
+      len = pts.back();
+      break;
+    }
+    pts.push_back((uint32_t)k);
+  }
+  // slot layout for this tick: descs[n] | block0[n+1] | item0[n+1] | blk[m][n+1]
+  const size_t m = pts.size();
   lgx::LatDesc* descs = (lgx::LatDesc*)slot.host;
-  uint32_t* block0 = (uint32_t*)(descs + s->max_active);
-  uint32_t* item0 = block0 + s->max_active + 1;
-  uint32_t* blk0 = item0 + s->max_active + 1;
-  block0[0] = item0[0] = blk0[0] = 0;
+  uint32_t* block0 = (uint32_t*)(descs + n);
+  uint32_t* item0 = block0 + n + 1;
+  uint32_t* blk = item0 + n + 1;
+  const size_t bytes = n * sizeof(lgx::LatDesc) + (2 + m) * (n + 1) * sizeof(uint32_t);
+  block0[0] = item0[0] = 0;
+  for (size_t j = 0; j < m; ++j) blk[j * (n + 1)] = 0;
   uint32_t rest_blocks = 0;
   for (size_t i = 0; i < n; ++i) {
     Req* r = s->active[i];
@@ -273,48 +316,49 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     block0[i + 1] = block0[i] + (r->dm.total + 255) / 256;
     if (r->spec.rest_particles) rest_blocks = block0[i + 1];
     item0[i + 1] = item0[i] + (uint32_t)len * r->dm.h * r->dm.iw;
-    const uint64_t every = r->spec.sample_every;
-    const bool due = every > 0 && (r->since + len >= every || r->steps_done + len == r->spec.steps);
-    blk0[i + 1] = blk0[i] + (due ? r->bw * r->bh : 0);
+    for (size_t j = 0; j < m; ++j) blk[j * (n + 1) + i + 1] = blk[j * (n + 1) + i];
+    due_points(r, len, [&](uint64_t k) {
+      const size_t j = std::lower_bound(pts.begin(), pts.end(), (uint32_t)k) - pts.begin();
+      blk[j * (n + 1) + i + 1] = blk[j * (n + 1) + i] + r->bw * r->bh;
+    });
   }
   uint8_t* dev = (uint8_t*)slot.dev;
   lgx::LatDesc* d_descs = (lgx::LatDesc*)dev;
-  uint32_t* d_block0 = (uint32_t*)(d_descs + s->max_active);
-  uint32_t* d_item0 = d_block0 + s->max_active + 1;
-  uint32_t* d_blk0 = d_item0 + s->max_active + 1;
-  cudaError_t e = cudaMemcpyAsync(slot.dev, slot.host, s->slot_bytes, cudaMemcpyHostToDevice,
-                                  s->stream);
+  uint32_t* d_block0 = (uint32_t*)(d_descs + n);
+  uint32_t* d_item0 = d_block0 + n + 1;
+  uint32_t* d_blk = d_item0 + n + 1;
+  cudaError_t e = cudaEventRecord(slot.ev0, s->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(slot.dev, slot.host, bytes, cudaMemcpyHostToDevice, s->stream);
   const uint32_t nl = (uint32_t)n;
   if (e == cudaSuccess && item0[n]) {
     lgx::BatchInletArgs ia{d_descs, d_item0, nl, item0[n], s->d_zero};
     e = lgx::launch_batch_inlet(ia, s->stream);
     s->launches += 1;
   }
+  const int rule = rest_blocks == block0[n] ? lgx::kRuleRest
+                   : rest_blocks == 0     ? lgx::kRuleNoRest
+                                          : lgx::kRuleMixed;
+  size_t j = 0;
   for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
-    if (rest_blocks) {
-      lgx::BatchStepArgs sa{d_descs, d_block0, nl, s->d_zero, k, 0};
-      e = lgx::launch_batch_step(sa, rest_blocks, true, s->stream);
-      s->launches += 1;
-    }
-    if (e == cudaSuccess && block0[n] > rest_blocks) {
-      lgx::BatchStepArgs sa{d_descs, d_block0, nl, s->d_zero, k, rest_blocks};
-      e = lgx::launch_batch_step(sa, block0[n] - rest_blocks, false, s->stream);
-      s->launches += 1;
-    }
-  }
-  if (e == cudaSuccess && blk0[n]) {
-    lgx::BatchSampleArgs sp{d_descs, d_blk0, nl, blk0[n], s->d_zero, (uint32_t)len};
-    e = lgx::launch_batch_sample(sp, s->stream);
+    lgx::BatchStepArgs sa{d_descs, d_block0, nl, s->d_zero, k, 0};
+    e = lgx::launch_batch_step(sa, block0[n], rule, s->stream);
     s->launches += 1;
+    if (e == cudaSuccess && j < m && pts[j] == k + 1) {
+      const uint32_t* tb = blk + j * (n + 1);
+      lgx::BatchSampleArgs sp{d_descs, d_blk + j * (n + 1), nl, tb[n], s->d_zero, k + 1};
+      e = lgx::launch_batch_sample(sp, s->stream);
+      s->launches += 1;
+      ++j;
+    }
   }
   if (e == cudaSuccess) e = cudaEventRecord(slot.ev, s->stream);
   if (e != cudaSuccess) return e;
   s->ticks += 1;
   for (Req* r : s->active) {
     const uint64_t every = r->spec.sample_every;
-    const bool due = every > 0 && (r->since + len >= every || r->steps_done + len == r->spec.steps);
     r->steps_done += len;
-    r->since = due ? 0 : r->since + len;
+    r->since = every ? (r->since + len) % every : 0;
     r->cur ^= (int)(len & 1u);
     s->site_updates += (uint64_t)r->spec.w * r->spec.h * len;
   }
@@ -393,6 +437,8 @@ void serve(lgx_server* s) {
       }
     }
     if (s->active.empty()) {
+      for (auto& sl : s->ring)  // idle: account the ticks still in the ring
+        if (sl.used) settle(s, sl);
       if (s->retiring.empty())
         s->cv.wait_for(lk, std::chrono::milliseconds(2));
       else {
@@ -402,12 +448,10 @@ void serve(lgx_server* s) {
       }
       continue;
     }
-    // the tick: up to the nearest sampling point or end among the residents
+    // the tick: up to the nearest end among the residents (sampling points
+    // fall inside it)
     uint64_t len = lgx::kInletChunk;
-    for (Req* r : s->active) {
-      len = std::min<uint64_t>(len, r->spec.steps - r->steps_done);
-      if (r->spec.sample_every) len = std::min<uint64_t>(len, r->spec.sample_every - r->since);
-    }
+    for (Req* r : s->active) len = std::min<uint64_t>(len, r->spec.steps - r->steps_done);
     lk.unlock();
     cudaError_t e = tick(s, len);
     lk.lock();
@@ -487,11 +531,13 @@ int lgx_server_create(size_t budget_bytes, size_t max_active, lgx_server** out) 
     uint64_t keep = UINT64_MAX;  // keep freed memory in the pool between ticks
     e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  s->slot_bytes = max_active * sizeof(lgx::LatDesc) + 3 * (max_active + 1) * sizeof(uint32_t);
+  s->slot_bytes = max_active * sizeof(lgx::LatDesc) +
+                  (2 + kMaxSamplePoints) * (max_active + 1) * sizeof(uint32_t);
   for (int i = 0; i < kRing && e == cudaSuccess; ++i) {
     e = cudaHostAlloc(&s->ring[i].host, s->slot_bytes, cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaMalloc(&s->ring[i].dev, s->slot_bytes);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ring[i].ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ring[i].ev);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ring[i].ev0);
   }
   if (e == cudaSuccess) e = cudaMalloc(&s->d_zero, sizeof(uint64_t));
   if (e == cudaSuccess) e = cudaMemset(s->d_zero, 0, sizeof(uint64_t));
@@ -522,6 +568,7 @@ int lgx_server_destroy(lgx_server* s) {
     if (sl.host) cudaFreeHost(sl.host);
     if (sl.dev) cudaFree(sl.dev);
     if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.ev0) cudaEventDestroy(sl.ev0);
   }
   cudaFree(s->d_zero);
   if (s->pool) cudaMemPoolDestroy(s->pool);
@@ -698,6 +745,7 @@ int lgx_server_get_stats(lgx_server* s, lgx_server_stats* out) {
   out->bytes_in_use = s->in_use_now;
   out->peak_bytes = s->peak_bytes;
   out->peak_active = s->peak_active;
+  out->gpu_busy_ns = s->gpu_busy_ns;
   out->active = s->active.size();
   out->queued = s->pending.size();
   for (auto& kv : s->reqs) {

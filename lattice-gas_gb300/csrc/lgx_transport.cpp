@@ -201,7 +201,8 @@ int new_batch(Run& r, const std::vector<lgx_lattice*>& lats) {
     lgx_batch_destroy(r.batch);
     r.batch = nullptr;
   }
-  LGX_RC(lgx_batch_create(lats.data(), lats.size(), &r.batch));
+  // every step is followed by the profile hook, so no lattice may be resident
+  LGX_RC(lgx_batch_create_ex(lats.data(), lats.size(), LGX_BATCH_PER_STEP, &r.batch));
   return lgx::batch_set_step_hook(r.batch, profile_hook, &r);
 }
 

@@ -1,0 +1,189 @@
+// lgx_tune.cpp -- how to step a size class of lattices, chosen by measurement.
+//
+// A batch groups its small lattices into size classes (words per lattice
+// rounded up to a power of two).  For each class the tuner times, on
+// synthetic lattices of the class's size and count, the two ways the batch can
+// step it: one batched launch per step, or the resident kernel (a cluster of
+// csize CTAs of `threads` threads per lattice, all steps of an interval in one
+// launch) for every cluster shape that gives each warp between one and
+// sixteen 32-word chunks.  The fastest wins.  Results are kept per device and
+// class for the life of the process, so a class is timed once.
+//
+// The synthetic lattices are zero-filled: the step's work does not depend on
+// the state (the collision is a fixed circuit, the draws a fixed chain), only
+// on the word count and the obstacle summary, which is clear.
+#include <cuda_runtime.h>
+
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "lgx_batch.hpp"
+#include "lgx_tune.hpp"
+
+namespace lgx {
+namespace {
+
+constexpr uint32_t kTuneSteps = 48;
+constexpr size_t kTuneMaxWords = 4u << 20;  // per-plane words of all synthetic lattices
+
+std::mutex g_mu;
+std::map<std::tuple<int, uint32_t, uint32_t, bool>, ClassPlan> g_plans;
+
+struct Scratch {
+  std::vector<void*> ptrs;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ~Scratch() {
+    if (st) cudaStreamSynchronize(st);
+    for (void* p : ptrs) cudaFree(p);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+  }
+  cudaError_t alloc(void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) {
+      ptrs.push_back(*p);
+      e = cudaMemsetAsync(*p, 0, bytes, st);
+    }
+    return e;
+  }
+};
+
+cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
+  Scratch s;
+  cudaError_t e = cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&s.e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&s.e1);
+  if (e != cudaSuccess) return e;
+  // a lattice of `words` words: 64-word rows (or fewer), an even row count
+  const uint32_t wpr = std::min<uint32_t>(64, std::max<uint32_t>(1, words / 8));
+  uint32_t h = std::max<uint32_t>(6, (words + wpr - 1) / wpr);
+  h += h & 1u;
+  const Dims dm = make_dims(wpr * 32u, h, 0);
+  const uint32_t n = (uint32_t)std::max<size_t>(
+      1, std::min<size_t>(count, kTuneMaxWords / dm.total));
+  void *planes, *zero, *descs, *sched, *block0, *base;
+  e = s.alloc(&planes, (size_t)n * 2 * 7 * dm.total * 4);
+  if (e == cudaSuccess) e = s.alloc(&zero, (size_t)dm.total * 4 + ((dm.total + 31) / 32) * 4);
+  if (e == cudaSuccess) e = s.alloc(&descs, (size_t)n * sizeof(LatDesc));
+  if (e == cudaSuccess) e = s.alloc(&sched, (size_t)n * sizeof(ResSched));
+  if (e == cudaSuccess) e = s.alloc(&block0, (size_t)(n + 1) * 4);
+  if (e == cudaSuccess) e = s.alloc(&base, 8);
+  if (e != cudaSuccess) return e;
+  std::vector<LatDesc> d(n);
+  std::vector<uint32_t> b0(n + 1, 0);
+  for (uint32_t i = 0; i < n; ++i) {
+    LatDesc& x = d[i];
+    memset(&x, 0, sizeof(x));
+    x.planes[0] = (uint32_t*)planes + (size_t)i * 14 * dm.total;
+    x.planes[1] = x.planes[0] + 7 * (size_t)dm.total;
+    x.solid = (const uint32_t*)zero;
+    x.anysolid = (const uint32_t*)zero + dm.total;
+    x.dm = dm;
+    x.seed = i;
+    x.rest = rest ? 1u : 0u;
+    b0[i + 1] = b0[i] + (dm.total + 255) / 256;
+  }
+  e = cudaMemcpyAsync(descs, d.data(), n * sizeof(LatDesc), cudaMemcpyHostToDevice, s.st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(block0, b0.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s.st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s.st);
+  if (e != cudaSuccess) return e;
+
+  auto time_it = [&](auto&& run, float* us) -> cudaError_t {
+    cudaError_t r = run();  // warm-up (and first-launch costs)
+    if (r == cudaSuccess) r = cudaEventRecord(s.e0, s.st);
+    if (r == cudaSuccess) r = run();
+    if (r == cudaSuccess) r = cudaEventRecord(s.e1, s.st);
+    if (r == cudaSuccess) r = cudaEventSynchronize(s.e1);
+    float ms = 0;
+    if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, s.e0, s.e1);
+    *us = ms * 1e3f / kTuneSteps;
+    return r;
+  };
+  // one launch per step, replayed from a graph as the batch replays it
+  const int rule = rest ? kRuleRest : kRuleNoRest;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  e = cudaStreamBeginCapture(s.st, cudaStreamCaptureModeThreadLocal);
+  for (uint32_t k = 0; k < kTuneSteps && e == cudaSuccess; ++k) {
+    BatchStepArgs sa{(const LatDesc*)descs, (const uint32_t*)block0, n, (const uint64_t*)base,
+                     k, 0};
+    e = launch_batch_step(sa, b0[n], rule, s.st);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(s.st, &graph);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e == cudaSuccess) e = time_it([&]() { return cudaGraphLaunch(exec, s.st); }, &out->step_us);
+  if (exec) {
+    cudaStreamSynchronize(s.st);
+    cudaGraphExecDestroy(exec);
+  }
+  if (e != cudaSuccess) return e;
+  out->resident = false;
+  out->csize = out->threads = 0;
+  out->resident_us = 0;
+  out->tuned_count = n;
+  const uint32_t nchunks = (dm.total + 31) / 32;
+  for (uint32_t cs : {1u, 2u, 4u, 8u, 16u})
+    for (uint32_t th : {128u, 256u, 512u, 1024u}) {
+      const uint32_t warps = cs * th / 32;
+      if (warps > nchunks || warps * 16 < nchunks) continue;
+      float us = 0;
+      ResidentArgs ra{(const LatDesc*)descs, (const ResSched*)sched, 0, (const uint64_t*)base,
+                      kTuneSteps};
+      cudaError_t r = time_it([&]() { return launch_resident(ra, n, cs, th, s.st); }, &us);
+      if (r != cudaSuccess) {
+        cudaGetLastError();  // a cluster shape this device cannot place: skip it
+        continue;
+      }
+      if (out->resident_us == 0 || us < out->resident_us) {
+        out->resident_us = us;
+        out->csize = cs;
+        out->threads = th;
+      }
+    }
+  out->resident = out->resident_us > 0 && out->resident_us < out->step_us;
+  return cudaSuccess;
+}
+
+}  // namespace
+
+uint32_t class_bucket(uint32_t words) {
+  uint32_t b = 64;
+  while (b < words) b <<= 1;
+  return b;
+}
+
+cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
+  const uint32_t wb = class_bucket(words);
+  uint32_t cb = 1;
+  while (cb < count) cb <<= 1;
+  const auto key = std::make_tuple(device, wb, cb, rest);
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) {
+      *out = it->second;
+      return cudaSuccess;
+    }
+  }
+  ClassPlan p{};
+  cudaError_t e = measure(wb, cb, rest, &p);
+  if (e != cudaSuccess) return e;
+  p.words = wb;
+  p.count = cb;
+  std::lock_guard<std::mutex> g(g_mu);
+  g_plans[key] = p;
+  *out = p;
+  return cudaSuccess;
+}
+
+}  // namespace lgx

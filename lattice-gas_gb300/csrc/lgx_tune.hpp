@@ -1,0 +1,29 @@
+// lgx_tune.hpp -- the size-class tuner (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lgx {
+
+// Lattices up to this many words per plane may be stepped by the resident kernel.
+constexpr uint32_t kResidentMaxWords = 32768;
+
+// How a size class is stepped, and what the choice was based on (microseconds
+// per step of the class's synthetic lattices, each way).
+struct ClassPlan {
+  bool resident;
+  uint32_t csize, threads;  // cluster shape of the resident kernel
+  float step_us, resident_us;
+  uint32_t words, count;    // the class: words per lattice and lattice count, rounded up
+  uint32_t tuned_count;     // synthetic lattices actually timed
+};
+
+// Words per lattice rounded up to the class's power of two (at least 64).
+uint32_t class_bucket(uint32_t words);
+
+// The plan for `count` lattices of up to `words` words on `device` (the
+// current device), timed on first use and cached for the process.
+cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ClassPlan* out);
+
+}  // namespace lgx

@@ -52,7 +52,8 @@ class Request(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "cancelled", "active", "queued",
                                           "ticks", "kernel_launches", "site_updates",
-                                          "bytes_in_use", "peak_bytes", "peak_active")]
+                                          "bytes_in_use", "peak_bytes", "peak_active",
+                                          "gpu_busy_ns")]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
@@ -67,6 +68,19 @@ class Transport(C.Structure):
                 ("window_g", C.c_uint64), ("u_actual", C.c_float),
                 ("mode_nu", C.c_double * (2 * TRANSPORT_SAMPLES)),
                 ("mode_g", C.c_double * (2 * TRANSPORT_SAMPLES))]
+
+
+BATCH_AUTO, BATCH_PER_STEP, BATCH_RESIDENT = 0, 1, 2
+
+
+class BatchClass(C.Structure):
+    """lgx_batch_class: one size class of a batch and the tuner's timings."""
+    _fields_ = [("words", C.c_uint32), ("lattices", C.c_uint32), ("rest", C.c_int),
+                ("resident", C.c_int), ("cluster", C.c_uint32), ("threads", C.c_uint32),
+                ("step_us", C.c_float), ("resident_us", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class LgxError(RuntimeError):
@@ -149,6 +163,8 @@ def lib():
         _sig(L, "lgx_byte_total_particles", vp, C.POINTER(C.c_uint64))
         _sig(L, "lgx_byte_steps", vp, C.POINTER(C.c_uint64))
         _sig(L, "lgx_batch_create", C.POINTER(vp), sz, C.POINTER(vp))
+        _sig(L, "lgx_batch_create_ex", C.POINTER(vp), sz, C.c_int, C.POINTER(vp))
+        _sig(L, "lgx_batch_plan", vp, C.POINTER(BatchClass), sz, C.POINTER(sz))
         _sig(L, "lgx_batch_destroy", vp)
         _sig(L, "lgx_batch_advance_sampling", vp, C.c_uint64, C.c_uint64, C.c_float)
         _sig(L, "lgx_batch_advance", vp, C.c_uint64)
@@ -420,11 +436,21 @@ class Batch:
     each sampling interval a replayed CUDA graph.  The lattices stay owned by
     the caller; advance them only through the batch while it is alive."""
 
-    def __init__(self, lattices):
+    def __init__(self, lattices, policy=BATCH_AUTO):
         self.lattices = list(lattices)
         arr = (vp * len(self.lattices))(*[l.handle.value for l in self.lattices])
         self._h = vp()
-        _check(lib().lgx_batch_create(arr, len(self.lattices), C.byref(self._h)))
+        _check(lib().lgx_batch_create_ex(arr, len(self.lattices), int(policy),
+                                         C.byref(self._h)))
+
+    @property
+    def plan(self):
+        """The size classes of the batch's small lattices, as the tuner planned them."""
+        n = C.c_size_t()
+        _check(lib().lgx_batch_plan(self._h, None, 0, C.byref(n)))
+        out = (BatchClass * max(n.value, 1))()
+        _check(lib().lgx_batch_plan(self._h, out, n.value, C.byref(n)))
+        return [out[i].as_dict() for i in range(n.value)]
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -59,27 +59,49 @@ SPECS = [
 ]
 
 
+POLICIES = [0, 1, 2]  # LG.BATCH_AUTO, BATCH_PER_STEP, BATCH_RESIDENT
+
+
+@pytest.mark.parametrize("policy", POLICIES)
 @pytest.mark.parametrize("n,every", [(1, 0), (37, 0), (300, 50), (257, 100), (400, 500)])
-def test_batch_equals_each_lattice_alone(LG, n, every):
+def test_batch_equals_each_lattice_alone(LG, n, every, policy):
     specs = make(LG, SPECS)
     alone = [build(LG, s) for s in specs]
     for g in alone:
         g.advance_sampling(n, every, 0.4)
     together = [build(LG, s) for s in specs]
-    b = LG.Batch(together)
+    b = LG.Batch(together, policy)
     b.advance_sampling(n, every, 0.4)
     for x, y in zip(alone, together):
         same(snapshot(x), snapshot(y))
     b.close()
 
 
-def test_batch_replays_and_continues(LG):
+def test_resident_policy_plans_small_classes(LG):
+    """Every class of up to 32768 words is listed; under BATCH_RESIDENT those with
+    a usable cluster shape run resident, under BATCH_PER_STEP none does."""
+    specs = make(LG, SPECS)
+    lats = [build(LG, s) for s in specs]
+    plan = LG.Batch(lats, LG.BATCH_RESIDENT).plan
+    words = sorted({c["words"] for c in plan})
+    assert words == sorted({max(64, 1 << (((w + 31) // 32 * h) - 1).bit_length())
+                            for w, h, *_ in SPECS if (w + 31) // 32 * h <= 32768})
+    assert all(c["resident"] == (c["cluster"] > 0) for c in plan)
+    assert any(c["resident"] for c in plan)
+    assert sum(c["lattices"] for c in plan) == sum(
+        1 for w, h, *_ in SPECS if (w + 31) // 32 * h <= 32768)
+    lats2 = [build(LG, s) for s in specs]
+    assert not any(c["resident"] for c in LG.Batch(lats2, LG.BATCH_PER_STEP).plan)
+
+
+@pytest.mark.parametrize("policy", POLICIES)
+def test_batch_replays_and_continues(LG, policy):
     """Several calls (graph replays, mixed lengths), then a plain advance after
     the batch: still identical to the lattices run alone throughout."""
     specs = make(LG, SPECS[:4])
     alone = [build(LG, s) for s in specs]
     together = [build(LG, s) for s in specs]
-    b = LG.Batch(together)
+    b = LG.Batch(together, policy)
     for n, every in ((100, 50), (100, 50), (33, 0), (150, 50)):
         for g in alone:
             g.advance_sampling(n, every, 1.0)
@@ -91,10 +113,11 @@ def test_batch_replays_and_continues(LG):
         same(snapshot(x), snapshot(y))
 
 
-def test_batch_matches_oracle(LG, O):
+@pytest.mark.parametrize("policy", [1, 2])
+def test_batch_matches_oracle(LG, O, policy):
     specs = make(LG, SPECS[:5])
     together = [build(LG, s) for s in specs]
-    b = LG.Batch(together)
+    b = LG.Batch(together, policy)
     b.advance_sampling(120, 40, 0.5)
     for (w, h, rest, inlet, block, seed, cells), g in zip(specs, together):
         o = O.BitplaneLattice(w, h, rest, seed, 4)
@@ -112,7 +135,7 @@ def test_batch_matches_oracle(LG, O):
 
 def test_transport_sweep_batch_equals_alone(LG):
     """The 64-lattice transport sweep (shear-wave starts, 16x16 blocks every 50
-    steps), 200 steps: batch == each alone."""
+    steps), 200 steps: batch == each alone, under every policy."""
     from lattice_gas import workloads as W
     wls = W.transport_sweep()
     def mk(wl):
@@ -123,11 +146,13 @@ def test_transport_sweep_batch_equals_alone(LG):
     alone = [mk(wl) for wl in wls]
     for g in alone:
         g.advance_sampling(200, 50, 1.0)
-    together = [mk(wl) for wl in wls]
-    b = LG.Batch(together)
-    b.advance_sampling(200, 50, 1.0)
-    for x, y in zip(alone, together):
-        same(snapshot(x), snapshot(y))
+    for policy in POLICIES:
+        together = [mk(wl) for wl in wls]
+        b = LG.Batch(together, policy)
+        b.advance_sampling(200, 50, 1.0)
+        for x, y in zip(alone, together):
+            same(snapshot(x), snapshot(y))
+        b.close()
 
 
 def test_batch_rejects_bad_arguments(LG):
