@@ -51,7 +51,7 @@ __device__ __forceinline__ uint32_t owner_of(const uint32_t* prefix, uint32_t n,
 template <bool REST>
 __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
-  const uint32_t li = owner_of(p.block0, p.nlat, blk);
+  const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
   uint32_t g = (blk - __ldg(p.block0 + li)) * (uint32_t)kThreads + threadIdx.x;
   const bool live = g < d.dm.total;
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepAr
 // lattices, to keep one launch per step.
 __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_mixed_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
-  const uint32_t li = owner_of(p.block0, p.nlat, blk);
+  const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
   uint32_t g = (blk - __ldg(p.block0 + li)) * (uint32_t)kThreads + threadIdx.x;
   const bool live = g < d.dm.total;
@@ -134,6 +134,12 @@ __global__ void __launch_bounds__(256) lgx_batch_sample_kernel(BatchSampleArgs p
 
 __global__ void lgx_batch_base_kernel(uint64_t* base, uint32_t n) { *base += n; }
 
+__global__ void lgx_batch_owner_kernel(const uint32_t* block0, uint32_t nlat, uint32_t nblocks,
+                                       uint32_t* owner) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nblocks) owner[b] = owner_of(block0, nlat, b);
+}
+
 }  // namespace
 
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule,
@@ -161,6 +167,13 @@ cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st) {
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st) {
   if (a.total_blocks == 0) return cudaSuccess;
   lgx_batch_sample_kernel<<<(a.total_blocks + 7) / 8, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_owner(const uint32_t* block0, uint32_t nlat, uint32_t nblocks,
+                               uint32_t* owner, cudaStream_t st) {
+  if (nblocks == 0) return cudaSuccess;
+  lgx_batch_owner_kernel<<<(nblocks + 255) / 256, 256, 0, st>>>(block0, nlat, nblocks, owner);
   return cudaGetLastError();
 }
 

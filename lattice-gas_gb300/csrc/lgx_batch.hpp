@@ -28,6 +28,7 @@ struct LatDesc {
 struct BatchStepArgs {
   const LatDesc* descs;
   const uint32_t* block0;  // prefix of per-lattice 256-word blocks, nlat + 1 entries
+  const uint32_t* owner;   // lattice of each block (null: binary search of block0)
   uint32_t nlat;
   const uint64_t* base;    // batch steps completed before this interval
   uint32_t k;              // step index within the interval
@@ -78,6 +79,9 @@ constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule,
                               cudaStream_t st);
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st);
+// owner[b] = the lattice whose blocks include block b, for b < nblocks.
+cudaError_t launch_batch_owner(const uint32_t* block0, uint32_t nlat, uint32_t nblocks,
+                               uint32_t* owner, cudaStream_t st);
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st);
 cudaError_t launch_batch_base(uint64_t* base, uint32_t n, cudaStream_t st);
 

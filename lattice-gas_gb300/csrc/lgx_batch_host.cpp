@@ -59,6 +59,7 @@ struct lgx_batch {
   std::vector<lgx::LatDesc> descs;
   lgx::LatDesc* d_descs = nullptr;
   uint32_t* d_block0 = nullptr;
+  uint32_t* d_owner = nullptr;  // lattice of each per-step block
   uint32_t* d_item0 = nullptr;
   uint32_t* d_blk0 = nullptr;
   uint64_t* d_base = nullptr;
@@ -96,6 +97,7 @@ void free_batch(lgx_batch* b) {
   if (b->side) cudaStreamDestroy(b->side);
   cudaFree(b->d_descs);
   cudaFree(b->d_block0);
+  cudaFree(b->d_owner);
   cudaFree(b->d_item0);
   cudaFree(b->d_blk0);
   cudaFree(b->d_base);
@@ -179,7 +181,7 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
   }
   for (uint32_t k = 0; k < len && e == cudaSuccess && b->nstep; ++k) {
     // rest-particle lattices' blocks first, then the six-direction ones
-    lgx::BatchStepArgs sa{b->d_descs, b->d_block0, b->nstep, b->d_base, k, 0};
+    lgx::BatchStepArgs sa{b->d_descs, b->d_block0, b->d_owner, b->nstep, b->d_base, k, 0};
     e = lgx::launch_batch_step(sa, b->nblocks, step_rule(b->rest_blocks, b->nblocks),
                                b->stream);
     if (e == cudaSuccess && b->hook) e = b->hook(b->hook_ctx, b->stream, b->d_base, k + 1);
@@ -371,6 +373,10 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
   if (e == cudaSuccess) e = cudaMalloc(&b->d_base, sizeof(uint64_t));
   if (e == cudaSuccess)
     e = cudaMemcpy(b->d_block0, block0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && b->nblocks) e = cudaMalloc(&b->d_owner, (size_t)b->nblocks * 4);
+  if (e == cudaSuccess)
+    e = lgx::launch_batch_owner(b->d_block0, b->nstep, b->nblocks, b->d_owner, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   // The batched inlet kernel writes lattice i's draws for step s of the
   // interval at item (item0[i] * len + s * h * iw ...); lay the prefix out
   // for the longest interval and let each buffer hold kInletChunk steps.

@@ -6,7 +6,8 @@
 // a whole interval: its CTAs split the lattice's 32-word chunks between them,
 // run the step on their chunks, meet at a cluster barrier (release / acquire at
 // cluster scope, so every CTA's stores of the step are visible to the others'
-// loads of the next), and go on to the next step, all inside one launch.  The
+// loads of the next; the next step's draws are made between arrive and wait),
+// and go on to the next step, all inside one launch.  The
 // planes are read through L2 (ld.global.cg), never the read-only path, since
 // they change during the launch.  Sampling points are handled by the cluster
 // itself between steps: each CTA coarse-grains a fixed share of the field
@@ -26,7 +27,7 @@ namespace {
 
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArgs p) {
-  cg::cluster_group cluster = cg::this_cluster();
+  const cg::cluster_group cluster = cg::this_cluster();
   const uint32_t csize = cluster.num_blocks(), rank = cluster.block_rank();
   const uint32_t li = p.first_lat + blockIdx.x / csize;
   const LatDesc& d = p.descs[li];
@@ -39,6 +40,11 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
   const uint64_t base = p.base ? *p.base : 0ull;
   const uint32_t nb = d.bw * d.bh;
 
+  // The draws of a warp's first chunk for step k are made while the cluster
+  // barrier of step k - 1 is pending: they depend on (word, step) only.
+  const uint32_t cfirst = c0 + warp;
+  const uint32_t gfirst = min(cfirst * 32u + lane, dm.total - 1u);
+  Draws first = draws(gfirst ^ step_seed32(d.seed, d.steps0 + base));
   for (uint32_t k = 0; k < p.len; ++k) {
     const uint64_t local = base + k;
     const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
@@ -46,17 +52,20 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
     uint32_t* dst = par ? d.planes[0] : d.planes[1];
     const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
     const uint32_t* inlet = dm.iw ? d.inlet + (size_t)k * dm.h * dm.iw * 7u : nullptr;
-    for (uint32_t c = c0 + warp; c < c1; c += nw) {
+    for (uint32_t c = cfirst; c < c1; c += nw) {
       uint32_t g = c * 32u + lane;
       const bool live = g < dm.total;
       if (!live) g = dm.total - 1u;
-      const Draws s = draws(g ^ seed32);
+      const Draws s = c == cfirst ? first : draws(g ^ seed32);
       if (d.rest)
         step_word<true, true>(src, dst, d.solid, d.anysolid, inlet, dm, s, g, live);
       else
         step_word<false, true>(src, dst, d.solid, d.anysolid, inlet, dm, s, g, live);
     }
-    cluster.sync();
+    // arrive (stores released at cluster scope), draw ahead, then wait
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    if (k + 1u < p.len) first = draws(gfirst ^ step_seed32(d.seed, d.steps0 + local + 1u));
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     // sampling point after step k + 1 of this launch
     const uint32_t t = k + 1u;
     const bool due = nb && sch.every &&

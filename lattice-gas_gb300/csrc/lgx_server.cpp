@@ -111,6 +111,8 @@ struct lgx_server {
     void* dev = nullptr;
     cudaEvent_t ev = nullptr;   // the tick's end
     cudaEvent_t ev0 = nullptr;  // and its start, for the device time of ticks
+    uint32_t* owner = nullptr;  // lattice of each step block (stream-ordered allocation)
+    size_t owner_cap = 0;
     bool used = false;
   } ring[kRing];
   size_t slot_bytes = 0;
@@ -330,6 +332,18 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
   cudaError_t e = cudaEventRecord(slot.ev0, s->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(slot.dev, slot.host, bytes, cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess && block0[n] > slot.owner_cap) {  // grow the block-owner table
+    if (slot.owner) e = cudaFreeAsync(slot.owner, s->stream);
+    slot.owner = nullptr;
+    slot.owner_cap = 0;
+    const size_t cap = std::max<size_t>(block0[n], 2 * (size_t)block0[n]);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&slot.owner, cap * 4, s->stream);
+    if (e == cudaSuccess) slot.owner_cap = cap;
+  }
+  if (e == cudaSuccess) {
+    e = lgx::launch_batch_owner(d_block0, (uint32_t)n, block0[n], slot.owner, s->stream);
+    s->launches += 1;
+  }
   const uint32_t nl = (uint32_t)n;
   if (e == cudaSuccess && item0[n]) {
     lgx::BatchInletArgs ia{d_descs, d_item0, nl, item0[n], s->d_zero};
@@ -341,7 +355,7 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
                                           : lgx::kRuleMixed;
   size_t j = 0;
   for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
-    lgx::BatchStepArgs sa{d_descs, d_block0, nl, s->d_zero, k, 0};
+    lgx::BatchStepArgs sa{d_descs, d_block0, slot.owner, nl, s->d_zero, k, 0};
     e = lgx::launch_batch_step(sa, block0[n], rule, s->stream);
     s->launches += 1;
     if (e == cudaSuccess && j < m && pts[j] == k + 1) {
@@ -569,6 +583,7 @@ int lgx_server_destroy(lgx_server* s) {
     if (sl.dev) cudaFree(sl.dev);
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.ev0) cudaEventDestroy(sl.ev0);
+    if (sl.owner) cudaFree(sl.owner);
   }
   cudaFree(s->d_zero);
   if (s->pool) cudaMemPoolDestroy(s->pool);

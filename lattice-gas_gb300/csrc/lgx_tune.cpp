@@ -68,12 +68,13 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   const Dims dm = make_dims(wpr * 32u, h, 0);
   const uint32_t n = (uint32_t)std::max<size_t>(
       1, std::min<size_t>(count, kTuneMaxWords / dm.total));
-  void *planes, *zero, *descs, *sched, *block0, *base;
+  void *planes, *zero, *descs, *sched, *block0, *owner, *base;
   e = s.alloc(&planes, (size_t)n * 2 * 7 * dm.total * 4);
   if (e == cudaSuccess) e = s.alloc(&zero, (size_t)dm.total * 4 + ((dm.total + 31) / 32) * 4);
   if (e == cudaSuccess) e = s.alloc(&descs, (size_t)n * sizeof(LatDesc));
   if (e == cudaSuccess) e = s.alloc(&sched, (size_t)n * sizeof(ResSched));
   if (e == cudaSuccess) e = s.alloc(&block0, (size_t)(n + 1) * 4);
+  if (e == cudaSuccess) e = s.alloc(&owner, (size_t)n * ((dm.total + 255) / 256) * 4);
   if (e == cudaSuccess) e = s.alloc(&base, 8);
   if (e != cudaSuccess) return e;
   std::vector<LatDesc> d(n);
@@ -93,6 +94,8 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   e = cudaMemcpyAsync(descs, d.data(), n * sizeof(LatDesc), cudaMemcpyHostToDevice, s.st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(block0, b0.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s.st);
+  if (e == cudaSuccess)
+    e = launch_batch_owner((const uint32_t*)block0, n, b0[n], (uint32_t*)owner, s.st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s.st);
   if (e != cudaSuccess) return e;
 
@@ -113,8 +116,8 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   cudaGraphExec_t exec = nullptr;
   e = cudaStreamBeginCapture(s.st, cudaStreamCaptureModeThreadLocal);
   for (uint32_t k = 0; k < kTuneSteps && e == cudaSuccess; ++k) {
-    BatchStepArgs sa{(const LatDesc*)descs, (const uint32_t*)block0, n, (const uint64_t*)base,
-                     k, 0};
+    BatchStepArgs sa{(const LatDesc*)descs, (const uint32_t*)block0, (const uint32_t*)owner, n,
+                     (const uint64_t*)base, k, 0};
     e = launch_batch_step(sa, b0[n], rule, s.st);
   }
   cudaError_t e2 = cudaStreamEndCapture(s.st, &graph);
