@@ -7,12 +7,15 @@
 // steps of an interval in one launch) or with the rest, one batched launch
 // per step.  For each sampling interval the batch replays a CUDA graph
 // captured on first use:
-//   [batched inlet draws] -+-> L x batched step (programmatic dependent launch)
-//                          |   -> [batched coarse-graining]            -+-> counter += L
-//                          +-> one resident launch per class (own sampling) -+
+//   [batched inlet draws] -+-> chain 1: L x batched step (programmatic dependent launch) -+
+//                          +-> chain 2: L x batched step                                 -+
+//                          +-> one resident launch per class (own sampling)              -+
+//                                      -> [batched coarse-graining] -> counter += L
 // The graph holds only device pointers to the descriptor table and the step
 // counter, so one capture serves every interval of the same length.
 #include <cuda_runtime.h>
+
+#include <stdlib.h>
 
 #include <algorithm>
 #include <new>
@@ -31,6 +34,17 @@ struct GraphEntry {
   bool sample;
   cudaGraphExec_t exec;
   lgx::ResSched* sched;  // resident lattices' schedule for this interval shape
+};
+
+// A chain of per-step launches over lattices [first, first + count), with its
+// own block table; several chains run as parallel branches of the graph so
+// that one chain's launch gaps are filled by the others' blocks.
+struct StepGroup {
+  uint32_t first = 0, count = 0, nblocks = 0, rest_blocks = 0;
+  uint32_t* d_block0 = nullptr;
+  uint32_t* d_owner = nullptr;
+  cudaStream_t st = nullptr;  // null for the batch's own stream
+  cudaEvent_t done = nullptr;
 };
 
 // A size class on the resident kernel: lattices [first, first + count).
@@ -58,13 +72,11 @@ struct lgx_batch {
   std::vector<lgx_lattice*> lats;
   std::vector<lgx::LatDesc> descs;
   lgx::LatDesc* d_descs = nullptr;
-  uint32_t* d_block0 = nullptr;
-  uint32_t* d_owner = nullptr;  // lattice of each per-step block
   uint32_t* d_item0 = nullptr;
   uint32_t* d_blk0 = nullptr;
   uint64_t* d_base = nullptr;
   uint32_t nblocks = 0;
-  uint32_t rest_blocks = 0;     // leading blocks, those of rest-particle lattices
+  uint32_t rest_blocks = 0;     // leading per-step blocks, those of rest-particle lattices
   uint32_t items_per_step = 0;  // inlet draw items of one step, all lattices
   uint32_t field_blocks = 0;
   std::vector<uint32_t*> inlet_bufs;
@@ -80,9 +92,59 @@ struct lgx_batch {
   std::vector<lgx_batch_class> plan;  // every class, as reported
   cudaStream_t side = nullptr;        // resident launches' branch of the graph
   cudaEvent_t fork = nullptr, join = nullptr;
+  std::vector<StepGroup> groups;      // chains of per-step launches
 };
 
 namespace {
+
+// The per-step chains: contiguous runs of the per-step lattices, balanced by
+// blocks.  Two chains fill each other's launch gaps (+6% on the 64-lattice
+// transport sweep; three or four gain nothing more); LGX_BATCH_CHAINS
+// overrides the count at creation.
+void free_chains(lgx_batch* b) {
+  for (auto& g : b->groups) {
+    cudaFree(g.d_block0);
+    cudaFree(g.d_owner);
+    if (g.done) cudaEventDestroy(g.done);
+    if (g.st) cudaStreamDestroy(g.st);
+  }
+  b->groups.clear();
+}
+
+cudaError_t build_chains(lgx_batch* b, uint32_t ngroups) {
+  free_chains(b);
+  ngroups = std::min<uint32_t>(ngroups, b->nstep);
+  std::vector<uint32_t> block0(b->nstep + 1, 0);
+  for (uint32_t i = 0; i < b->nstep; ++i)
+    block0[i + 1] = block0[i] + (b->lats[i]->dm.total + 255) / 256;
+  cudaError_t e = cudaSuccess;
+  for (uint32_t g = 0, i = 0; g < ngroups && e == cudaSuccess; ++g) {
+    StepGroup sg;
+    sg.first = i;
+    const uint64_t target = (uint64_t)block0[b->nstep] * (g + 1) / ngroups;
+    std::vector<uint32_t> gb0(1, 0);
+    while (i < b->nstep && (g + 1 == ngroups || block0[i] < target || sg.count == 0)) {
+      gb0.push_back(gb0.back() + block0[i + 1] - block0[i]);
+      if (b->lats[i]->rest) sg.rest_blocks = gb0.back();
+      ++sg.count;
+      ++i;
+    }
+    if (sg.count == 0) continue;
+    sg.nblocks = gb0.back();
+    b->groups.push_back(sg);
+    StepGroup& G = b->groups.back();
+    e = cudaMalloc(&G.d_block0, gb0.size() * 4);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(G.d_block0, gb0.data(), gb0.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && G.nblocks) e = cudaMalloc(&G.d_owner, (size_t)G.nblocks * 4);
+    if (e == cudaSuccess)
+      e = lgx::launch_batch_owner(G.d_block0, G.count, G.nblocks, G.d_owner, b->stream);
+    if (e == cudaSuccess && g > 0) e = cudaStreamCreateWithFlags(&G.st, cudaStreamNonBlocking);
+    if (e == cudaSuccess && g > 0) e = cudaEventCreateWithFlags(&G.done, cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  return e;
+}
 
 void free_batch(lgx_batch* b) {
   cudaSetDevice(b->device);
@@ -92,12 +154,11 @@ void free_batch(lgx_batch* b) {
     cudaFree(g.sched);
   }
   for (auto* p : b->inlet_bufs) cudaFree(p);
+  free_chains(b);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
   if (b->side) cudaStreamDestroy(b->side);
   cudaFree(b->d_descs);
-  cudaFree(b->d_block0);
-  cudaFree(b->d_owner);
   cudaFree(b->d_item0);
   cudaFree(b->d_blk0);
   cudaFree(b->d_base);
@@ -168,29 +229,40 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
     // the item prefix scales with the interval length
     e = lgx::launch_batch_inlet(ia, b->stream);
   }
-  // the resident classes on their own branch, when there is a per-step chain
-  cudaStream_t rs = b->nstep ? b->side : b->stream;
-  if (e == cudaSuccess && !b->classes.empty() && b->nstep) {
-    e = cudaEventRecord(b->fork, b->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork, 0);
-  }
+  // branches: the resident classes (when there is also a per-step chain) and
+  // every per-step chain after the first
+  const bool res_branch = !b->classes.empty() && b->nstep;
+  const bool fork = res_branch || b->groups.size() > 1;
+  if (e == cudaSuccess && fork) e = cudaEventRecord(b->fork, b->stream);
+  if (e == cudaSuccess && res_branch) e = cudaStreamWaitEvent(b->side, b->fork, 0);
+  for (size_t g = 1; g < b->groups.size() && e == cudaSuccess; ++g)
+    e = cudaStreamWaitEvent(b->groups[g].st, b->fork, 0);
+  cudaStream_t rs = res_branch ? b->side : b->stream;
   for (const ResClass& c : b->classes) {
     if (e != cudaSuccess) break;
     lgx::ResidentArgs ra{b->d_descs, sched, c.first, b->d_base, len};
     e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, rs);
   }
-  for (uint32_t k = 0; k < len && e == cudaSuccess && b->nstep; ++k) {
-    // rest-particle lattices' blocks first, then the six-direction ones
-    lgx::BatchStepArgs sa{b->d_descs, b->d_block0, b->d_owner, b->nstep, b->d_base, k, 0};
-    e = lgx::launch_batch_step(sa, b->nblocks, step_rule(b->rest_blocks, b->nblocks),
-                               b->stream);
-    if (e == cudaSuccess && b->hook) e = b->hook(b->hook_ctx, b->stream, b->d_base, k + 1);
+  for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; ++g) {
+    const StepGroup& sg = b->groups[g];
+    cudaStream_t st = sg.st ? sg.st : b->stream;
+    for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
+      // rest-particle lattices' blocks first, then the six-direction ones
+      lgx::BatchStepArgs sa{b->d_descs + sg.first, sg.d_block0, sg.d_owner, sg.count,
+                            b->d_base, k, 0};
+      e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks), st);
+      if (e == cudaSuccess && b->hook) e = b->hook(b->hook_ctx, st, b->d_base, k + 1);
+    }
+    if (e == cudaSuccess && sg.st) {
+      e = cudaEventRecord(sg.done, sg.st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, sg.done, 0);
+    }
   }
   if (e == cudaSuccess && sample && b->field_blocks) {
     lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, b->nstep, b->field_blocks, b->d_base, len};
     e = lgx::launch_batch_sample(sp, b->stream);
   }
-  if (e == cudaSuccess && !b->classes.empty() && b->nstep) {
+  if (e == cudaSuccess && res_branch) {
     e = cudaEventRecord(b->join, b->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->join, 0);
   }
@@ -240,6 +312,7 @@ int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx) {
   }
   LGX_CUDA(cudaSetDevice(b->device));
   LGX_CUDA(cudaStreamSynchronize(b->stream));
+  if (fn && b->groups.size() > 1) LGX_CUDA(build_chains(b, 1));  // the hook follows every step
   for (auto& g : b->graphs) {
     cudaGraphExecDestroy(g.exec);
     cudaFree(g.sched);
@@ -367,15 +440,12 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
   b->items_per_step = item0[n];
   b->field_blocks = blk0[n];
   if (e == cudaSuccess) e = cudaMalloc(&b->d_descs, n * sizeof(lgx::LatDesc));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_block0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_item0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_blk0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_base, sizeof(uint64_t));
-  if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_block0, block0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && b->nblocks) e = cudaMalloc(&b->d_owner, (size_t)b->nblocks * 4);
-  if (e == cudaSuccess)
-    e = lgx::launch_batch_owner(b->d_block0, b->nstep, b->nblocks, b->d_owner, b->stream);
+  uint32_t chains = 2;
+  if (const char* v = getenv("LGX_BATCH_CHAINS")) chains = (uint32_t)std::max(1, atoi(v));
+  if (e == cudaSuccess) e = build_chains(b, chains);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   // The batched inlet kernel writes lattice i's draws for step s of the
   // interval at item (item0[i] * len + s * h * iw ...); lay the prefix out
@@ -436,7 +506,7 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
     if (rc) return rc;
     LGX_CUDA(cudaGraphLaunch(ex, b->stream));
     b->graph_launches += 1;
-    const uint64_t per_step = b->nstep ? 1 : 0;
+    const uint64_t per_step = b->groups.size();
     b->launches += len * (per_step + (b->hook ? 1 : 0)) + 1 +
                    (sample && b->field_blocks ? 1 : 0) + (b->items_per_step ? 1 : 0) +
                    b->classes.size();

@@ -44,6 +44,7 @@ namespace {
 
 constexpr int kRing = 4;
 constexpr size_t kMaxSamplePoints = 16;  // batched coarse-grainings per tick
+constexpr size_t kChains = 2;            // parallel launch chains per tick
 
 double now_s() {
   using namespace std::chrono;
@@ -93,6 +94,8 @@ size_t device_bytes(const lgx::Dims& dm, uint32_t nb) {
 struct lgx_server {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;           // the second launch chain of a tick
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaMemPool_t pool = nullptr;
   size_t budget = 0, in_use = 0;
   size_t max_active = 0;
@@ -284,87 +287,139 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     }
     pts.push_back((uint32_t)k);
   }
-  // slot layout for this tick: descs[n] | block0[n+1] | item0[n+1] | blk[m][n+1]
+  // chains: contiguous runs of the active lattices balanced by blocks, run as
+  // parallel launch chains on the server's two streams
   const size_t m = pts.size();
-  lgx::LatDesc* descs = (lgx::LatDesc*)slot.host;
-  uint32_t* block0 = (uint32_t*)(descs + n);
-  uint32_t* item0 = block0 + n + 1;
-  uint32_t* blk = item0 + n + 1;
-  const size_t bytes = n * sizeof(lgx::LatDesc) + (2 + m) * (n + 1) * sizeof(uint32_t);
-  block0[0] = item0[0] = 0;
-  for (size_t j = 0; j < m; ++j) blk[j * (n + 1)] = 0;
-  uint32_t rest_blocks = 0;
+  std::vector<uint32_t> words_blocks(n);
+  uint64_t total_blocks = 0;
   for (size_t i = 0; i < n; ++i) {
-    Req* r = s->active[i];
-    lgx::LatDesc& d = descs[i];
-    d.planes[0] = r->planes[r->cur];
-    d.planes[1] = r->planes[r->cur ^ 1];
-    d.solid = r->solid;
-    d.anysolid = r->anysolid;
-    d.inlet = r->inlet;
-    d.dm = r->dm;
-    d.seed = r->spec.seed;
-    d.steps0 = r->steps_done;
-    d.cur0 = 0;
-    d.rest = r->spec.rest_particles ? 1u : 0u;
-    memcpy(d.thresh, r->thresh, sizeof(d.thresh));
-    d.field = r->field;
-    d.sums = r->sums;
-    d.bx = (uint32_t)r->spec.bx;
-    d.by = (uint32_t)r->spec.by;
-    d.bw = r->bw;
-    d.bh = r->bh;
-    d.alpha = r->spec.alpha;
-    block0[i + 1] = block0[i] + (r->dm.total + 255) / 256;
-    if (r->spec.rest_particles) rest_blocks = block0[i + 1];
-    item0[i + 1] = item0[i] + (uint32_t)len * r->dm.h * r->dm.iw;
-    for (size_t j = 0; j < m; ++j) blk[j * (n + 1) + i + 1] = blk[j * (n + 1) + i];
-    due_points(r, len, [&](uint64_t k) {
-      const size_t j = std::lower_bound(pts.begin(), pts.end(), (uint32_t)k) - pts.begin();
-      blk[j * (n + 1) + i + 1] = blk[j * (n + 1) + i] + r->bw * r->bh;
-    });
+    words_blocks[i] = (s->active[i]->dm.total + 255) / 256;
+    total_blocks += words_blocks[i];
+  }
+  const size_t nch = std::min<size_t>(kChains, n);
+  std::vector<size_t> cfirst(nch + 1, n);
+  {
+    size_t i = 0;
+    uint64_t acc = 0;
+    for (size_t c = 0; c < nch; ++c) {
+      cfirst[c] = i;
+      const uint64_t target = total_blocks * (c + 1) / nch;
+      // at least one lattice per chain: leave one for each chain after this one
+      const size_t stop = n - (nch - 1 - c);
+      while (i < stop && (c + 1 == nch || acc < target || i == cfirst[c])) acc += words_blocks[i++];
+    }
+    cfirst[nch] = n;
+  }
+  // slot layout: descs[n] | item0[n+1] | per chain c: block0[nc+1] | blk[m][nc+1]
+  lgx::LatDesc* descs = (lgx::LatDesc*)slot.host;
+  uint32_t* item0 = (uint32_t*)(descs + n);
+  std::vector<size_t> off(nch);  // each chain's block0, in words from item0
+  size_t words = n + 1;
+  for (size_t c = 0; c < nch; ++c) {
+    off[c] = words;
+    words += (1 + m) * (cfirst[c + 1] - cfirst[c] + 1);
+  }
+  const size_t bytes = n * sizeof(lgx::LatDesc) + words * sizeof(uint32_t);
+  item0[0] = 0;
+  std::vector<uint32_t> nblocks(nch, 0), rest_blocks(nch, 0);
+  for (size_t c = 0; c < nch; ++c) {
+    const size_t nc = cfirst[c + 1] - cfirst[c];
+    uint32_t* block0 = item0 + off[c];
+    uint32_t* blk = block0 + nc + 1;
+    block0[0] = 0;
+    for (size_t j = 0; j < m; ++j) blk[j * (nc + 1)] = 0;
+    for (size_t q = 0; q < nc; ++q) {
+      const size_t i = cfirst[c] + q;
+      Req* r = s->active[i];
+      lgx::LatDesc& d = descs[i];
+      d.planes[0] = r->planes[r->cur];
+      d.planes[1] = r->planes[r->cur ^ 1];
+      d.solid = r->solid;
+      d.anysolid = r->anysolid;
+      d.inlet = r->inlet;
+      d.dm = r->dm;
+      d.seed = r->spec.seed;
+      d.steps0 = r->steps_done;
+      d.cur0 = 0;
+      d.rest = r->spec.rest_particles ? 1u : 0u;
+      memcpy(d.thresh, r->thresh, sizeof(d.thresh));
+      d.field = r->field;
+      d.sums = r->sums;
+      d.bx = (uint32_t)r->spec.bx;
+      d.by = (uint32_t)r->spec.by;
+      d.bw = r->bw;
+      d.bh = r->bh;
+      d.alpha = r->spec.alpha;
+      block0[q + 1] = block0[q] + words_blocks[i];
+      if (r->spec.rest_particles) rest_blocks[c] = block0[q + 1];
+      item0[i + 1] = item0[i] + (uint32_t)len * r->dm.h * r->dm.iw;
+      for (size_t j = 0; j < m; ++j) blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q];
+      due_points(r, len, [&](uint64_t k) {
+        const size_t j = std::lower_bound(pts.begin(), pts.end(), (uint32_t)k) - pts.begin();
+        blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q] + r->bw * r->bh;
+      });
+    }
+    nblocks[c] = block0[nc];
   }
   uint8_t* dev = (uint8_t*)slot.dev;
   lgx::LatDesc* d_descs = (lgx::LatDesc*)dev;
-  uint32_t* d_block0 = (uint32_t*)(d_descs + n);
-  uint32_t* d_item0 = d_block0 + n + 1;
-  uint32_t* d_blk = d_item0 + n + 1;
+  uint32_t* d_item0 = (uint32_t*)(d_descs + n);
   cudaError_t e = cudaEventRecord(slot.ev0, s->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(slot.dev, slot.host, bytes, cudaMemcpyHostToDevice, s->stream);
-  if (e == cudaSuccess && block0[n] > slot.owner_cap) {  // grow the block-owner table
+  if (e == cudaSuccess && total_blocks > slot.owner_cap) {  // grow the block-owner table
     if (slot.owner) e = cudaFreeAsync(slot.owner, s->stream);
     slot.owner = nullptr;
     slot.owner_cap = 0;
-    const size_t cap = std::max<size_t>(block0[n], 2 * (size_t)block0[n]);
+    const size_t cap = 2 * (size_t)total_blocks;
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&slot.owner, cap * 4, s->stream);
     if (e == cudaSuccess) slot.owner_cap = cap;
   }
-  if (e == cudaSuccess) {
-    e = lgx::launch_batch_owner(d_block0, (uint32_t)n, block0[n], slot.owner, s->stream);
+  std::vector<uint32_t*> owner(nch);
+  for (size_t c = 0, o = 0; c < nch && e == cudaSuccess; o += nblocks[c], ++c) {
+    owner[c] = slot.owner + o;
+    e = lgx::launch_batch_owner(d_item0 + off[c], (uint32_t)(cfirst[c + 1] - cfirst[c]),
+                                nblocks[c], owner[c], s->stream);
     s->launches += 1;
   }
-  const uint32_t nl = (uint32_t)n;
   if (e == cudaSuccess && item0[n]) {
-    lgx::BatchInletArgs ia{d_descs, d_item0, nl, item0[n], s->d_zero};
+    lgx::BatchInletArgs ia{d_descs, d_item0, (uint32_t)n, item0[n], s->d_zero};
     e = lgx::launch_batch_inlet(ia, s->stream);
     s->launches += 1;
   }
-  const int rule = rest_blocks == block0[n] ? lgx::kRuleRest
-                   : rest_blocks == 0     ? lgx::kRuleNoRest
-                                          : lgx::kRuleMixed;
-  size_t j = 0;
-  for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
-    lgx::BatchStepArgs sa{d_descs, d_block0, slot.owner, nl, s->d_zero, k, 0};
-    e = lgx::launch_batch_step(sa, block0[n], rule, s->stream);
-    s->launches += 1;
-    if (e == cudaSuccess && j < m && pts[j] == k + 1) {
-      const uint32_t* tb = blk + j * (n + 1);
-      lgx::BatchSampleArgs sp{d_descs, d_blk + j * (n + 1), nl, tb[n], s->d_zero, k + 1};
-      e = lgx::launch_batch_sample(sp, s->stream);
+  if (e == cudaSuccess && nch > 1) {
+    e = cudaEventRecord(s->fork, s->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream2, s->fork, 0);
+  }
+  for (size_t c = 0; c < nch && e == cudaSuccess; ++c) {
+    cudaStream_t st = c == 0 ? s->stream : s->stream2;
+    const size_t nc = cfirst[c + 1] - cfirst[c];
+    const lgx::LatDesc* dd = d_descs + cfirst[c];
+    const uint32_t* d_block0 = d_item0 + off[c];
+    const uint32_t* blk = item0 + off[c] + nc + 1;
+    const int rule = rest_blocks[c] == nblocks[c] ? lgx::kRuleRest
+                     : rest_blocks[c] == 0       ? lgx::kRuleNoRest
+                                                 : lgx::kRuleMixed;
+    size_t j = 0;
+    for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
+      lgx::BatchStepArgs sa{dd, d_block0, owner[c], (uint32_t)nc, s->d_zero, k, 0};
+      e = lgx::launch_batch_step(sa, nblocks[c], rule, st);
       s->launches += 1;
-      ++j;
+      if (e == cudaSuccess && j < m && pts[j] == k + 1) {
+        const uint32_t* tb = blk + j * (nc + 1);
+        if (tb[nc]) {
+          lgx::BatchSampleArgs sp{dd, d_block0 + nc + 1 + j * (nc + 1), (uint32_t)nc, tb[nc],
+                                  s->d_zero, k + 1};
+          e = lgx::launch_batch_sample(sp, st);
+          s->launches += 1;
+        }
+        ++j;
+      }
     }
+  }
+  if (e == cudaSuccess && nch > 1) {
+    e = cudaEventRecord(s->join, s->stream2);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->join, 0);
   }
   if (e == cudaSuccess) e = cudaEventRecord(slot.ev, s->stream);
   if (e != cudaSuccess) return e;
@@ -534,6 +589,9 @@ int lgx_server_create(size_t budget_bytes, size_t max_active, lgx_server** out) 
   s->budget = budget_bytes;
   s->max_active = max_active;
   cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
   if (e == cudaSuccess) {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
@@ -546,7 +604,8 @@ int lgx_server_create(size_t budget_bytes, size_t max_active, lgx_server** out) 
     e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   s->slot_bytes = max_active * sizeof(lgx::LatDesc) +
-                  (2 + kMaxSamplePoints) * (max_active + 1) * sizeof(uint32_t);
+                  ((max_active + 1) + (1 + kMaxSamplePoints) * (max_active + kChains)) *
+                      sizeof(uint32_t);
   for (int i = 0; i < kRing && e == cudaSuccess; ++i) {
     e = cudaHostAlloc(&s->ring[i].host, s->slot_bytes, cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaMalloc(&s->ring[i].dev, s->slot_bytes);
@@ -587,6 +646,9 @@ int lgx_server_destroy(lgx_server* s) {
   }
   cudaFree(s->d_zero);
   if (s->pool) cudaMemPoolDestroy(s->pool);
+  if (s->fork) cudaEventDestroy(s->fork);
+  if (s->join) cudaEventDestroy(s->join);
+  if (s->stream2) cudaStreamDestroy(s->stream2);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return LGX_OK;
