@@ -23,6 +23,9 @@ namespace lgx {
 namespace {
 
 constexpr int kThreads = 256;
+#ifndef LGX_BATCH_MINB
+#define LGX_BATCH_MINB 4  // resident blocks per SM the register allocation must allow
+#endif
 
 template <bool REST>
 __device__ __forceinline__ void batch_word(const LatDesc& d, uint64_t local, uint32_t k,
@@ -49,7 +52,7 @@ __device__ __forceinline__ uint32_t owner_of(const uint32_t* prefix, uint32_t n,
 }
 
 template <bool REST>
-__global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepArgs p) {
+__global__ void __launch_bounds__(kThreads, LGX_BATCH_MINB) lgx_batch_step_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
@@ -66,7 +69,7 @@ __global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_kernel(BatchStepAr
 // Both rules in one launch: a block belongs to one lattice, so the rule is
 // uniform across it.  Used when a batch mixes rest-particle and six-direction
 // lattices, to keep one launch per step.
-__global__ void __launch_bounds__(kThreads, 4) lgx_batch_step_mixed_kernel(BatchStepArgs p) {
+__global__ void __launch_bounds__(kThreads, LGX_BATCH_MINB) lgx_batch_step_mixed_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];

@@ -5,7 +5,8 @@
 
 Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
-`sweep` (the 64-lattice transport sweep as one batch).  --mode picks the step
+`sweep` (the 64-lattice transport sweep as one batch), `transport` (one
+transport::measure at --size, density 0.22).  --mode picks the step
 launch mode (1 one launch per step, 2 persistent waves, 3 temporal blocking).
 """
 import argparse
@@ -20,11 +21,17 @@ from lattice_gas import workloads as W  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="wake", choices=["wake", "big", "sweep"])
+    ap.add_argument("--case", default="wake", choices=["wake", "big", "sweep", "transport"])
+    ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--mode", type=int, default=1)
     ap.add_argument("--depth", type=int, default=4)
     a = ap.parse_args()
+    if a.case == "transport":
+        r = LG.transport_measure([0.22], rest=True, seed=0x5EED, size=a.size)[0]
+        print("transport %d: nu %.4f g %.4f windows %d %d" % (a.size, r.nu, r.g, r.window_nu,
+                                                             r.window_g))
+        return
     if a.case == "sweep":
         wls = W.transport_sweep(steps=a.steps)
         lats = []
