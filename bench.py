@@ -293,6 +293,10 @@ def bench_roofline_case(LG, W, steps: int):
                      "value": round(wl.sites / (ms * 1e-3) / 1e9, 1),
                      "algorithmic_GBps": round(wl.sites * ALGO_BYTES_PER_SITE / (ms * 1e-3) / 1e9, 1)}
         g.close()
+    probe = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+    out["step_plan"] = {k: (round(v, 3) if isinstance(v, float) else v)
+                        for k, v in probe.step_plan.items()}
+    probe.close()
     out["single"]["dram_GBps_from_ncu"] = round(
         wl.sites * BIG_DRAM_BYTES_PER_SITE / (out["single"]["ms_per_step"] * 1e-3) / 1e9, 1)
     out["bit_exact_temporal_vs_single"] = bool(
@@ -530,6 +534,8 @@ def run_gb300(args, world, rank, local):
                                   "peak_kind": "measured (lgx_probe_int_rate, lop3)"}},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": wl.sites,
                 "d2h_bytes_per_step": 8 * nb * 4},
+        "step_plan": {k: (round(v, 3) if isinstance(v, float) else v)
+                      for k, v in g.step_plan.items()},
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cpu,

@@ -81,19 +81,31 @@ int lgx_advance(lgx_lattice *lat, uint64_t n);
  * lattice into the attached field every sample_every steps and after the last
  * one; sample_every == 0 never samples. */
 int lgx_advance_sampling(lgx_lattice *lat, uint64_t n, uint64_t sample_every, float alpha);
-/* How steps are launched.  AUTO (default) and SINGLE launch one kernel per
- * step, as the reference dispatches one lgca_step per step, with programmatic
- * dependent launch so each step's state-independent draws overlap the
- * previous step's tail.  WAVE runs up to 128 steps per cooperative launch of a
- * persistent kernel (each block owns a fixed range of words and waits, with a
- * bounded spin, only for the blocks owning the rows next to its own).
- * Results are identical in every mode. */
+/* How steps are launched.  SINGLE launches one kernel per step, as the
+ * reference dispatches one lgca_step per step, with programmatic dependent
+ * launch so each step's state-independent draws overlap the previous step's
+ * tail.  WAVE runs up to 128 steps per cooperative launch of a persistent
+ * kernel (each block owns a fixed range of words and waits, with a bounded
+ * spin, only for the blocks owning the rows next to its own).  TEMPORAL: see
+ * lgx_set_temporal_depth.  AUTO (default) uses whichever of SINGLE, WAVE and
+ * TEMPORAL with depth 4 or 8 a tuner measured fastest for the lattice's size
+ * class (timed on a scratch lattice of the same shape at its first advance,
+ * cached for the process; lgx_get_step_plan).  Results are identical in every
+ * mode. */
 enum { LGX_STEP_AUTO = 0, LGX_STEP_SINGLE = 1, LGX_STEP_WAVE = 2, LGX_STEP_TEMPORAL = 3 };
 int lgx_set_step_mode(lgx_lattice *lat, int mode);
 /* TEMPORAL: runs of k steps (k = 4 or 8, lgx_set_temporal_depth) in one pass
  * over HBM, the intermediate steps kept in registers (lattices at least 64
  * words wide; other runs, and steps up to a sampling point, go one at a time). */
 int lgx_set_temporal_depth(lgx_lattice *lat, int k);
+/* What AUTO resolves to for this lattice, and the tuner's times per step (0 where a
+ * mode does not apply); tunes the size class now if it has not been. */
+typedef struct lgx_step_plan {
+  int mode;
+  uint32_t depth;
+  float single_us, wave_us, temporal4_us, temporal8_us;
+} lgx_step_plan;
+int lgx_get_step_plan(lgx_lattice *lat, lgx_step_plan *out);
 /* GpuLattice::sample_field (src/gpu.rs:710-721). */
 int lgx_sample_field(lgx_lattice *lat, float alpha);
 /* GpuLattice::read_field (src/gpu.rs:725-736): n_blocks must be bw*bh. */

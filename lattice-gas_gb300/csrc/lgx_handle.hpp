@@ -45,6 +45,10 @@ struct lgx_lattice {
   // persistent multi-step kernel
   int step_mode = LGX_STEP_AUTO;
   uint32_t temporal_depth = 4;  // steps per pass in LGX_STEP_TEMPORAL
+  bool auto_resolved = false;   // LGX_STEP_AUTO: the tuner's choice below is set
+  int auto_mode = LGX_STEP_SINGLE;
+  uint32_t auto_depth = 0;
+  float auto_us[4] = {0, 0, 0, 0};  // single, wave, temporal 4, temporal 8 (us per step)
   uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
   uint32_t* done = nullptr;  // [wave_grid] published step per CTA
   uint32_t* error = nullptr; // timeout flag

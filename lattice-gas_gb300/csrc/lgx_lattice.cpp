@@ -16,6 +16,7 @@
 #include "../../include/lgx.h"
 #include "lgx_handle.hpp"
 #include "lgx_profile.hpp"
+#include "lgx_tune.hpp"
 #include "lgx_internal.hpp"
 
 namespace lgx {
@@ -199,7 +200,13 @@ int enqueue_temporal(lgx_lattice* lat, uint32_t k) {
   ta.dm = lat->dm;
   ta.seed = lat->seed;
   ta.steps = lat->steps;
-  lgx::temporal_tiling(lat->dm, 128, &ta);
+  // bands of up to 128 rows, shorter when the lattice would give fewer than
+  // about 16 warps per SM (152 SMs), but at least 4k rows (each band also
+  // computes k rows of halo above and below)
+  const uint32_t strips = (lat->dm.wpr + 28) / 29;
+  const uint32_t fill = (uint32_t)(((uint64_t)lat->dm.h * strips) / (152u * 16u));
+  const uint32_t band = std::max<uint32_t>(4u * k, std::min<uint32_t>(128u, fill));
+  lgx::temporal_tiling(lat->dm, band, &ta);
   LGX_CUDA(lgx::launch_temporal(ta, lat->rest, k, lat->stream));
   lat->launches += 1;
   lat->cur ^= 1;
@@ -229,12 +236,34 @@ int enqueue_single(lgx_lattice* lat) {
 // Enqueue n steps, sampling every `every` steps and after the last
 // (src/gpu.rs:668-706).  In the persistent mode one launch runs up to the
 // next sampling point, the end of the inlet chunk in hand, or kInletChunk.
+// LGX_STEP_AUTO: the step-mode tuner's choice for this lattice's size class.
+int resolve_auto(lgx_lattice* lat) {
+  if (lat->auto_resolved) return LGX_OK;
+  lgx::StepPlan p;
+  const int rc = lgx::plan_step_mode(lat->device, lat->dm.w, lat->dm.h, lat->rest, &p);
+  if (rc) return rc;
+  lat->auto_mode = p.mode;
+  lat->auto_depth = p.depth;
+  lat->auto_us[0] = p.single_us;
+  lat->auto_us[1] = p.wave_us;
+  lat->auto_us[2] = p.temporal4_us;
+  lat->auto_us[3] = p.temporal8_us;
+  lat->auto_resolved = true;
+  return LGX_OK;
+}
+
 int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
   uint64_t left = n, since = 0;
-  const bool wave = lat->step_mode == LGX_STEP_WAVE;
-  const uint32_t tk = lat->temporal_depth;
-  const bool temporal =
-      lat->step_mode == LGX_STEP_TEMPORAL && lgx::temporal_supported(lat->dm, tk);
+  int mode = lat->step_mode;
+  uint32_t tk = lat->temporal_depth;
+  if (mode == LGX_STEP_AUTO && n > 0) {
+    const int rc = resolve_auto(lat);
+    if (rc) return rc;
+    mode = lat->auto_mode;
+    if (mode == LGX_STEP_TEMPORAL) tk = lat->auto_depth;
+  }
+  const bool wave = mode == LGX_STEP_WAVE;
+  const bool temporal = mode == LGX_STEP_TEMPORAL && lgx::temporal_supported(lat->dm, tk);
   while (left > 0) {
     int rc = ensure_inlet(lat, left);
     if (rc) return rc;
@@ -509,6 +538,24 @@ int lgx_set_step_mode(lgx_lattice* lat, int mode) {
     return LGX_ERR_ARG;
   }
   lat->step_mode = mode;
+  return LGX_OK;
+}
+
+int lgx_get_step_plan(lgx_lattice* lat, lgx_step_plan* out) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!out) {
+    lgx::set_error("lgx_get_step_plan: null output");
+    return LGX_ERR_ARG;
+  }
+  rc = resolve_auto(lat);
+  if (rc) return rc;
+  out->mode = lat->auto_mode;
+  out->depth = lat->auto_depth;
+  out->single_us = lat->auto_us[0];
+  out->wave_us = lat->auto_us[1];
+  out->temporal4_us = lat->auto_us[2];
+  out->temporal8_us = lat->auto_us[3];
   return LGX_OK;
 }
 

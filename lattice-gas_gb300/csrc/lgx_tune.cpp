@@ -22,6 +22,7 @@
 #include <tuple>
 #include <vector>
 
+#include "../../include/lgx.h"
 #include "lgx_batch.hpp"
 #include "lgx_tune.hpp"
 
@@ -33,6 +34,7 @@ constexpr size_t kTuneMaxWords = 4u << 20;  // per-plane words of all synthetic 
 
 std::mutex g_mu;
 std::map<std::tuple<int, uint32_t, uint32_t, bool>, ClassPlan> g_plans;
+std::map<std::tuple<int, uint32_t, bool, bool>, StepPlan> g_step_plans;
 
 struct Scratch {
   std::vector<void*> ptrs;
@@ -157,7 +159,75 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   return cudaSuccess;
 }
 
+// Microseconds per step of `mode` on the scratch lattice, over about 1.5 ms of
+// steps (a multiple of 8, at least 8).  <0: the mode failed to run here.
+float time_mode(lgx_lattice* t, int mode, uint32_t depth, float est_us) {
+  if (lgx_set_step_mode(t, mode) || (depth && lgx_set_temporal_depth(t, (int)depth))) return -1;
+  uint64_t k = est_us > 0 ? (uint64_t)(1500.0f / est_us) : 8;
+  k = std::min<uint64_t>(std::max<uint64_t>(k, 8), 512);
+  k = (k + 7) / 8 * 8;
+  float ms = 0;
+  if (lgx_advance(t, 8) || lgx_timing_mark(t, 0) || lgx_advance(t, k) || lgx_timing_mark(t, 1) ||
+      lgx_timing_elapsed(t, 0, 1, &ms)) {
+    cudaGetLastError();
+    return -1;
+  }
+  return ms * 1e3f / (float)k;
+}
+
 }  // namespace
+
+int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out) {
+  const Dims dm = make_dims(w, h, 0);
+  const bool wide = temporal_supported(dm, 4);
+  const auto key = std::make_tuple(device, class_bucket(dm.total), wide, rest);
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    auto it = g_step_plans.find(key);
+    if (it != g_step_plans.end()) {
+      *out = it->second;
+      return LGX_OK;
+    }
+  }
+  lgx_lattice* t = nullptr;
+  int rc = lgx_create(w, h, rest ? 1 : 0, 0x7E57ull, &t);
+  if (rc) return rc;
+  StepPlan p{LGX_STEP_SINGLE, 0, 0, 0, 0, 0};
+  const float est = time_mode(t, LGX_STEP_SINGLE, 0, 0);
+  p.single_us = time_mode(t, LGX_STEP_SINGLE, 0, est);
+  const float w_us = time_mode(t, LGX_STEP_WAVE, 0, p.single_us);
+  p.wave_us = w_us > 0 ? w_us : 0;
+  if (wide) {
+    const float t4 = time_mode(t, LGX_STEP_TEMPORAL, 4, p.single_us);
+    const float t8 = time_mode(t, LGX_STEP_TEMPORAL, 8, p.single_us);
+    p.temporal4_us = t4 > 0 ? t4 : 0;
+    p.temporal8_us = t8 > 0 ? t8 : 0;
+  }
+  lgx_destroy(t);
+  if (p.single_us <= 0) {
+    set_error("step-mode tuner: the one-launch-per-step run failed");
+    return LGX_ERR_CUDA;
+  }
+  float best = p.single_us;
+  if (p.wave_us > 0 && p.wave_us < best) {
+    best = p.wave_us;
+    p.mode = LGX_STEP_WAVE;
+  }
+  if (p.temporal4_us > 0 && p.temporal4_us < best) {
+    best = p.temporal4_us;
+    p.mode = LGX_STEP_TEMPORAL;
+    p.depth = 4;
+  }
+  if (p.temporal8_us > 0 && p.temporal8_us < best) {
+    best = p.temporal8_us;
+    p.mode = LGX_STEP_TEMPORAL;
+    p.depth = 8;
+  }
+  std::lock_guard<std::mutex> g(g_mu);
+  g_step_plans[key] = p;
+  *out = p;
+  return LGX_OK;
+}
 
 uint32_t class_bucket(uint32_t words) {
   uint32_t b = 64;

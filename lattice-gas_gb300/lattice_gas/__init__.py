@@ -83,6 +83,16 @@ class BatchClass(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class StepPlan(C.Structure):
+    """lgx_step_plan: what LGX_STEP_AUTO resolves to and the tuner's times per step."""
+    _fields_ = [("mode", C.c_int), ("depth", C.c_uint32), ("single_us", C.c_float),
+                ("wave_us", C.c_float), ("temporal4_us", C.c_float),
+                ("temporal8_us", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class LgxError(RuntimeError):
     """A C-ABI call returned a non-zero lgx_status."""
 
@@ -122,6 +132,7 @@ def lib():
         _sig(L, "lgx_sample_field", vp, C.c_float)
         _sig(L, "lgx_set_step_mode", vp, C.c_int)
         _sig(L, "lgx_set_temporal_depth", vp, C.c_int)
+        _sig(L, "lgx_get_step_plan", vp, C.POINTER(StepPlan))
         _sig(L, "lgx_read_field", vp, f32p, f32p, f32p, f32p, sz)
         _sig(L, "lgx_read_block_sums", vp, i32p, i32p, i32p, i32p, sz)
         _sig(L, "lgx_total_particles", vp, C.POINTER(C.c_uint64))
@@ -265,6 +276,13 @@ class GpuLattice:
             out = np.zeros(self.w * self.h, np.uint8)
         _check(lib().lgx_store(self._h, _p(out, C.c_uint8), out.size))
         return out
+
+    @property
+    def step_plan(self) -> dict:
+        """What the default step mode resolves to for this lattice's size class."""
+        p = StepPlan()
+        _check(lib().lgx_get_step_plan(self._h, C.byref(p)))
+        return p.as_dict()
 
     def row_ux(self) -> np.ndarray:
         """transport::row_ux (src/transport.rs:87-91), reduced on the device."""

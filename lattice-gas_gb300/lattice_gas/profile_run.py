@@ -6,7 +6,10 @@
 Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
 `sweep` (the 64-lattice transport sweep as one batch), `transport` (one
-transport::measure at --size, density 0.22).  --mode picks the step
+transport::measure at --size, density 0.22).  --policy picks the sweep's batch
+policy (under a profiler pass 1: the tuner's timings are not meaningful there, and
+without one it picks one launch per step for every class of this sweep).  --mode
+picks the step
 launch mode (1 one launch per step, 2 persistent waves, 3 temporal blocking).
 """
 import argparse
@@ -23,6 +26,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="wake", choices=["wake", "big", "sweep", "transport"])
     ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--policy", type=int, default=0,
+                    help="batch policy for the sweep: 0 tuned, 1 one launch per step, 2 resident")
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--mode", type=int, default=1)
     ap.add_argument("--depth", type=int, default=4)
@@ -40,7 +45,7 @@ def main():
             g.attach_field(wl.block, wl.block)
             g.load(wl.cells)
             lats.append(g)
-        b = LG.Batch(lats)
+        b = LG.Batch(lats, a.policy)
         b.advance_sampling(a.steps, 50, 1.0)
         print("sweep: %d lattices, %d steps" % (len(lats), a.steps))
         return
