@@ -101,7 +101,7 @@ cudaError_t wave_grid(bool rest, uint32_t total, uint32_t* grid);
 cudaError_t launch_wave(const WaveArgs& w, bool rest, uint32_t grid, cudaStream_t st);
 // Temporal blocking: supported depths and widths, the tiling, the launch.
 bool temporal_supported(const Dims& dm, uint32_t k);
-void temporal_tiling(const Dims& dm, uint32_t band_rows, TemporalArgs* t);
+void temporal_tiling(const Dims& dm, uint32_t k, TemporalArgs* t);  // k steps per pass
 cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaStream_t st);
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,

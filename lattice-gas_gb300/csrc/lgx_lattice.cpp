@@ -200,13 +200,7 @@ int enqueue_temporal(lgx_lattice* lat, uint32_t k) {
   ta.dm = lat->dm;
   ta.seed = lat->seed;
   ta.steps = lat->steps;
-  // bands of up to 128 rows, shorter when the lattice would give fewer than
-  // about 16 warps per SM (152 SMs), but at least 4k rows (each band also
-  // computes k rows of halo above and below)
-  const uint32_t strips = (lat->dm.wpr + 28) / 29;
-  const uint32_t fill = (uint32_t)(((uint64_t)lat->dm.h * strips) / (152u * 16u));
-  const uint32_t band = std::max<uint32_t>(4u * k, std::min<uint32_t>(128u, fill));
-  lgx::temporal_tiling(lat->dm, band, &ta);
+  lgx::temporal_tiling(lat->dm, k, &ta);
   LGX_CUDA(lgx::launch_temporal(ta, lat->rest, k, lat->stream));
   lat->launches += 1;
   lat->cur ^= 1;

@@ -187,10 +187,14 @@ cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaSt
   return cudaGetLastError();
 }
 
-void temporal_tiling(const Dims& dm, uint32_t band_rows, TemporalArgs* t) {
+// Bands of up to 128 rows, shorter when the lattice would give fewer than
+// about 16 warps per SM (152 SMs), but at least 4k rows: each band also
+// computes k rows of halo above and below.
+void temporal_tiling(const Dims& dm, uint32_t k, TemporalArgs* t) {
   t->nstrips = (dm.wpr + kStrip - 1) / kStrip;
-  t->band_rows = band_rows;
-  t->nbands = (dm.h + band_rows - 1) / band_rows;
+  const uint32_t fill = (uint32_t)(((uint64_t)dm.h * t->nstrips) / (152u * 16u));
+  t->band_rows = std::max<uint32_t>(4u * k, std::min<uint32_t>(128u, fill));
+  t->nbands = (dm.h + t->band_rows - 1) / t->band_rows;
 }
 
 }  // namespace lgx
