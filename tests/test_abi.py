@@ -81,3 +81,39 @@ def test_no_device_is_a_loud_error(engine_lib):
     with pytest.raises(LG.LgxError) as e:
         LG.GpuLattice(64, 64, True, 1)
     assert e.value.code == 3
+
+
+def test_new_entry_points_refuse_bad_arguments(engine_lib):
+    """Argument checks come before any device work, so they hold without a GPU."""
+    LG = engine_lib
+    L = LG.lib()
+    ARG = 1
+    d = np.array([0.22], np.float32)
+    out = (LG.Transport * 1)()
+    dp = d.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lgx_transport_measure(dp, 1, 1, 5, 7, out) == ARG      # odd size
+    assert L.lgx_transport_measure(dp, 1, 1, 5, 4, out) == ARG      # too small
+    assert L.lgx_transport_measure(dp, 0, 1, 5, 64, out) == ARG     # no densities
+    assert L.lgx_transport_measure(None, 1, 1, 5, 64, out) == ARG
+    assert L.lgx_transport_measure(dp, 9000, 1, 5, 64, out) == ARG  # too many for one batch
+    h = C.c_void_p()
+    arr = (C.c_void_p * 1)(None)
+    assert L.lgx_batch_create_ex(arr, 1, 9, C.byref(h)) == ARG      # unknown policy
+    assert L.lgx_batch_create_ex(arr, 0, 0, C.byref(h)) == ARG      # no lattices
+    assert L.lgx_batch_create_ex(arr, 1, 0, C.byref(h)) == ARG      # null lattice
+    n = C.c_size_t()
+    assert L.lgx_batch_plan(None, None, 0, C.byref(n)) == ARG
+    assert L.lgx_get_step_plan(None, None) == ARG
+    u = np.zeros(8, np.float32)
+    assert L.lgx_row_ux(None, u.ctypes.data_as(C.POINTER(C.c_float)), 8) == ARG
+    assert L.lgx_column_uy(None, u.ctypes.data_as(C.POINTER(C.c_float)), 8) == ARG
+    assert L.lgx_line_sums(None, None, 0, None, 0) == ARG
+    assert L.lgx_init_equilibrium(None, 0.3, 0.0, 0.0, 1) == ARG
+    assert L.lgx_byte_init_equilibrium(None) == ARG
+
+
+@pytest.mark.skipif(_gpu_present(), reason="checks the no-device path")
+def test_transport_without_a_device_is_an_error(engine_lib):
+    LG = engine_lib
+    with pytest.raises(LG.LgxError):
+        LG.transport_measure([0.22], size=64)
