@@ -71,8 +71,15 @@ struct ResidentArgs {
   uint32_t len;
 };
 bool resident_config_valid(uint32_t csize, uint32_t threads);
+// Shared memory one CTA of a csize-CTA cluster holds for a lattice (both
+// buffers of its band), and whether the lattice can run resident that way.
+constexpr size_t kResidentMaxSmem = 200u * 1024u;
+size_t resident_smem_bytes(const Dims& dm, uint32_t csize);
+bool resident_fits(const Dims& dm, uint32_t csize);
+// smem: dynamic shared memory per CTA, at least resident_smem_bytes of every
+// lattice of the launch.
 cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
-                            uint32_t threads, cudaStream_t st);
+                            uint32_t threads, size_t smem, cudaStream_t st);
 
 // The rule of the blocks a batched step launch covers.
 constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;

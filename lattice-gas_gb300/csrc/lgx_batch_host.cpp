@@ -51,6 +51,7 @@ struct StepGroup {
 struct ResClass {
   uint32_t first, count;
   lgx::ClassPlan plan;
+  size_t smem;  // shared memory per CTA: the largest member's band
 };
 
 int cuda_fail(cudaError_t e, const char* what) {
@@ -241,7 +242,7 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
   for (const ResClass& c : b->classes) {
     if (e != cudaSuccess) break;
     lgx::ResidentArgs ra{b->d_descs, sched, c.first, b->d_base, len};
-    e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, rs);
+    e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, c.smem, rs);
   }
   for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; ++g) {
     const StepGroup& sg = b->groups[g];
@@ -394,6 +395,8 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
     e = lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, &keys[k].plan);
     const lgx::ClassPlan& p = keys[k].plan;
     res_class[k] = policy == LGX_BATCH_RESIDENT ? p.csize != 0 : p.resident;
+    for (size_t i = 0; i < n && res_class[k]; ++i)  // every member's band must fit
+      if (cls[i] == (int)k && !lgx::resident_fits(lats[i]->dm, p.csize)) res_class[k] = false;
     lgx_batch_class c{};
     c.words = keys[k].words;
     c.lattices = keys[k].count;
@@ -414,9 +417,12 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
   b->nstep = (uint32_t)b->lats.size();
   for (size_t k = 0; k < keys.size(); ++k) {
     if (!res_class[k]) continue;
-    ResClass rc{(uint32_t)b->lats.size(), 0, keys[k].plan};
+    ResClass rc{(uint32_t)b->lats.size(), 0, keys[k].plan, 0};
     for (size_t i = 0; i < n; ++i)
-      if (cls[i] == (int)k) b->lats.push_back(lats[i]);
+      if (cls[i] == (int)k) {
+        b->lats.push_back(lats[i]);
+        rc.smem = std::max(rc.smem, lgx::resident_smem_bytes(lats[i]->dm, rc.plan.csize));
+      }
     rc.count = (uint32_t)b->lats.size() - rc.first;
     b->classes.push_back(rc);
   }

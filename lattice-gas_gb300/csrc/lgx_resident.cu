@@ -1,17 +1,19 @@
-// lgx_resident.cu -- many steps of small lattices in one launch.
+// lgx_resident.cu -- many steps of small lattices in one launch, the state in
+// the shared memory of a thread-block cluster.
 //
 // A lattice of a few thousand words is too small to fill the GPU for one step,
 // so stepping it one launch per step costs a launch's latency per step however
-// little work the step is.  Here one thread-block cluster owns one lattice for
-// a whole interval: its CTAs split the lattice's 32-word chunks between them,
-// run the step on their chunks, meet at a cluster barrier (release / acquire at
-// cluster scope, so every CTA's stores of the step are visible to the others'
-// loads of the next; the next step's draws are made between arrive and wait),
-// and go on to the next step, all inside one launch.  The
-// planes are read through L2 (ld.global.cg), never the read-only path, since
-// they change during the launch.  Sampling points are handled by the cluster
-// itself between steps: each CTA coarse-grains a fixed share of the field
-// blocks after the steps where its lattice is due.
+// little work the step is.  Here one cluster of C CTAs owns one lattice for a
+// whole interval.  CTA r holds rows [r h / C, (r + 1) h / C) of both ping-pong
+// buffers in its shared memory ([2][7][ceil(h / C)][wpr] words); a step reads
+// its own rows there and the one row above and below its band from the
+// neighbouring CTAs' shared memory (distributed shared memory, through
+// addresses from map_shared_rank), writes its rows of the other buffer, and
+// meets the others at a cluster barrier (arrive.release / wait.acquire; the
+// next step's draws are made between arrive and wait).  The planes are read
+// from global memory once at the start and written back once at the end, and
+// at each sampling point, where the cluster coarse-grains from global memory
+// after writing its rows there.
 //
 // Clusters never wait on one another, so any number of lattices can share the
 // launch; clusters the GPU cannot hold at once run when others finish.
@@ -25,54 +27,119 @@ namespace cg = cooperative_groups;
 namespace lgx {
 namespace {
 
+__device__ __forceinline__ uint32_t band_start(uint32_t r, uint32_t h, uint32_t c) {
+  return (uint32_t)(((uint64_t)r * h) / c);
+}
+
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArgs p) {
+  extern __shared__ uint32_t shm[];
   const cg::cluster_group cluster = cg::this_cluster();
-  const uint32_t csize = cluster.num_blocks(), rank = cluster.block_rank();
-  const uint32_t li = p.first_lat + blockIdx.x / csize;
+  const uint32_t C = cluster.num_blocks(), rank = cluster.block_rank();
+  const uint32_t li = p.first_lat + blockIdx.x / C;
   const LatDesc& d = p.descs[li];
   const ResSched sch = p.sched[li];
   const Dims& dm = d.dm;
-  const uint32_t nchunks = (dm.total + 31u) >> 5;
-  const uint32_t c0 = (uint32_t)(((uint64_t)rank * nchunks) / csize);
-  const uint32_t c1 = (uint32_t)(((uint64_t)(rank + 1u) * nchunks) / csize);
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = THREADS / 32;
+  const size_t S = dm.total;
+  const uint32_t y0 = band_start(rank, dm.h, C), y1 = band_start(rank + 1u, dm.h, C);
+  const uint32_t cap = (dm.h + C - 1u) / C;      // rows of the largest band
+  const size_t lps = (size_t)cap * dm.wpr;       // local plane stride
+  const size_t lbs = 7 * lps;                    // local buffer stride
+  const uint32_t nw = (y1 - y0) * dm.wpr;        // words of this band
   const uint64_t base = p.base ? *p.base : 0ull;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = THREADS / 32;
   const uint32_t nb = d.bw * d.bh;
 
+  // this band of the state the interval starts from, into buffer 0
+  {
+    const uint32_t* g = ((d.cur0 + (uint32_t)base) & 1u) ? d.planes[1] : d.planes[0];
+    for (uint32_t i = threadIdx.x; i < nw; i += THREADS)
+#pragma unroll
+      for (int q = 0; q < 7; ++q) shm[q * lps + i] = __ldcg(g + q * S + (size_t)y0 * dm.wpr + i);
+  }
+  // Write band buffer `buf` to the global planes of parity `par`.
+  auto store_band = [&](uint32_t buf, uint32_t par) {
+    uint32_t* g = par ? d.planes[1] : d.planes[0];
+    for (uint32_t i = threadIdx.x; i < nw; i += THREADS)
+#pragma unroll
+      for (int q = 0; q < 7; ++q) g[q * S + (size_t)y0 * dm.wpr + i] = shm[buf * lbs + q * lps + i];
+  };
+  cluster.sync();  // every band is loaded before a neighbour reads it
+
+  // Word c * 32 + lane of the band; lanes past its end repeat its last word.
+  const uint32_t nch = (nw + 31u) >> 5;
+  auto word_of = [&](uint32_t c, uint32_t* lw, bool* live) {
+    *lw = c * 32u + lane;
+    *live = *lw < nw;
+    if (!*live) *lw = nw - 1u;
+  };
+  auto div_wpr = [&](uint32_t x) {  // x / wpr by the lattice's multiply-shift
+    const uint32_t t = __umulhi(x, dm.div_m);
+    return (t + ((x - t) >> dm.div_s1)) >> dm.div_s2;
+  };
+  auto global_word = [&](uint32_t lw) {
+    const uint32_t yr = div_wpr(lw);
+    return (y0 + yr) * dm.wpr + (lw - yr * dm.wpr);
+  };
+  // The rows next to the band belong to the neighbouring CTAs (every band has
+  // at least two rows): the row above the band is the last row of rank - 1's,
+  // the row below is the first of rank + 1's.
+  const uint32_t up = (rank + C - 1u) % C, down = (rank + 1u) % C;
+  const uint32_t ya = (y0 == 0u) ? dm.h - 1u : y0 - 1u;  // the row above the band
+  const uint32_t up_last = ya - band_start(up, dm.h, C);
+  uint32_t* up_base = cluster.map_shared_rank(shm, up) + (size_t)up_last * dm.wpr;
+  uint32_t* down_base = cluster.map_shared_rank(shm, down);
   // The draws of a warp's first chunk for step k are made while the cluster
   // barrier of step k - 1 is pending: they depend on (word, step) only.
-  const uint32_t cfirst = c0 + warp;
-  const uint32_t gfirst = min(cfirst * 32u + lane, dm.total - 1u);
-  Draws first = draws(gfirst ^ step_seed32(d.seed, d.steps0 + base));
+  uint32_t lw0;
+  bool live0;
+  word_of(min(warp, nch - 1u), &lw0, &live0);
+  const uint32_t g0 = global_word(lw0);
+  Draws first = draws(g0 ^ step_seed32(d.seed, d.steps0 + base));
+
   for (uint32_t k = 0; k < p.len; ++k) {
     const uint64_t local = base + k;
-    const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
-    const uint32_t* src = par ? d.planes[1] : d.planes[0];
-    uint32_t* dst = par ? d.planes[0] : d.planes[1];
+    const uint32_t sb = k & 1u, db = sb ^ 1u;
     const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
     const uint32_t* inlet = dm.iw ? d.inlet + (size_t)k * dm.h * dm.iw * 7u : nullptr;
-    for (uint32_t c = cfirst; c < c1; c += nw) {
-      uint32_t g = c * 32u + lane;
-      const bool live = g < dm.total;
-      if (!live) g = dm.total - 1u;
-      const Draws s = c == cfirst ? first : draws(g ^ seed32);
+    // plane q of row yy (in the band or next to it) of the source buffer
+    auto row = [&](uint32_t q, uint32_t yy) -> const uint32_t* {
+      const size_t off = sb * lbs + q * lps;
+      if (yy - y0 < y1 - y0) return shm + off + (size_t)(yy - y0) * dm.wpr;
+      return (yy == ya ? up_base : down_base) + off;
+    };
+    for (uint32_t c = warp; c < nch; c += nwarps) {
+      uint32_t lw;
+      bool live;
+      word_of(c, &lw, &live);
+      const uint32_t yr = div_wpr(lw), j = lw - yr * dm.wpr, y = y0 + yr;
+      const uint32_t g = y * dm.wpr + j;
+      const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
+      const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
+      const uint32_t* rows[7] = {row(0, y), row(1, ym), row(2, ym), row(3, y),
+                                 row(4, yp), row(5, yp), row(6, y)};
+      uint32_t* out = shm + db * lbs + (size_t)yr * dm.wpr + j;
+      const Draws s = c == warp ? first : draws(g ^ seed32);
       if (d.rest)
-        step_word<true, true>(src, dst, d.solid, d.anysolid, inlet, dm, s, g, live);
+        step_core<true, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, s, g, y, j,
+                                    live);
       else
-        step_word<false, true>(src, dst, d.solid, d.anysolid, inlet, dm, s, g, live);
+        step_core<false, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, s, g, y, j,
+                                     live);
     }
-    // arrive (stores released at cluster scope), draw ahead, then wait
+    // arrive (shared-memory stores released at cluster scope), draw ahead, wait
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    if (k + 1u < p.len) first = draws(gfirst ^ step_seed32(d.seed, d.steps0 + local + 1u));
+    if (k + 1u < p.len) first = draws(g0 ^ step_seed32(d.seed, d.steps0 + local + 1u));
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-    // sampling point after step k + 1 of this launch
+    // sampling point after step k + 1 of this launch: from global memory
     const uint32_t t = k + 1u;
-    const bool due = nb && sch.every &&
-                     ((sch.since + t) % sch.every == 0u || t == sch.left);
+    const bool due = nb && sch.every && ((sch.since + t) % sch.every == 0u || t == sch.left);
     if (due) {
+      const uint32_t par = (d.cur0 + (uint32_t)(local + 1u)) & 1u;
+      store_band(db, par);
+      cluster.sync();
       SampleArgs sa;
-      sa.a = dst;
+      sa.a = par ? d.planes[1] : d.planes[0];
       sa.solid = d.solid;
       sa.dm = dm;
       sa.bx = d.bx;
@@ -85,22 +152,28 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
       sa.rho = d.field + 2 * nb;
       sa.sol = d.field + 3 * nb;
       sa.sums = d.sums;
-      for (uint32_t b = rank * nw + warp; b < nb; b += csize * nw) sample_block(sa, b);
+      for (uint32_t b = rank * nwarps + warp; b < nb; b += C * nwarps) sample_block(sa, b);
     }
   }
+  // the state after the interval, to the planes the next launch reads
+  store_band(p.len & 1u, (d.cur0 + (uint32_t)(base + p.len)) & 1u);
 }
 
 template <int THREADS>
 cudaError_t launch_resident_t(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
-                              cudaStream_t st) {
+                              size_t smem, cudaStream_t st) {
   if (csize > 8) {  // 16-CTA clusters are an opt-in per kernel (and device)
     cudaError_t e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
   }
+  cudaError_t e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nlat * csize);
   cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -119,15 +192,25 @@ bool resident_config_valid(uint32_t csize, uint32_t threads) {
          (threads == 128 || threads == 256 || threads == 512 || threads == 1024);
 }
 
+size_t resident_smem_bytes(const Dims& dm, uint32_t csize) {
+  const size_t cap = (dm.h + csize - 1) / csize;
+  return 2 * 7 * cap * dm.wpr * sizeof(uint32_t);
+}
+
+bool resident_fits(const Dims& dm, uint32_t csize) {
+  return dm.h >= 2 * csize && resident_smem_bytes(dm, csize) <= kResidentMaxSmem;
+}
+
 cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
-                            uint32_t threads, cudaStream_t st) {
+                            uint32_t threads, size_t smem, cudaStream_t st) {
   if (nlat == 0 || a.len == 0) return cudaSuccess;
-  if (!resident_config_valid(csize, threads)) return cudaErrorInvalidValue;
+  if (!resident_config_valid(csize, threads) || smem > kResidentMaxSmem)
+    return cudaErrorInvalidValue;
   switch (threads) {
-    case 128: return launch_resident_t<128>(a, nlat, csize, st);
-    case 256: return launch_resident_t<256>(a, nlat, csize, st);
-    case 512: return launch_resident_t<512>(a, nlat, csize, st);
-    default: return launch_resident_t<1024>(a, nlat, csize, st);
+    case 128: return launch_resident_t<128>(a, nlat, csize, smem, st);
+    case 256: return launch_resident_t<256>(a, nlat, csize, smem, st);
+    case 512: return launch_resident_t<512>(a, nlat, csize, smem, st);
+    default: return launch_resident_t<1024>(a, nlat, csize, smem, st);
   }
 }
 

@@ -126,6 +126,8 @@ struct lgx_server {
   std::atomic<size_t> in_use_now{0};
   std::atomic<size_t> peak_bytes{0}, peak_active{0};
   std::atomic<uint64_t> gpu_busy_ns{0};  // device time of finished ticks
+  std::atomic<uint64_t> host_tick_ns{0};  // host time spent in ticks
+  std::atomic<uint64_t> host_wait_ns{0};  // of which waiting for a ring slot (the device)
   int fault_alloc = 0;  // test hook: fail the next N admissions' allocation
   std::string fatal;
 };
@@ -270,7 +272,9 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
   auto& slot = s->ring[s->next_slot];
   s->next_slot = (s->next_slot + 1) % kRing;
   if (slot.used) {
+    const double t_wait = now_s();
     cudaError_t e = settle(s, slot);
+    s->host_wait_ns += (uint64_t)((now_s() - t_wait) * 1e9);
     if (e != cudaSuccess) return e;
   }
   slot.used = true;
@@ -522,7 +526,9 @@ void serve(lgx_server* s) {
     uint64_t len = lgx::kInletChunk;
     for (Req* r : s->active) len = std::min<uint64_t>(len, r->spec.steps - r->steps_done);
     lk.unlock();
+    const double t_tick = now_s();
     cudaError_t e = tick(s, len);
+    s->host_tick_ns += (uint64_t)((now_s() - t_tick) * 1e9);
     lk.lock();
     if (e != cudaSuccess) {
       s->fatal = std::string("serving tick: ") + cudaGetErrorString(e);
@@ -823,6 +829,8 @@ int lgx_server_get_stats(lgx_server* s, lgx_server_stats* out) {
   out->peak_bytes = s->peak_bytes;
   out->peak_active = s->peak_active;
   out->gpu_busy_ns = s->gpu_busy_ns;
+  out->host_tick_ns = s->host_tick_ns;
+  out->host_wait_ns = s->host_wait_ns;
   out->active = s->active.size();
   out->queued = s->pending.size();
   for (auto& kv : s->reqs) {

@@ -7,67 +7,65 @@
 
 namespace lgx {
 
-// Plane loads.  Within the persistent kernel the planes change between steps
-// and are written by other SMs, so they are read through L2 (ld.global.cg);
-// the single-step kernel may use the read-only path.
-template <bool COHERENT>
+// Plane loads.  LD_NC: the read-only path (the single-step and batched
+// kernels, whose planes do not change during the launch).  LD_CG: through L2
+// (ld.global.cg), for planes written by other SMs during the launch (the
+// persistent kernels).  LD_GENERIC: a plain load through a generic address,
+// for planes held in this CTA's or another cluster CTA's shared memory.
+enum { LD_NC = 0, LD_CG = 1, LD_GENERIC = 2 };
+
+template <int LD>
 __device__ __forceinline__ uint32_t ldp(const uint32_t* p) {
-  if (COHERENT) return __ldcg(p);
-  return __ldg(p);
+  if (LD == LD_NC) return __ldg(p);
+  if (LD == LD_CG) return __ldcg(p);
+  return *p;
 }
 
 // Word to the left of `j` in the same row, with the row's periodic wrap: for
 // j == 0 the bit that enters is bit `lastbit` of the last word, placed at 31.
-template <bool COHERENT>
+template <int LD>
 __device__ __forceinline__ uint32_t left_word(const uint32_t* row, uint32_t j, bool in_warp,
                                               uint32_t shuffled, const Dims& dm) {
   if (in_warp) return shuffled;
-  if (j > 0) return ldp<COHERENT>(row + j - 1);
-  return ldp<COHERENT>(row + dm.lastword) << (31u - dm.lastbit);
+  if (j > 0) return ldp<LD>(row + j - 1);
+  return ldp<LD>(row + dm.lastword) << (31u - dm.lastbit);
 }
 
 // Bits x+1 into x: (w >> 1) | (next << 31), and on the last word of the row
 // the bit at `lastbit` comes from bit 0 of word 0 (src/gpu.rs:248-254).
-template <bool COHERENT>
+template <int LD>
 __device__ __forceinline__ uint32_t shift_from_right(uint32_t w, const uint32_t* row, uint32_t j,
                                                      bool in_warp, uint32_t shuffled,
                                                      const Dims& dm) {
-  uint32_t hi = in_warp ? shuffled : ((j + 1u < dm.wpr) ? ldp<COHERENT>(row + j + 1u) : 0u);
+  uint32_t hi = in_warp ? shuffled : ((j + 1u < dm.wpr) ? ldp<LD>(row + j + 1u) : 0u);
   uint32_t v = __funnelshift_r(w, hi, 1);
   if (j == dm.lastword)
-    v = (v & ~(1u << dm.lastbit)) | ((ldp<COHERENT>(row) & 1u) << dm.lastbit);
+    v = (v & ~(1u << dm.lastbit)) | ((ldp<LD>(row) & 1u) << dm.lastbit);
   return v;
 }
 
-// One step of lattice word g (g clamped into range for idle lanes, which
-// still take part in the shuffles; `live` lanes store).  All 32 lanes of the
-// warp call this together with consecutive g.
-template <bool REST, bool COHERENT>
-__device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
-                                          const uint32_t* __restrict__ solid,
+// The update of one lattice word: word j of row y, global word index g (for
+// the draws' key, the obstacle planes and the inflow).  rows[d] points at
+// word 0 of the row plane d is gathered from (planes 1, 2: row y-1; 0, 3, 6:
+// row y; 4, 5: row y+1), out at word j of row y of plane 0 of the
+// destination, whose planes are `ostride` words apart.  All 32 lanes of the
+// warp call this together with consecutive words (lanes past the end repeat
+// the last word and do not store: `live`).
+template <bool REST, int LD>
+__device__ __forceinline__ void step_core(const uint32_t* const rows[7], uint32_t* out,
+                                          size_t ostride, const uint32_t* __restrict__ solid,
                                           const uint32_t* __restrict__ anysolid,
                                           const uint32_t* __restrict__ inlet, const Dims& dm,
-                                          const Draws& s, uint32_t g, bool live) {
+                                          const Draws& s, uint32_t g, uint32_t y, uint32_t j,
+                                          bool live) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t t = __umulhi(g, dm.div_m);
-  const uint32_t y = (t + ((g - t) >> dm.div_s1)) >> dm.div_s2;  // g / wpr
-  const uint32_t j = g - y * dm.wpr;
   const bool odd = y & 1u;
-  const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
-  const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
-  const size_t S = dm.total;
-
-  const uint32_t* r0 = a + 0 * S + (size_t)y * dm.wpr;
-  const uint32_t* r1 = a + 1 * S + (size_t)ym * dm.wpr;
-  const uint32_t* r2 = a + 2 * S + (size_t)ym * dm.wpr;
-  const uint32_t* r3 = a + 3 * S + (size_t)y * dm.wpr;
-  const uint32_t* r4 = a + 4 * S + (size_t)yp * dm.wpr;
-  const uint32_t* r5 = a + 5 * S + (size_t)yp * dm.wpr;
-
-  const uint32_t w0 = ldp<COHERENT>(r0 + j), w1 = ldp<COHERENT>(r1 + j);
-  const uint32_t w2 = ldp<COHERENT>(r2 + j), w3 = ldp<COHERENT>(r3 + j);
-  const uint32_t w4 = ldp<COHERENT>(r4 + j), w5 = ldp<COHERENT>(r5 + j);
-  const uint32_t w6 = ldp<COHERENT>(a + 6 * S + g);
+  const uint32_t *r0 = rows[0], *r1 = rows[1], *r2 = rows[2], *r3 = rows[3], *r4 = rows[4],
+                 *r5 = rows[5];
+  const uint32_t w0 = ldp<LD>(r0 + j), w1 = ldp<LD>(r1 + j);
+  const uint32_t w2 = ldp<LD>(r2 + j), w3 = ldp<LD>(r3 + j);
+  const uint32_t w4 = ldp<LD>(r4 + j), w5 = ldp<LD>(r5 + j);
+  const uint32_t w6 = ldp<LD>(rows[6] + j);
 
   // Partner lanes hold the neighbouring word of the same plane and row
   // exactly when they sit in the same row.
@@ -85,18 +83,18 @@ __device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
   //   d1: even x-1, odd x      d2: even x, odd x+1     (row y-1)
   //   d4: even x, odd x+1      d5: even x-1, odd x     (row y+1)
   uint32_t n[7];
-  n[0] = __funnelshift_l(left_word<COHERENT>(r0, j, lok, l0, dm), w0, 1);
-  n[3] = shift_from_right<COHERENT>(w3, r3, j, rok, q3, dm);
+  n[0] = __funnelshift_l(left_word<LD>(r0, j, lok, l0, dm), w0, 1);
+  n[3] = shift_from_right<LD>(w3, r3, j, rok, q3, dm);
   if (odd) {
     n[1] = w1;
-    n[2] = shift_from_right<COHERENT>(w2, r2, j, rok, q2, dm);
-    n[4] = shift_from_right<COHERENT>(w4, r4, j, rok, q4, dm);
+    n[2] = shift_from_right<LD>(w2, r2, j, rok, q2, dm);
+    n[4] = shift_from_right<LD>(w4, r4, j, rok, q4, dm);
     n[5] = w5;
   } else {
-    n[1] = __funnelshift_l(left_word<COHERENT>(r1, j, lok, l1, dm), w1, 1);
+    n[1] = __funnelshift_l(left_word<LD>(r1, j, lok, l1, dm), w1, 1);
     n[2] = w2;
     n[4] = w4;
-    n[5] = __funnelshift_l(left_word<COHERENT>(r5, j, lok, l5, dm), w5, 1);
+    n[5] = __funnelshift_l(left_word<LD>(r5, j, lok, l5, dm), w5, 1);
   }
   n[6] = w6;
 
@@ -132,8 +130,30 @@ __device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
   }
   if (live) {
 #pragma unroll
-    for (int d = 0; d < 7; ++d) b[d * S + g] = res[d];
+    for (int d = 0; d < 7; ++d) out[d * ostride] = res[d];
   }
+}
+
+// One step of lattice word g of planes a -> b (g clamped into range for idle
+// lanes, which still take part in the shuffles; `live` lanes store).
+template <bool REST, bool COHERENT>
+__device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
+                                          const uint32_t* __restrict__ solid,
+                                          const uint32_t* __restrict__ anysolid,
+                                          const uint32_t* __restrict__ inlet, const Dims& dm,
+                                          const Draws& s, uint32_t g, bool live) {
+  const uint32_t t = __umulhi(g, dm.div_m);
+  const uint32_t y = (t + ((g - t) >> dm.div_s1)) >> dm.div_s2;  // g / wpr
+  const uint32_t j = g - y * dm.wpr;
+  const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
+  const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
+  const size_t S = dm.total;
+  const uint32_t* rows[7] = {a + 0 * S + (size_t)y * dm.wpr,  a + 1 * S + (size_t)ym * dm.wpr,
+                             a + 2 * S + (size_t)ym * dm.wpr, a + 3 * S + (size_t)y * dm.wpr,
+                             a + 4 * S + (size_t)yp * dm.wpr, a + 5 * S + (size_t)yp * dm.wpr,
+                             a + 6 * S + (size_t)y * dm.wpr};
+  step_core<REST, COHERENT ? LD_CG : LD_NC>(rows, b + g, S, solid, anysolid, inlet, dm, s, g, y,
+                                            j, live);
 }
 
 

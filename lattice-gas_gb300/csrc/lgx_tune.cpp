@@ -4,9 +4,10 @@
 // rounded up to a power of two).  For each class the tuner times, on
 // synthetic lattices of the class's size and count, the two ways the batch can
 // step it: one batched launch per step, or the resident kernel (a cluster of
-// csize CTAs of `threads` threads per lattice, all steps of an interval in one
-// launch) for every cluster shape that gives each warp between one and
-// sixteen 32-word chunks.  The fastest wins.  Results are kept per device and
+// csize CTAs of `threads` threads per lattice holding it in shared memory, all
+// steps of an interval in one launch) for every cluster shape whose shared
+// memory holds the lattice and that gives each warp between one and sixteen
+// 32-word chunks.  The fastest wins.  Results are kept per device and
 // class for the life of the process, so a class is timed once.
 //
 // The synthetic lattices are zero-filled: the step's work does not depend on
@@ -140,11 +141,13 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   for (uint32_t cs : {1u, 2u, 4u, 8u, 16u})
     for (uint32_t th : {128u, 256u, 512u, 1024u}) {
       const uint32_t warps = cs * th / 32;
-      if (warps > nchunks || warps * 16 < nchunks) continue;
+      if (warps > nchunks || warps * 16 < nchunks || !resident_fits(dm, cs)) continue;
       float us = 0;
       ResidentArgs ra{(const LatDesc*)descs, (const ResSched*)sched, 0, (const uint64_t*)base,
                       kTuneSteps};
-      cudaError_t r = time_it([&]() { return launch_resident(ra, n, cs, th, s.st); }, &us);
+      const size_t smem = resident_smem_bytes(dm, cs);
+      cudaError_t r =
+          time_it([&]() { return launch_resident(ra, n, cs, th, smem, s.st); }, &us);
       if (r != cudaSuccess) {
         cudaGetLastError();  // a cluster shape this device cannot place: skip it
         continue;

@@ -53,7 +53,7 @@ class ServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "cancelled", "active", "queued",
                                           "ticks", "kernel_launches", "site_updates",
                                           "bytes_in_use", "peak_bytes", "peak_active",
-                                          "gpu_busy_ns")]
+                                          "gpu_busy_ns", "host_tick_ns", "host_wait_ns")]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
