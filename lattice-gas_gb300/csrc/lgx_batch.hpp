@@ -92,12 +92,15 @@ cudaError_t launch_batch_owner(const uint32_t* block0, uint32_t nlat, uint32_t n
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st);
 cudaError_t launch_batch_base(uint64_t* base, uint32_t n, cudaStream_t st);
 
-// Work enqueued after every batch step, inside the captured graphs: called
-// with the batch's stream, its device step counter for the interval and the
-// step's index within the interval plus one (the state after batch step
-// *base + k_after).  Setting a hook drops the graphs captured without it.
+// Work enqueued inside the captured graphs, after every batch step
+// (per_step) or once at the end of every interval that samples: called with
+// the batch's stream, its device step counter for the interval and the step's
+// index within the interval plus one (the state after batch step
+// *base + k_after).  A per-step hook needs every lattice in one chain of
+// per-step launches; an end-of-interval hook works with any policy.  Setting
+// a hook drops the graphs captured without it.
 typedef cudaError_t (*BatchStepHook)(void* ctx, cudaStream_t st, const uint64_t* base,
                                      uint32_t k_after);
-int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx);
+int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx, bool per_step);
 
 }  // namespace lgx

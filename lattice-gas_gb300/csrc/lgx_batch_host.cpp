@@ -87,6 +87,7 @@ struct lgx_batch {
   cudaEvent_t ev[8] = {};
   lgx::BatchStepHook hook = nullptr;
   void* hook_ctx = nullptr;
+  bool hook_per_step = true;
   int policy = LGX_BATCH_AUTO;
   uint32_t nstep = 0;                 // leading lattices stepped one launch per step
   std::vector<ResClass> classes;      // then the resident classes
@@ -252,7 +253,8 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
       lgx::BatchStepArgs sa{b->d_descs + sg.first, sg.d_block0, sg.d_owner, sg.count,
                             b->d_base, k, 0};
       e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks), st);
-      if (e == cudaSuccess && b->hook) e = b->hook(b->hook_ctx, st, b->d_base, k + 1);
+      if (e == cudaSuccess && b->hook && b->hook_per_step)
+        e = b->hook(b->hook_ctx, st, b->d_base, k + 1);
     }
     if (e == cudaSuccess && sg.st) {
       e = cudaEventRecord(sg.done, sg.st);
@@ -267,6 +269,8 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
     e = cudaEventRecord(b->join, b->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->join, 0);
   }
+  if (e == cudaSuccess && sample && b->hook && !b->hook_per_step)
+    e = b->hook(b->hook_ctx, b->stream, b->d_base, len);
   if (e == cudaSuccess) e = lgx::launch_batch_base(b->d_base, len, b->stream);
   cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
   if (e != cudaSuccess) {
@@ -278,6 +282,17 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
   return LGX_OK;
+}
+
+// Captured interval shapes a batch keeps; lengths beyond them run as
+// power-of-two pieces, so a caller that advances by many different lengths
+// does not pay a capture for each.
+constexpr size_t kMaxGraphs = 24;
+
+bool has_graph(const lgx_batch* b, uint32_t len, bool sample) {
+  for (const auto& g : b->graphs)
+    if (g.len == len && g.sample == sample) return true;
+  return false;
 }
 
 int graph_for(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
@@ -302,18 +317,19 @@ int graph_for(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out) {
 
 namespace lgx {
 
-int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx) {
+int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx, bool per_step) {
   if (!b) {
     lgx::set_error("null batch handle");
     return LGX_ERR_ARG;
   }
-  if (fn && !b->classes.empty()) {
+  if (fn && per_step && !b->classes.empty()) {
     lgx::set_error("a per-step hook needs every lattice stepped one launch per step");
     return LGX_ERR_STATE;
   }
   LGX_CUDA(cudaSetDevice(b->device));
   LGX_CUDA(cudaStreamSynchronize(b->stream));
-  if (fn && b->groups.size() > 1) LGX_CUDA(build_chains(b, 1));  // the hook follows every step
+  if (fn && per_step && b->groups.size() > 1)
+    LGX_CUDA(build_chains(b, 1));  // the hook follows every step of every lattice
   for (auto& g : b->graphs) {
     cudaGraphExecDestroy(g.exec);
     cudaFree(g.sched);
@@ -321,6 +337,7 @@ int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx) {
   b->graphs.clear();
   b->hook = fn;
   b->hook_ctx = ctx;
+  b->hook_per_step = per_step;
   return LGX_OK;
 }
 
@@ -498,7 +515,14 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
   while (left > 0) {
     uint64_t len = std::min<uint64_t>(left, lgx::kInletChunk);
     if (every > 0) len = std::min<uint64_t>(len, every - since);
-    const bool sample = every > 0 && (since + len >= every || len == left);
+    bool sample = every > 0 && (since + len >= every || len == left);
+    if (b->graphs.size() >= kMaxGraphs && !has_graph(b, (uint32_t)len, sample)) {
+      // enough shapes captured: run a new length as power-of-two pieces
+      uint64_t p2 = 1;
+      while (p2 * 2 <= len) p2 *= 2;
+      len = p2;
+      sample = every > 0 && (since + len >= every || len == left);
+    }
     if (b->items_per_step) {
       // prefix for this interval length
       std::vector<uint32_t> item0(b->lats.size() + 1, 0);
@@ -513,7 +537,8 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
     LGX_CUDA(cudaGraphLaunch(ex, b->stream));
     b->graph_launches += 1;
     const uint64_t per_step = b->groups.size();
-    b->launches += len * (per_step + (b->hook ? 1 : 0)) + 1 +
+    b->launches += len * (per_step + (b->hook && b->hook_per_step ? 1 : 0)) + 1 +
+                   (b->hook && !b->hook_per_step && sample ? 1 : 0) +
                    (sample && b->field_blocks ? 1 : 0) + (b->items_per_step ? 1 : 0) +
                    b->classes.size();
     left -= len;

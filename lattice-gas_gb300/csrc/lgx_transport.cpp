@@ -196,14 +196,17 @@ int upload_profiles(Run& r, const std::vector<lgx_lattice*>& lats,
   return LGX_OK;
 }
 
-int new_batch(Run& r, const std::vector<lgx_lattice*>& lats) {
+// per_step: the profile hook after every step (every lattice one launch per
+// step); otherwise at the end of every interval, which the advances end at
+// the sampling points, with the size classes stepped as the tuner finds fastest.
+int new_batch(Run& r, const std::vector<lgx_lattice*>& lats, bool per_step) {
   if (r.batch) {
     lgx_batch_destroy(r.batch);
     r.batch = nullptr;
   }
-  // every step is followed by the profile hook, so no lattice may be resident
-  LGX_RC(lgx_batch_create_ex(lats.data(), lats.size(), LGX_BATCH_PER_STEP, &r.batch));
-  return lgx::batch_set_step_hook(r.batch, profile_hook, &r);
+  LGX_RC(lgx_batch_create_ex(lats.data(), lats.size(),
+                             per_step ? LGX_BATCH_PER_STEP : LGX_BATCH_AUTO, &r.batch));
+  return lgx::batch_set_step_hook(r.batch, profile_hook, &r, per_step);
 }
 
 int measure(const float* densities, size_t n, int rest, uint64_t seed, size_t size,
@@ -297,7 +300,7 @@ int measure(const float* densities, size_t n, int rest, uint64_t seed, size_t si
     }
     r.meas[i].u_actual = mass ? (float)px2 * 0.5f / (float)mass : 0.0f;
   }
-  LGX_RC(new_batch(r, l1));
+  LGX_RC(new_batch(r, l1, false));
   uint64_t ran = 0, seen = 0;  // phase steps run; looks evaluated (slot index)
   std::vector<float> u((size_t)looks * N);
   size_t pending = M;
@@ -305,7 +308,8 @@ int measure(const float* densities, size_t n, int rest, uint64_t seed, size_t si
     const uint64_t last = kTransient + kBlock * kWindowLooks;
     const uint64_t target = std::min(last, ran == 0 ? kTransient + kBlock * 40 : ran + 2000);
     LGX_RC(upload_profiles(r, l1, m1, traj1, s1, ev1, looks, ran));
-    LGX_RC(lgx_batch_advance(r.batch, target - ran));
+    // intervals of 25 steps: every phase step that is a multiple of 25 ends one
+    LGX_RC(lgx_batch_advance_sampling(r.batch, target - ran, kBlock, 0.0f));
     ran = target;
     const uint64_t avail = (ran - kTransient) / kBlock + 1;  // slots written
     for (size_t i = 0; i < M; ++i) {
@@ -352,11 +356,32 @@ int measure(const float* densities, size_t n, int rest, uint64_t seed, size_t si
     traj2[i] = traj1[i / kReps] + (size_t)(i % kReps) * kSamples * N;  // reuse phase-1 space
     LGX_RC(restart(m, i % kReps, l2[i]));
   }
-  LGX_RC(new_batch(r, l2));
-  LGX_RC(upload_profiles(r, l2, m2, traj2, scratch, ev2, kSamples, 0));
-  // the last sample is taken after TRANSIENT + (SAMPLES - 1) * interval steps; the
-  // reference's final advance after it changes nothing it looks at
-  LGX_RC(lgx_batch_advance(r.batch, kTransient + (kSamples - 1) * longest));
+  // The last sample is taken after TRANSIENT + (SAMPLES - 1) * interval steps;
+  // the reference's final advance after it changes nothing it looks at.  With
+  // few sampling points (of any measurement) the batch advances from one to the
+  // next, each advance one interval ending at the point (a host round trip per
+  // point); with many, one advance runs every step with the profile hook after
+  // each (an extra launch per step, the lattices' own sampling steps picked on
+  // the device).
+  std::vector<uint64_t> points;
+  for (const Meas& m : r.meas)
+    for (int j = 0; j < kSamples; ++j) points.push_back(kTransient + (uint64_t)j * m.interval);
+  std::sort(points.begin(), points.end());
+  points.erase(std::unique(points.begin(), points.end()), points.end());
+  const uint64_t total = kTransient + (kSamples - 1) * longest;
+  const bool per_step = points.size() * 16 > total;
+  LGX_RC(new_batch(r, l2, per_step));
+  if (per_step) {
+    LGX_RC(upload_profiles(r, l2, m2, traj2, scratch, ev2, kSamples, 0));
+    LGX_RC(lgx_batch_advance(r.batch, total));
+  } else {
+    ran = 0;
+    for (uint64_t pt : points) {
+      LGX_RC(upload_profiles(r, l2, m2, traj2, scratch, ev2, kSamples, ran));
+      LGX_RC(lgx_batch_advance_sampling(r.batch, pt - ran, pt - ran, 0.0f));
+      ran = pt;
+    }
+  }
   std::vector<float> tr((size_t)kSamples * N);
   for (size_t mi = 0; mi < M; ++mi) {
     Meas& m = r.meas[mi];
