@@ -181,6 +181,24 @@ def cpu_reference_rate(wl, seconds: float, threads: int, chunk: int = 20):
     return wl.sites * steps / dt, steps, dt
 
 
+def cpu_bitplane_rate(wl, seconds: float, threads: int, chunk: int = 20):
+    """Site-updates/s of the bitplane update restated in C (the oracle's
+    GpuLattice, the same words and draws as the engine) on the host's cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    g = O.BitplaneLattice(wl.w, wl.h, wl.rest, wl.seed, threads)
+    g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, wl.rest)
+    g.attach_field(wl.block, wl.block)
+    g.load(wl.cells)
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        g.advance_sampling(chunk, wl.sample_every, wl.alpha)
+        steps += chunk
+    dt = time.perf_counter() - t0
+    return wl.sites * steps / dt, steps, dt
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
@@ -410,6 +428,8 @@ def bench_served(LG, W, n: int, budget: int):
             "served_s": round(t_served, 3), "plain_s": round(clock, 3),
             "ticks": st["ticks"], "kernel_launches": st["kernel_launches"],
             "device_busy_s": round(st["gpu_busy_ns"] / 1e9, 4),
+            "host_tick_s": round(st["host_tick_ns"] / 1e9, 4),
+            "host_wait_s": round(st["host_wait_ns"] / 1e9, 4),
             "latency_note": "includes queueing; the stream offers more work than the GPU "
                             "serves, so the queue grows while it arrives"}
 
@@ -496,6 +516,12 @@ def run_gb300(args, world, rank, local):
                "sample": "%d lattice steps of the wake run (%.1f s), byte-per-cell "
                          "Lattice::step restated in C (oracle/), %d threads"
                          % (nsteps, dt, threads)}
+        brate, bsteps, bdt = cpu_bitplane_rate(wl, 4.0, threads)
+        cpu["bitplane"] = {"value": round(brate / 1e9, 4), "unit": UNIT, "cores": threads,
+                           "kind": "port",
+                           "sample": "%d lattice steps of the wake run (%.1f s), the bitplane "
+                                     "update (GpuLattice's shader) restated in C, %d threads"
+                                     % (bsteps, bdt, threads)}
 
     batched = served = big = transport = None
     if not args.no_patterns:
@@ -561,8 +587,8 @@ def main():
     ap.add_argument("--no-patterns", action="store_true",
                     help="skip the batched and served measurements")
     ap.add_argument("--sweep-steps", type=int, default=5000)
-    ap.add_argument("--requests", type=int, default=64)
-    ap.add_argument("--budget-mib", type=int, default=4096)
+    ap.add_argument("--requests", type=int, default=256)
+    ap.add_argument("--budget-mib", type=int, default=16384)
     ap.add_argument("--big-steps", type=int, default=96)
     args = ap.parse_args()
     world, rank, local = dist_setup()
