@@ -409,7 +409,13 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
   }
   std::vector<bool> res_class(keys.size(), false);
   for (size_t k = 0; k < keys.size() && e == cudaSuccess; ++k) {
-    e = lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, &keys[k].plan);
+    if (lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, &keys[k].plan) !=
+        cudaSuccess) {
+      // the tuner could not run here (e.g. no room for its synthetic lattices):
+      // the class takes one launch per step
+      cudaGetLastError();
+      keys[k].plan = lgx::ClassPlan{};
+    }
     const lgx::ClassPlan& p = keys[k].plan;
     res_class[k] = policy == LGX_BATCH_RESIDENT ? p.csize != 0 : p.resident;
     for (size_t i = 0; i < n && res_class[k]; ++i)  // every member's band must fit

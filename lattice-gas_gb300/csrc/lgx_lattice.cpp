@@ -234,8 +234,12 @@ int enqueue_single(lgx_lattice* lat) {
 int resolve_auto(lgx_lattice* lat) {
   if (lat->auto_resolved) return LGX_OK;
   lgx::StepPlan p;
-  const int rc = lgx::plan_step_mode(lat->device, lat->dm.w, lat->dm.h, lat->rest, &p);
-  if (rc) return rc;
+  if (lgx::plan_step_mode(lat->device, lat->dm.w, lat->dm.h, lat->rest, &p) != LGX_OK) {
+    // the tuner could not run here (e.g. no room for its scratch lattice): the
+    // reference's own launch pattern, one kernel per step
+    cudaGetLastError();
+    p = lgx::StepPlan{LGX_STEP_SINGLE, 0, 0, 0, 0, 0};
+  }
   lat->auto_mode = p.mode;
   lat->auto_depth = p.depth;
   lat->auto_us[0] = p.single_us;
