@@ -6,7 +6,8 @@
 Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
 `sweep` (the 64-lattice transport sweep as one batch), `transport` (one
-transport::measure at --size, density 0.22).  --policy picks the sweep's batch
+transport::measure at --size, density 0.22), `fill` (init_equilibrium on the
+device over the roofline case's geometry at 16384 x 8192).  --policy picks the sweep's batch
 policy (under a profiler pass 1: the tuner's timings are not meaningful there, and
 without one it picks one launch per step for every class of this sweep).  --mode
 picks the step
@@ -24,7 +25,8 @@ from lattice_gas import workloads as W  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="wake", choices=["wake", "big", "sweep", "transport"])
+    ap.add_argument("--case", default="wake",
+                    choices=["wake", "big", "sweep", "transport", "fill"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--policy", type=int, default=0,
                     help="batch policy for the sweep: 0 tuned, 1 one launch per step, 2 resident")
@@ -32,6 +34,14 @@ def main():
     ap.add_argument("--mode", type=int, default=1)
     ap.add_argument("--depth", type=int, default=4)
     a = ap.parse_args()
+    if a.case == "fill":
+        wl = W.roofline_case(w=16384, h=8192, n_circles=50)
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.load(wl.cells)
+        for _ in range(3):
+            g.init_equilibrium(0.2, (0.1, 0.0), 0x5EED)
+        print("fill: %d x %d, %d particles" % (wl.w, wl.h, g.total_particles()))
+        return
     if a.case == "transport":
         r = LG.transport_measure([0.22], rest=True, seed=0x5EED, size=a.size)[0]
         print("transport %d: nu %.4f g %.4f windows %d %d" % (a.size, r.nu, r.g, r.window_nu,
