@@ -111,6 +111,12 @@ int lgx_sample_field(lgx_lattice *lat, float alpha);
 /* GpuLattice::read_field (src/gpu.rs:725-736): n_blocks must be bw*bh. */
 int lgx_read_field(lgx_lattice *lat, float *ux, float *uy, float *rho, float *sol,
                    size_t n_blocks);
+/* Field::vorticity (src/render.rs:127-143) of the attached field, on the device:
+ * n_blocks must be bw*bh. */
+int lgx_field_vorticity(lgx_lattice *lat, float *w, size_t n_blocks);
+/* Field::mean_velocity (src/render.rs:146-161): the mean of the blocks whose solid
+ * fraction is below one half, summed in block order as the reference does. */
+int lgx_field_mean_velocity(lgx_lattice *lat, float *ux, float *uy);
 /* New: the exact integer block sums (FLUID view, src/moments.rs:37-74) of the
  * most recent sample: mass, px2 (half units), py2 (units of sqrt(3)/2), and
  * the count of obstacle cells.  n_blocks must be bw*bh. */
@@ -286,6 +292,8 @@ typedef struct {
   uint64_t ticks, kernel_launches, site_updates;
   uint64_t bytes_in_use, peak_bytes, peak_active;
   uint64_t gpu_busy_ns;  /* device time of the ticks run so far (start to end of each) */
+  uint64_t host_tick_ns; /* host time the server thread spent in ticks */
+  uint64_t host_wait_ns; /* of which waiting for the device to free a descriptor slot */
 } lgx_server_stats;
 
 typedef struct lgx_server lgx_server;

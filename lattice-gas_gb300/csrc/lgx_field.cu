@@ -9,6 +9,9 @@
 
 namespace lgx {
 
+// A single f32 product on the host (one rounding, as the reference's `by as f32 * SQRT3_2`).
+static inline float __fmul_rn_host(float a, float b) { return a * b; }
+
 namespace {
 
 __global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p) {
@@ -105,6 +108,57 @@ __global__ void lgx_verify_kernel(uint32_t* out, uint32_t n) {
 }
 
 }  // namespace
+
+// Field::vorticity (src/render.rs:127-143): on the block grid, dv/dx by a
+// one-sided difference at the first and last column and a central one
+// between, du/dy central with the rows periodic; f32 operations one by one,
+// rounded to nearest, as the reference's Rust (which never fuses).
+__global__ void __launch_bounds__(256) lgx_vorticity_kernel(const float* __restrict__ ux,
+                                                            const float* __restrict__ uy,
+                                                            uint32_t bw, uint32_t bh, float dx,
+                                                            float dy, float* __restrict__ out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= bw * bh) return;
+  const uint32_t j = k / bw, i = k - j * bw;
+  const uint32_t ip = min(i + 1u, bw - 1u), im = i ? i - 1u : 0u;
+  const uint32_t jp = j + 1u < bh ? j + 1u : 0u, jm = j ? j - 1u : bh - 1u;
+  const float dvdx = __fdiv_rn(__fsub_rn(uy[j * bw + ip], uy[j * bw + im]),
+                               __fmul_rn(__uint2float_rn(ip - im), dx));
+  const float dudy = __fdiv_rn(__fsub_rn(ux[jp * bw + i], ux[jm * bw + i]), __fmul_rn(2.0f, dy));
+  out[k] = __fsub_rn(dvdx, dudy);
+}
+
+// Field::mean_velocity (src/render.rs:146-161): the f32 sums run in block
+// order, as the reference adds them, so one thread adds them all.
+__global__ void lgx_mean_velocity_kernel(const float* __restrict__ ux,
+                                         const float* __restrict__ uy,
+                                         const float* __restrict__ sol, uint32_t nb,
+                                         float* __restrict__ out) {
+  float sx = 0.0f, sy = 0.0f, n = 0.0f;
+  for (uint32_t k = 0; k < nb; ++k)
+    if (sol[k] < 0.5f) {
+      sx = __fadd_rn(sx, ux[k]);
+      sy = __fadd_rn(sy, uy[k]);
+      n = __fadd_rn(n, 1.0f);
+    }
+  out[0] = n == 0.0f ? 0.0f : __fdiv_rn(sx, n);
+  out[1] = n == 0.0f ? 0.0f : __fdiv_rn(sy, n);
+}
+
+cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
+                             uint32_t by, float* out, cudaStream_t st) {
+  const uint32_t nb = bw * bh;
+  if (nb == 0) return cudaSuccess;
+  const float dx = (float)bx;
+  const float dy = __fmul_rn_host((float)by, 0.8660254f);
+  lgx_vorticity_kernel<<<(nb + 255) / 256, 256, 0, st>>>(field, field + nb, bw, bh, dx, dy, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cudaStream_t st) {
+  lgx_mean_velocity_kernel<<<1, 1, 0, st>>>(field, field + nb, field + 3 * nb, nb, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st) {
   const uint32_t nb = s.bw * s.bh;

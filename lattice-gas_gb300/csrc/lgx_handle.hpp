@@ -55,4 +55,5 @@ struct lgx_lattice {
   // row and column profiles: scratch, row_ux[h], column_uy[w], column sums
   // [3][w] and the device copy of the profile descriptor, one allocation
   void* prof = nullptr;
+  float* vort = nullptr;  // vorticity of the field, bw*bh, then the mean velocity (2)
 };

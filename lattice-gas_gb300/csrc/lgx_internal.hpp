@@ -104,6 +104,11 @@ bool temporal_supported(const Dims& dm, uint32_t k);
 void temporal_tiling(const Dims& dm, uint32_t k, TemporalArgs* t);  // k steps per pass
 cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaStream_t st);
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
+// Field::vorticity and Field::mean_velocity of a field laid out ux | uy | rho |
+// sol (bw * bh each); out: bw * bh floats, or (mean ux, mean uy).
+cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
+                             uint32_t by, float* out, cudaStream_t st);
+cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
                          cudaStream_t st);
 // Byte cells (w*h, row-major) <-> planes + solid + anysolid.

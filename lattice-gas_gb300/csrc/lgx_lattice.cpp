@@ -91,6 +91,7 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->field);
   cudaFree(lat->sums);
   cudaFree(lat->prof);
+  cudaFree(lat->vort);
   cudaFree(lat->done);
   cudaFree(lat->error);
   for (auto& e : lat->ev)
@@ -446,8 +447,10 @@ int lgx_attach_field(lgx_lattice* lat, size_t bx, size_t by) {
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
   cudaFree(lat->field);
   cudaFree(lat->sums);
+  cudaFree(lat->vort);  // sized for the old block grid
   lat->field = nullptr;
   lat->sums = nullptr;
+  lat->vort = nullptr;
   lat->has_field = false;
   lat->bx = (uint32_t)bx;
   lat->by = (uint32_t)by;
@@ -594,6 +597,57 @@ int lgx_read_field(lgx_lattice* lat, float* ux, float* uy, float* rho, float* so
       LGX_CUDA(cudaMemcpyAsync(dst[i], lat->field + i * nb, nb * sizeof(float),
                                cudaMemcpyDeviceToHost, lat->stream));
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+// The vorticity / mean-velocity buffer of the attached field.
+static int field_scratch(lgx_lattice* lat, float** out) {
+  if (!lat->has_field) {
+    lgx::set_error("no field attached to this lattice");
+    return LGX_ERR_STATE;
+  }
+  if (!lat->vort) LGX_CUDA(cudaMalloc(&lat->vort, ((size_t)lat->bw * lat->bh + 2) * 4));
+  *out = lat->vort;
+  return LGX_OK;
+}
+
+int lgx_field_vorticity(lgx_lattice* lat, float* w, size_t n_blocks) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  float* d = nullptr;
+  rc = field_scratch(lat, &d);
+  if (rc) return rc;
+  const size_t nb = (size_t)lat->bw * lat->bh;
+  if (!w || n_blocks != nb) {
+    lgx::set_error("lgx_field_vorticity: need one value per field block");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(lgx::launch_vorticity(lat->field, lat->bw, lat->bh, lat->bx, lat->by, d,
+                                 lat->stream));
+  lat->launches += 1;
+  LGX_CUDA(cudaMemcpyAsync(w, d, nb * 4, cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  return LGX_OK;
+}
+
+int lgx_field_mean_velocity(lgx_lattice* lat, float* ux, float* uy) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  float* d = nullptr;
+  rc = field_scratch(lat, &d);
+  if (rc) return rc;
+  if (!ux || !uy) {
+    lgx::set_error("lgx_field_mean_velocity: null output");
+    return LGX_ERR_ARG;
+  }
+  const size_t nb = (size_t)lat->bw * lat->bh;
+  LGX_CUDA(lgx::launch_mean_velocity(lat->field, (uint32_t)nb, d + nb, lat->stream));
+  lat->launches += 1;
+  float v[2];
+  LGX_CUDA(cudaMemcpyAsync(v, d + nb, 8, cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  *ux = v[0];
+  *uy = v[1];
   return LGX_OK;
 }
 

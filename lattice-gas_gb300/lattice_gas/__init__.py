@@ -137,6 +137,8 @@ def lib():
         _sig(L, "lgx_read_block_sums", vp, i32p, i32p, i32p, i32p, sz)
         _sig(L, "lgx_total_particles", vp, C.POINTER(C.c_uint64))
         _sig(L, "lgx_row_ux", vp, f32p, sz)
+        _sig(L, "lgx_field_vorticity", vp, f32p, sz)
+        _sig(L, "lgx_field_mean_velocity", vp, f32p, f32p)
         _sig(L, "lgx_column_uy", vp, f32p, sz)
         _sig(L, "lgx_line_sums", vp, i32p, sz, i32p, sz)
         _sig(L, "lgx_steps", vp, C.POINTER(C.c_uint64))
@@ -276,6 +278,19 @@ class GpuLattice:
             out = np.zeros(self.w * self.h, np.uint8)
         _check(lib().lgx_store(self._h, _p(out, C.c_uint8), out.size))
         return out
+
+    def vorticity(self) -> np.ndarray:
+        """Field::vorticity (src/render.rs:127-143) of the attached field, on the device."""
+        bx, by, bw, bh = self._field
+        out = np.zeros(bw * bh, np.float32)
+        _check(lib().lgx_field_vorticity(self._h, _p(out, C.c_float), out.size))
+        return out
+
+    def mean_velocity(self):
+        """Field::mean_velocity (src/render.rs:146-161) of the attached field."""
+        ux, uy = C.c_float(), C.c_float()
+        _check(lib().lgx_field_mean_velocity(self._h, C.byref(ux), C.byref(uy)))
+        return np.float32(ux.value), np.float32(uy.value)
 
     @property
     def step_plan(self) -> dict:

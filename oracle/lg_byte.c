@@ -501,3 +501,37 @@ uint64_t lgo_fnv1a(const uint8_t *bytes, size_t n) {
     }
     return h;
 }
+
+/* ---- render.rs: Field::vorticity, Field::mean_velocity ---------------------- */
+void lgo_field_vorticity(const float *ux, const float *uy, size_t bw, size_t bh, size_t bx,
+                         size_t by, float *out) {
+    float dx = (float)bx;
+    float dy = (float)by * SQRT3_2;
+    for (size_t j = 0; j < bh; ++j)
+        for (size_t i = 0; i < bw; ++i) {
+            size_t ip = i + 1 < bw - 1 ? i + 1 : bw - 1;
+            size_t im = i > 0 ? i - 1 : 0;
+            size_t jp = j + 1 < bh ? j + 1 : 0;
+            size_t jm = j == 0 ? bh - 1 : j - 1;
+            float num = uy[j * bw + ip] - uy[j * bw + im];
+            float den = (float)(ip - im) * dx;
+            float dvdx = num / den;
+            float num2 = ux[jp * bw + i] - ux[jm * bw + i];
+            float den2 = 2.0f * dy;
+            float dudy = num2 / den2;
+            out[j * bw + i] = dvdx - dudy;
+        }
+}
+
+void lgo_field_mean_velocity(const float *ux, const float *uy, const float *sol, size_t nb,
+                             float *mx, float *my) {
+    float sx = 0.0f, sy = 0.0f, n = 0.0f;
+    for (size_t k = 0; k < nb; ++k)
+        if (sol[k] < 0.5f) {
+            sx += ux[k];
+            sy += uy[k];
+            n += 1.0f;
+        }
+    *mx = n == 0.0f ? 0.0f : sx / n;
+    *my = n == 0.0f ? 0.0f : sy / n;
+}

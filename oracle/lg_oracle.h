@@ -96,6 +96,12 @@ void lgo_field_sample(const uint8_t *cells, size_t w, size_t h, size_t bx, size_
 void lgo_block_sums(const uint8_t *cells, size_t w, size_t h, size_t bx, size_t by,
                     int32_t *mass, int32_t *px2, int32_t *py2, int32_t *nsolid);
 uint64_t lgo_fnv1a(const uint8_t *bytes, size_t n);                   /* golden.rs:40 */
+/* Field::vorticity and Field::mean_velocity (render.rs:127-161) of a field. */
+void lgo_field_vorticity(const float *ux, const float *uy, size_t bw, size_t bh, size_t bx,
+                         size_t by, float *out);
+void lgo_field_mean_velocity(const float *ux, const float *uy, const float *sol, size_t nb,
+                             float *mx, float *my);
+
 
 /* ---- bitplane path (src/gpu.rs) ------------------------------------------ */
 uint32_t lgo_mix(uint32_t x);                                          /* gpu.rs:147 */

@@ -89,6 +89,8 @@ def lib():
         _sig(L, "lgo_cells_column_wave", None, u8p, sz, sz, C.c_float, C.c_float, f32p, C.c_int,
              C.c_uint64)
         _sig(L, "lgo_row_ux", None, u8p, sz, sz, f32p)
+        _sig(L, "lgo_field_vorticity", None, f32p, f32p, sz, sz, sz, sz, f32p)
+        _sig(L, "lgo_field_mean_velocity", None, f32p, f32p, f32p, sz, f32p, f32p)
         _sig(L, "lgo_column_uy", None, u8p, sz, sz, f32p)
         _sig(L, "lgo_transport_measure", None, C.c_float, C.c_int, sz, C.c_uint64, sz, C.c_int,
              C.POINTER(TransportResult))
@@ -378,3 +380,24 @@ def transport_measure(density, rest, threads, seed, size, gpu):
     lib().lgo_transport_measure(float(density), int(bool(rest)), int(threads),
                                 seed & (2**64 - 1), int(size), int(bool(gpu)), C.byref(r))
     return r
+
+
+def field_vorticity(ux, uy, bw, bh, bx, by):
+    """Field::vorticity (src/render.rs:127-143)."""
+    a = np.ascontiguousarray(ux, dtype=np.float32)
+    b = np.ascontiguousarray(uy, dtype=np.float32)
+    out = np.zeros(bw * bh, np.float32)
+    lib().lgo_field_vorticity(ptr(a, C.c_float), ptr(b, C.c_float), bw, bh, bx, by,
+                              ptr(out, C.c_float))
+    return out
+
+
+def field_mean_velocity(ux, uy, sol):
+    """Field::mean_velocity (src/render.rs:146-161)."""
+    a = np.ascontiguousarray(ux, dtype=np.float32)
+    b = np.ascontiguousarray(uy, dtype=np.float32)
+    c = np.ascontiguousarray(sol, dtype=np.float32)
+    mx, my = C.c_float(), C.c_float()
+    lib().lgo_field_mean_velocity(ptr(a, C.c_float), ptr(b, C.c_float), ptr(c, C.c_float), a.size,
+                                  C.byref(mx), C.byref(my))
+    return np.float32(mx.value), np.float32(my.value)

@@ -1,0 +1,31 @@
+"""Field::vorticity and Field::mean_velocity (src/render.rs:127-161) on the device,
+against the oracle's restatement applied to the same field, bit for bit (NaN where
+the reference divides 0 by 0, a one-column block grid).  Needs a GPU."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("w,h,bx,by", [(256, 128, 16, 16), (300, 96, 20, 8), (128, 64, 32, 32),
+                                       (64, 40, 64, 10)])
+def test_vorticity_and_mean_velocity_match_the_oracle(LG, O, w, h, bx, by):
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, w / 3.0, h * 0.43, h / 5.0)
+    LG.init_equilibrium(cells, 0.3, 0.2, 0.05, True, 77)
+    g = LG.GpuLattice(w, h, True, 5)
+    g.set_inlet(8, 0.3, (0.2, 0.0), True)
+    g.attach_field(bx, by)
+    g.load(cells)
+    g.advance_sampling(150, 30, 0.5)
+    f = g.read_field()
+    bw, bh = w // bx, h // by
+    want = O.field_vorticity(f.ux, f.uy, bw, bh, bx, by)
+    got = g.vorticity()
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    ok = ~np.isnan(want)
+    assert np.array_equal(got[ok].view(np.uint32), want[ok].view(np.uint32))
+    mx, my = g.mean_velocity()
+    wx, wy = O.field_mean_velocity(f.ux, f.uy, f.solid)
+    assert np.float32(mx).view(np.uint32) == np.float32(wx).view(np.uint32)
+    assert np.float32(my).view(np.uint32) == np.float32(wy).view(np.uint32)
