@@ -108,3 +108,24 @@ def test_destroy_with_work_in_flight(LG):
     for r in reqs:
         srv.submit_workload(r.work)
     srv.close()   # cancels what is queued or running, then joins
+
+
+def test_mixed_rules_in_one_tick(LG):
+    """Rest-particle and six-direction requests resident together (one launch per step
+    for both rules, two launch chains): each result is still the one it has alone."""
+    import dataclasses
+    reqs = small_stream(11, 12)
+    works = []
+    for i, r in enumerate(reqs):
+        wl = r.work
+        if i % 2:
+            cells = wl.cells & np.uint8(0xBF)  # no rest particles in a six-direction lattice
+            wl = dataclasses.replace(wl, rest=False, cells=cells)
+        works.append(wl)
+    srv = LG.Server(budget_bytes=512 << 20, max_active=64)
+    ids = [srv.submit_workload(wl) for wl in works]
+    for rid in ids:
+        assert srv.wait(rid, 120.0) == LG.REQ_DONE
+    for wl, rid in zip(works, ids):
+        check_same(srv.result(rid), alone(LG, wl))
+    srv.close()
