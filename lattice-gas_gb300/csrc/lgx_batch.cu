@@ -22,10 +22,9 @@
 namespace lgx {
 namespace {
 
-constexpr int kThreads = 256;
-#ifndef LGX_BATCH_MINB
-#define LGX_BATCH_MINB 4  // resident blocks per SM the register allocation must allow
-#endif
+// A block of the batched step covers 256 lattice words (the unit of the block
+// tables): WORDS consecutive 32-word chunks per warp, 256 / WORDS threads,
+// compiled for 4 * WORDS resident blocks per SM (64 registers).
 
 template <bool REST>
 __device__ __forceinline__ void batch_word(const LatDesc& d, uint64_t local, uint32_t k,
@@ -51,39 +50,42 @@ __device__ __forceinline__ uint32_t owner_of(const uint32_t* prefix, uint32_t n,
   return lo;
 }
 
-template <bool REST>
-__global__ void __launch_bounds__(kThreads, LGX_BATCH_MINB) lgx_batch_step_kernel(BatchStepArgs p) {
+// One step of the lattice words a block covers; RULE: 0 six-direction, 1 rest
+// particles, 2 the lattice's own (a block belongs to one lattice, so the rule
+// is uniform across it: one launch serves a batch mixing both).
+template <int RULE, int WORDS>
+__device__ __forceinline__ void batch_block(const BatchStepArgs& p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
-  uint32_t g = (blk - __ldg(p.block0 + li)) * (uint32_t)kThreads + threadIdx.x;
-  const bool live = g < d.dm.total;
-  if (!live) g = d.dm.total - 1u;
+  const uint32_t g0 = (blk - __ldg(p.block0 + li)) * 256u + (threadIdx.x & ~31u) * WORDS +
+                      (threadIdx.x & 31u);
   const uint64_t local = *p.base + p.k;
-  const Draws s = draws(g ^ step_seed32(d.seed, d.steps0 + local));
+  const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
+  uint32_t g[WORDS];
+  bool live[WORDS];
+  Draws s[WORDS];
+#pragma unroll
+  for (int q = 0; q < WORDS; ++q) {
+    g[q] = g0 + 32u * q;
+    live[q] = g[q] < d.dm.total;
+    if (!live[q]) g[q] = d.dm.total - 1u;
+    s[q] = draws(g[q] ^ seed32);
+  }
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  batch_word<REST>(d, local, p.k, g, live, s);
+#pragma unroll
+  for (int q = 0; q < WORDS; ++q) {
+    if (RULE == 2 ? d.rest != 0 : RULE == 1)
+      batch_word<true>(d, local, p.k, g[q], live[q], s[q]);
+    else
+      batch_word<false>(d, local, p.k, g[q], live[q], s[q]);
+  }
 }
 
-// Both rules in one launch: a block belongs to one lattice, so the rule is
-// uniform across it.  Used when a batch mixes rest-particle and six-direction
-// lattices, to keep one launch per step.
-__global__ void __launch_bounds__(kThreads, LGX_BATCH_MINB) lgx_batch_step_mixed_kernel(BatchStepArgs p) {
-  const uint32_t blk = p.first_block + blockIdx.x;
-  const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
-  const LatDesc& d = p.descs[li];
-  uint32_t g = (blk - __ldg(p.block0 + li)) * (uint32_t)kThreads + threadIdx.x;
-  const bool live = g < d.dm.total;
-  if (!live) g = d.dm.total - 1u;
-  const uint64_t local = *p.base + p.k;
-  const Draws s = draws(g ^ step_seed32(d.seed, d.steps0 + local));
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  if (d.rest)
-    batch_word<true>(d, local, p.k, g, live, s);
-  else
-    batch_word<false>(d, local, p.k, g, live, s);
+template <int RULE, int WORDS>
+__global__ void __launch_bounds__(256 / WORDS, 4 * WORDS) lgx_batch_step_kernel(BatchStepArgs p) {
+  batch_block<RULE, WORDS>(p);
 }
 
 // Inlet draws for steps base .. base + nsteps - 1 of every lattice with an
@@ -145,20 +147,25 @@ __global__ void lgx_batch_owner_kernel(const uint32_t* block0, uint32_t nlat, ui
 
 }  // namespace
 
-cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule,
+cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
-  cfg.blockDim = dim3(kThreads);
+  cfg.blockDim = dim3(words == 2 ? 128 : 256);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_step_mixed_kernel, a);
-  if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<true>, a);
-  return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<false>, a);
+  if (words == 2) {
+    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<2, 2>, a);
+    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<1, 2>, a);
+    return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<0, 2>, a);
+  }
+  if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<2, 1>, a);
+  if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<1, 1>, a);
+  return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<0, 1>, a);
 }
 
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st) {

@@ -83,7 +83,12 @@ cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize
 
 // The rule of the blocks a batched step launch covers.
 constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;
-cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule,
+// words: 32-word chunks per warp (1: 256-thread blocks, 2: 128-thread blocks);
+// a block covers 256 words either way.  Two chunks per warp give each thread
+// two independent word updates to interleave: +2% on the graph-replayed
+// transport sweep, but -14% on the served stream's host-launched ticks, so
+// the batch uses 2 and the server 1.
+cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st);
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st);
 // owner[b] = the lattice whose blocks include block b, for b < nblocks.
