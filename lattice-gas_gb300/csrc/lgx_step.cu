@@ -31,19 +31,13 @@ namespace lgx {
 
 namespace {
 
-// The single-step kernel's shape: 128-thread blocks, each warp taking two
-// consecutive 32-word chunks (two independent word updates per thread for the
-// scheduler to interleave), compiled for six resident blocks per SM.  Measured
-// against one chunk per warp in 256-thread blocks: 7.69 -> 7.22 us per
-// wake-run step, 95.6 -> 91.4 us at 16384 x 8192.
-#ifndef LGX_STEP_THREADS
-#define LGX_STEP_THREADS 128
-#endif
-constexpr int kStepThreads = LGX_STEP_THREADS;
-#ifndef LGX_STEP_WORDS
-#define LGX_STEP_WORDS 2  // 32-word chunks per warp of the single-step kernel
-#endif
-constexpr int kStepWords = LGX_STEP_WORDS;
+// The single-step kernel's shapes, both compiled for six resident blocks per
+// SM.  A lattice that fills the GPU takes 128-thread blocks with two
+// consecutive 32-word chunks per warp (two independent word updates per thread
+// for the scheduler to interleave: 7.69 -> 7.22 us per wake-run step, 95.6 ->
+// 91.4 us at 16384 x 8192); a smaller one, whose step is latency-bound, takes
+// 256-thread blocks with one chunk per warp (twice the threads in flight).
+constexpr uint32_t kTwoChunkMinWords = 152u * 6u * 256u;  // one wave of two-chunk blocks
 constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
 // Resident blocks per SM the register allocation must allow (64 registers).
 #ifndef LGX_STEP_MINB
@@ -61,11 +55,11 @@ constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
 // visible (griddepcontrol.wait).  Step N+1's draws thereby fill the SMs that
 // step N's last blocks leave idle.  Without a programmatic predecessor the
 // wait returns at once, so the kernel is also correct launched plainly.
-template <bool REST>
-__global__ void __launch_bounds__(kStepThreads, LGX_STEP_MINB) lgx_step_kernel(const StepArgs p) {
-  // a warp takes kStepWords consecutive 32-word chunks
-  const uint32_t g0 = blockIdx.x * (kStepThreads * kStepWords) +
-                      (threadIdx.x & ~31u) * kStepWords + (threadIdx.x & 31u);
+template <bool REST, int WORDS>
+__global__ void __launch_bounds__(256 / WORDS, LGX_STEP_MINB) lgx_step_kernel(const StepArgs p) {
+  // a warp takes WORDS consecutive 32-word chunks; a block covers 256 words
+  constexpr int kStepWords = WORDS;
+  const uint32_t g0 = blockIdx.x * 256u + (threadIdx.x & ~31u) * kStepWords + (threadIdx.x & 31u);
   const uint32_t seed32 = step_seed32(p.seed, p.steps);
   uint32_t g[kStepWords];
   bool live[kStepWords];
@@ -217,8 +211,9 @@ __global__ void __launch_bounds__(128) lgx_inlet_kernel(const InletArgs p) {
 
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((s.dm.total + kStepThreads * kStepWords - 1) / (kStepThreads * kStepWords));
-  cfg.blockDim = dim3(kStepThreads);
+  const bool two = s.dm.total >= kTwoChunkMinWords;
+  cfg.gridDim = dim3((s.dm.total + 255u) / 256u);
+  cfg.blockDim = dim3(two ? 128 : 256);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -226,8 +221,12 @@ cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (rest) return cudaLaunchKernelEx(&cfg, lgx_step_kernel<true>, s);
-  return cudaLaunchKernelEx(&cfg, lgx_step_kernel<false>, s);
+  if (two) {
+    if (rest) return cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 2>, s);
+    return cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 2>, s);
+  }
+  if (rest) return cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 1>, s);
+  return cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 1>, s);
 }
 
 cudaError_t wave_grid(bool rest, uint32_t total, uint32_t* grid) {
