@@ -103,7 +103,10 @@ int lgx_set_temporal_depth(lgx_lattice *lat, int k);
 typedef struct lgx_step_plan {
   int mode;
   uint32_t depth;
-  float single_us, wave_us, temporal4_us, temporal8_us;
+  uint32_t words;          /* 32-word chunks per warp of the single-step kernel */
+  float single_us;         /* one launch per step, with that shape */
+  float single1_us, single2_us;  /* one launch per step, one and two chunks per warp */
+  float wave_us, temporal4_us, temporal8_us;
 } lgx_step_plan;
 int lgx_get_step_plan(lgx_lattice *lat, lgx_step_plan *out);
 /* GpuLattice::sample_field (src/gpu.rs:710-721). */

@@ -48,7 +48,9 @@ struct lgx_lattice {
   bool auto_resolved = false;   // LGX_STEP_AUTO: the tuner's choice below is set
   int auto_mode = LGX_STEP_SINGLE;
   uint32_t auto_depth = 0;
-  float auto_us[4] = {0, 0, 0, 0};  // single, wave, temporal 4, temporal 8 (us per step)
+  uint32_t auto_words = 0;        // chunks per warp of the single-step kernel
+  float auto_us[6] = {0, 0, 0, 0, 0, 0};  // single (best, 1, 2 chunks), wave, temporal 4, 8
+  uint32_t step_words = 0;        // a pinned kernel shape (0: by size, or the tuner's)
   uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
   uint32_t* done = nullptr;  // [wave_grid] published step per CTA
   uint32_t* error = nullptr; // timeout flag

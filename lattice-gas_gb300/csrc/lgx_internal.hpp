@@ -37,6 +37,7 @@ struct StepArgs {
   Dims dm;
   uint64_t seed;
   uint64_t steps;  // steps taken before this one
+  uint32_t words;  // 32-word chunks per warp (1 or 2; 0: chosen by the lattice's size)
 };
 
 // `nsteps` steps of one lattice in one cooperative launch.  The state after

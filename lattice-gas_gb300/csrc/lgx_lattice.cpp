@@ -221,6 +221,9 @@ int enqueue_single(lgx_lattice* lat) {
   sa.dm = lat->dm;
   sa.seed = lat->seed;
   sa.steps = lat->steps;
+  sa.words = lat->step_words ? lat->step_words
+             : (lat->step_mode == LGX_STEP_AUTO && lat->auto_resolved) ? lat->auto_words
+                                                                        : 0u;
   LGX_CUDA(lgx::launch_step(sa, lat->rest, lat->stream));
   lat->launches += 1;
   lat->cur ^= 1;
@@ -239,14 +242,17 @@ int resolve_auto(lgx_lattice* lat) {
     // the tuner could not run here (e.g. no room for its scratch lattice): the
     // reference's own launch pattern, one kernel per step
     cudaGetLastError();
-    p = lgx::StepPlan{LGX_STEP_SINGLE, 0, 0, 0, 0, 0};
+    p = lgx::StepPlan{LGX_STEP_SINGLE, 0, 0, 0, 0, 0, 0, 0, 0};
   }
   lat->auto_mode = p.mode;
   lat->auto_depth = p.depth;
+  lat->auto_words = p.words;
   lat->auto_us[0] = p.single_us;
-  lat->auto_us[1] = p.wave_us;
-  lat->auto_us[2] = p.temporal4_us;
-  lat->auto_us[3] = p.temporal8_us;
+  lat->auto_us[1] = p.single1_us;
+  lat->auto_us[2] = p.single2_us;
+  lat->auto_us[3] = p.wave_us;
+  lat->auto_us[4] = p.temporal4_us;
+  lat->auto_us[5] = p.temporal8_us;
   lat->auto_resolved = true;
   return LGX_OK;
 }
@@ -553,10 +559,13 @@ int lgx_get_step_plan(lgx_lattice* lat, lgx_step_plan* out) {
   if (rc) return rc;
   out->mode = lat->auto_mode;
   out->depth = lat->auto_depth;
+  out->words = lat->auto_words;
   out->single_us = lat->auto_us[0];
-  out->wave_us = lat->auto_us[1];
-  out->temporal4_us = lat->auto_us[2];
-  out->temporal8_us = lat->auto_us[3];
+  out->single1_us = lat->auto_us[1];
+  out->single2_us = lat->auto_us[2];
+  out->wave_us = lat->auto_us[3];
+  out->temporal4_us = lat->auto_us[4];
+  out->temporal8_us = lat->auto_us[5];
   return LGX_OK;
 }
 

@@ -114,6 +114,7 @@ extern "C" int lgx_step_planes_noalloc(const uint32_t* planes_in, uint32_t* plan
   sa.dm = dm;
   sa.seed = seed;
   sa.steps = steps;
+  sa.words = 0;
   e = lgx::launch_step(sa, rest_particles != 0, st);
   if (e != cudaSuccess) {
     lgx::set_error(std::string("lgx_step_planes_noalloc: ") + cudaGetErrorString(e));

@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(128) lgx_inlet_kernel(const InletArgs p) {
 
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
-  const bool two = s.dm.total >= kTwoChunkMinWords;
+  const bool two = s.words ? s.words == 2 : s.dm.total >= kTwoChunkMinWords;
   cfg.gridDim = dim3((s.dm.total + 255u) / 256u);
   cfg.blockDim = dim3(two ? 128 : 256);
   cfg.dynamicSmemBytes = 0;

@@ -25,6 +25,7 @@
 
 #include "../../include/lgx.h"
 #include "lgx_batch.hpp"
+#include "lgx_handle.hpp"
 #include "lgx_tune.hpp"
 
 namespace lgx {
@@ -195,9 +196,16 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
   lgx_lattice* t = nullptr;
   int rc = lgx_create(w, h, rest ? 1 : 0, 0x7E57ull, &t);
   if (rc) return rc;
-  StepPlan p{LGX_STEP_SINGLE, 0, 0, 0, 0, 0};
+  StepPlan p{LGX_STEP_SINGLE, 0, 1, 0, 0, 0, 0, 0, 0};
   const float est = time_mode(t, LGX_STEP_SINGLE, 0, 0);
-  p.single_us = time_mode(t, LGX_STEP_SINGLE, 0, est);
+  for (uint32_t words : {1u, 2u}) {  // the single-step kernel's two shapes
+    t->step_words = words;
+    const float us = time_mode(t, LGX_STEP_SINGLE, 0, est);
+    (words == 1 ? p.single1_us : p.single2_us) = us > 0 ? us : 0;
+  }
+  t->step_words = 0;
+  p.words = (p.single2_us > 0 && (p.single1_us <= 0 || p.single2_us < p.single1_us)) ? 2 : 1;
+  p.single_us = p.words == 2 ? p.single2_us : p.single1_us;
   const float w_us = time_mode(t, LGX_STEP_WAVE, 0, p.single_us);
   p.wave_us = w_us > 0 ? w_us : 0;
   if (wide) {

@@ -85,7 +85,8 @@ class BatchClass(C.Structure):
 
 class StepPlan(C.Structure):
     """lgx_step_plan: what LGX_STEP_AUTO resolves to and the tuner's times per step."""
-    _fields_ = [("mode", C.c_int), ("depth", C.c_uint32), ("single_us", C.c_float),
+    _fields_ = [("mode", C.c_int), ("depth", C.c_uint32), ("words", C.c_uint32),
+                ("single_us", C.c_float), ("single1_us", C.c_float), ("single2_us", C.c_float),
                 ("wave_us", C.c_float), ("temporal4_us", C.c_float),
                 ("temporal8_us", C.c_float)]
 

@@ -11,8 +11,9 @@ pytestmark = pytest.mark.gpu
 def test_auto_picks_the_fastest_timed_mode(LG, w, h):
     g = LG.GpuLattice(w, h, True, 3)
     p = g.step_plan
-    times = {1: p["single_us"], 2: p["wave_us"]}
-    assert p["single_us"] > 0
+    assert p["single1_us"] > 0 and p["single2_us"] > 0
+    assert p["single_us"] == min(p["single1_us"], p["single2_us"])
+    assert p["words"] == (1 if p["single_us"] == p["single1_us"] else 2)
     if (w + 31) // 32 >= 64:
         assert p["temporal4_us"] > 0 and p["temporal8_us"] > 0
     else:
