@@ -149,6 +149,7 @@ __global__ void lgx_batch_owner_kernel(const uint32_t* block0, uint32_t nlat, ui
 
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st) {
+  if (words == 0) words = nblocks >= 152u * 8u ? 2 : 1;  // two chunks once a wave is full
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
   cfg.blockDim = dim3(words == 2 ? 128 : 256);

@@ -83,11 +83,12 @@ cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize
 
 // The rule of the blocks a batched step launch covers.
 constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;
-// words: 32-word chunks per warp (1: 256-thread blocks, 2: 128-thread blocks);
-// a block covers 256 words either way.  Two chunks per warp give each thread
-// two independent word updates to interleave: +2% on the graph-replayed
-// transport sweep, but -14% on the served stream's host-launched ticks, so
-// the batch uses 2 and the server 1.
+// words: 32-word chunks per warp (1: 256-thread blocks, 2: 128-thread blocks;
+// 0: two once the launch fills a wave of 128-thread blocks, 152 x 8).  A block
+// covers 256 words either way.  Two chunks per warp give each thread two
+// independent word updates to interleave, which pays when the launch fills the
+// GPU (+2% on the transport sweep); below that a step is latency-bound and one
+// chunk, twice the threads, is faster.
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st);
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st);

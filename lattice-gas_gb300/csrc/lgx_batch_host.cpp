@@ -252,7 +252,7 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
       // rest-particle lattices' blocks first, then the six-direction ones
       lgx::BatchStepArgs sa{b->d_descs + sg.first, sg.d_block0, sg.d_owner, sg.count,
                             b->d_base, k, 0};
-      e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks), 2, st);
+      e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks), 0, st);
       if (e == cudaSuccess && b->hook && b->hook_per_step)
         e = b->hook(b->hook_ctx, st, b->d_base, k + 1);
     }

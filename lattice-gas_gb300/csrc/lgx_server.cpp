@@ -407,7 +407,7 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     size_t j = 0;
     for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
       lgx::BatchStepArgs sa{dd, d_block0, owner[c], (uint32_t)nc, s->d_zero, k, 0};
-      e = lgx::launch_batch_step(sa, nblocks[c], rule, 1, st);
+      e = lgx::launch_batch_step(sa, nblocks[c], rule, 0, st);
       s->launches += 1;
       if (e == cudaSuccess && j < m && pts[j] == k + 1) {
         const uint32_t* tb = blk + j * (nc + 1);

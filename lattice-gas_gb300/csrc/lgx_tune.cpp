@@ -122,7 +122,7 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   for (uint32_t k = 0; k < kTuneSteps && e == cudaSuccess; ++k) {
     BatchStepArgs sa{(const LatDesc*)descs, (const uint32_t*)block0, (const uint32_t*)owner, n,
                      (const uint64_t*)base, k, 0};
-    e = launch_batch_step(sa, b0[n], rule, 2, s.st);
+    e = launch_batch_step(sa, b0[n], rule, 0, s.st);
   }
   cudaError_t e2 = cudaStreamEndCapture(s.st, &graph);
   if (e == cudaSuccess) e = e2;
