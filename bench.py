@@ -46,17 +46,17 @@ def peaks():
     return 6800.0, "fallback"
 
 
-# From the ncu capture summarised in profiles/step_wake_run_pipes.md (the wake
-# run's lgx_step_kernel, one launch = one step): DRAM bytes read + written per
-# launch (cold cache under ncu; the 18 MB of planes stay in L2 between steps of
-# a timed run), and the ALU-pipe warp instructions per launch, which do not
-# depend on timing.
-STEP_TRAFFIC_BYTES = 8409344 + 0
-STEP_ALU_WARP_INSTR = 3400515
+# From the ncu metric capture summarised in profiles/step_wake_run_pipes.md
+# (the wake run's lgx_step_kernel, two chunks per warp, one launch = one step):
+# DRAM bytes read + written per launch (cold cache under ncu; the 18 MB of
+# planes stay in L2 between steps of a timed run), and the ALU-pipe warp
+# instructions per launch, which do not depend on timing.
+STEP_TRAFFIC_BYTES = 8419072 + 0
+STEP_ALU_WARP_INSTR = 3455811
 # Roofline-case DRAM bytes per site-update, from the 16384 x 8192 capture of the
-# same kernel (118.8 MB read + 73.4 MB written for 134.2 M sites); the full
+# same kernel (118.8 MB read + 72.7 MB written for 134.2 M sites); the full
 # 32768 x 16384 case scales with its sites.
-BIG_DRAM_BYTES_PER_SITE = (118771712 + 73354496) / (16384 * 8192)
+BIG_DRAM_BYTES_PER_SITE = (118769408 + 72740864) / (16384 * 8192)
 
 
 class ClockSampler:
