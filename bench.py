@@ -391,12 +391,28 @@ def bench_served(LG, W, n: int, budget: int):
         lat.append(srv.result(rid)["latency"])
     t_served = time.perf_counter() - t0
     st = srv.stats()
+
+    def digest(fields, sums, particles):
+        import hashlib
+        h = hashlib.blake2b(digest_size=16)
+        for a in list(fields) + list(sums):
+            h.update(np.ascontiguousarray(a).tobytes())
+        h.update(int(particles).to_bytes(8, "little"))
+        return h.hexdigest()
+
+    served_digest = []
+    for rid in ids:
+        res = srv.result(rid)
+        served_digest.append(digest((res["ux"], res["uy"], res["rho"], res["solid"]),
+                                    (res["mass"], res["px2"], res["py2"], res["nsolid"]),
+                                    res["particles"]))
     srv.close()
     # plain: each request alone, one lattice per launch, in arrival order
     clock = 0.0
     plain_lat = []
     busy = 0.0
-    for r in reqs:
+    same = 0
+    for r, sd in zip(reqs, served_digest):
         wl = r.work
         g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
         g.set_step_mode(1)
@@ -406,9 +422,10 @@ def bench_served(LG, W, n: int, budget: int):
         t1 = time.perf_counter()
         g.load(wl.cells)
         g.advance_sampling(wl.steps, wl.sample_every, wl.alpha)
-        g.read_field()
-        g.read_block_sums()
+        f = g.read_field()
+        sums = g.read_block_sums()
         svc = time.perf_counter() - t1
+        same += digest((f.ux, f.uy, f.rho, f.solid), sums, g.total_particles()) == sd
         g.close()
         busy += svc
         clock = max(clock, r.arrival) + svc
@@ -427,6 +444,7 @@ def bench_served(LG, W, n: int, budget: int):
             "plain_p99_latency_s": round(pct(plain_lat, 0.99), 4),
             "served_s": round(t_served, 3), "plain_s": round(clock, 3),
             "ticks": st["ticks"], "kernel_launches": st["kernel_launches"],
+            "bit_exact_vs_plain": "%d of %d requests" % (same, len(reqs)),
             "device_busy_s": round(st["gpu_busy_ns"] / 1e9, 4),
             "host_tick_s": round(st["host_tick_ns"] / 1e9, 4),
             "host_wait_s": round(st["host_wait_ns"] / 1e9, 4),
