@@ -269,12 +269,24 @@ def bench_batched(LG, W, steps: int):
     t_batch = b.timing_elapsed(0, 1) / 1e3
     k1, g1 = b.launches
     same = all(np.array_equal(x.store(), y.store()) for x, y in zip(plain, together))
+    # end to end through the public API: every lattice loaded from host memory,
+    # the batch run, every field read back
+    t0 = time.perf_counter()
+    for g, wl in zip(together, wls):
+        g.restart(wl.cells, wl.seed)
+    b.advance_sampling(steps, 50, 1.0)
+    for g in together:
+        g.read_field()
+    t_e2e = time.perf_counter() - t0
     out = {"workload": "transport sweep: 64 shear-wave lattices 256..2048 x 256..1024, "
                        "%d steps, 16x16 blocks every 50" % steps,
            "sites": sites, "value": round(sites * steps / t_batch / 1e9, 2),
            "plain_value": round(sites * steps / t_plain / 1e9, 2),
            "speedup_vs_plain": round(t_plain / t_batch, 2), "unit": UNIT,
            "batched_s": round(t_batch, 4), "plain_s": round(t_plain, 4),
+           "e2e_value": round(sites * steps / t_e2e / 1e9, 2),
+           "e2e_note": "host cells in, fields out, through GpuLattice.restart / Batch / "
+                       "read_field; the plain figure is host-timed the same way",
            "kernel_launches": k1 - k0, "graph_launches": g1 - g0,
            "bit_exact_vs_plain": bool(same),
            "size_classes": [{k: (round(v, 2) if isinstance(v, float) else v)
