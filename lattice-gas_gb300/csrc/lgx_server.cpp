@@ -152,7 +152,7 @@ void release_device(lgx_server* s, Req* r) {
 }
 
 // Allocate and load one request; false (with r->error) on failure.  Runs on
-// the server thread without the lock; `inject` is the test hook's verdict.
+// the server thread without the lock; `inject` is the test hook's decision.
 bool admit(lgx_server* s, Req* r, bool inject) {
   const lgx_request& q = r->spec;
   r->dm = lgx::make_dims((uint32_t)q.w, (uint32_t)q.h, (uint32_t)q.inlet_cols);

@@ -10,7 +10,7 @@
  *   src/moments.rs   packed integer moments (FLUID / WITH_WALLS)
  *   src/render.rs    Field::sample (coarse-graining)
  *   tests/golden.rs  FNV-1a
- * The checker for the CUDA engine; the product never calls it.
+ * The oracle the CUDA engine is tested against; the product never calls it.
  */
 #include "lg_oracle.h"
 

@@ -1,8 +1,8 @@
 /*
  * lg_oracle.h -- CPU oracle for the FHP lattice gas (TEST INFRASTRUCTURE ONLY).
  *
- * This is a plain-C restatement of the reference (daleobrien/lattice-gas) used
- * as the checker for the CUDA engine.  Nothing in the product library links or
+ * This is a plain-C restatement of the reference (daleobrien/lattice-gas) that
+ * the CUDA engine is tested against.  Nothing in the product library links or
  * calls it; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
  * leg load it.
  *
