@@ -10,7 +10,7 @@
  *
  * The collision is NOT the generated circuit: it is the class rule the
  * reference's known-answer test states (gpu.rs:799-817), evaluated lane by
- * lane from the class enumeration.  That keeps this checker independent of
+ * lane from the class enumeration.  That keeps this oracle independent of
  * the circuit generator it checks.
  */
 #include "lg_oracle.h"
