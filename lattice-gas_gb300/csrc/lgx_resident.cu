@@ -19,6 +19,8 @@
 // launch; clusters the GPU cannot hold at once run when others finish.
 #include <cooperative_groups.h>
 
+#include <mutex>
+
 #include "lgx_batch.hpp"
 #include "lgx_step_impl.cuh"
 
@@ -108,36 +110,56 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
       if (yy - y0 < y1 - y0) return shm + off + (size_t)(yy - y0) * dm.wpr;
       return (yy == ya ? up_base : down_base) + off;
     };
-    for (uint32_t c = warp; c < nch; c += nwarps) {
-      uint32_t lw;
-      bool live;
-      word_of(c, &lw, &live);
-      const uint32_t yr = div_wpr(lw), j = lw - yr * dm.wpr, y = y0 + yr;
-      const uint32_t g = y * dm.wpr + j;
-      const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
-      const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
-      const uint32_t* rows[7] = {row(0, y), row(1, ym), row(2, ym), row(3, y),
-                                 row(4, yp), row(5, yp), row(6, y)};
-      uint32_t* out = shm + db * lbs + (size_t)yr * dm.wpr + j;
-      const Draws s = c == warp ? first : draws(g ^ seed32);
-      if (d.rest)
-        step_core<true, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, s, g, y, j,
-                                    live);
-      else
-        step_core<false, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, s, g, y, j,
-                                     live);
+    // one CTA holds the whole lattice: every row is in this CTA's shared
+    // memory, addressed from `shm` so that the loads compile to shared loads
+    auto own = [&](uint32_t q, uint32_t yy) -> const uint32_t* {
+      return shm + sb * lbs + q * lps + (size_t)yy * dm.wpr;
+    };
+    auto step_chunks = [&](auto&& rowf) {
+      for (uint32_t c = warp; c < nch; c += nwarps) {
+        uint32_t lw;
+        bool live;
+        word_of(c, &lw, &live);
+        const uint32_t yr = div_wpr(lw), j = lw - yr * dm.wpr, y = y0 + yr;
+        const uint32_t g = y * dm.wpr + j;
+        const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
+        const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
+        const uint32_t* rows[7] = {rowf(0, y),  rowf(1, ym), rowf(2, ym), rowf(3, y),
+                                   rowf(4, yp), rowf(5, yp), rowf(6, y)};
+        uint32_t* out = shm + db * lbs + (size_t)yr * dm.wpr + j;
+        const Draws s = c == warp ? first : draws(g ^ seed32);
+        if (d.rest)
+          step_core<true, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, s, g, y,
+                                      j, live);
+        else
+          step_core<false, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, s, g, y,
+                                       j, live);
+      }
+    };
+    if (C == 1u)
+      step_chunks(own);
+    else
+      step_chunks(row);
+    if (C == 1u) {
+      // the whole lattice in this CTA: a block barrier orders its shared memory
+      __syncthreads();
+      if (k + 1u < p.len) first = draws(g0 ^ step_seed32(d.seed, d.steps0 + local + 1u));
+    } else {
+      // arrive (shared-memory stores released at cluster scope), draw ahead, wait
+      asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+      if (k + 1u < p.len) first = draws(g0 ^ step_seed32(d.seed, d.steps0 + local + 1u));
+      asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
-    // arrive (shared-memory stores released at cluster scope), draw ahead, wait
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    if (k + 1u < p.len) first = draws(g0 ^ step_seed32(d.seed, d.steps0 + local + 1u));
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     // sampling point after step k + 1 of this launch: from global memory
     const uint32_t t = k + 1u;
     const bool due = nb && sch.every && ((sch.since + t) % sch.every == 0u || t == sch.left);
     if (due) {
       const uint32_t par = (d.cur0 + (uint32_t)(local + 1u)) & 1u;
       store_band(db, par);
-      cluster.sync();
+      if (C == 1u)
+        __syncthreads();
+      else
+        cluster.sync();
       SampleArgs sa;
       sa.a = par ? d.planes[1] : d.planes[0];
       sa.solid = d.solid;
@@ -159,16 +181,38 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
   store_band(p.len & 1u, (d.cur0 + (uint32_t)(base + p.len)) & 1u);
 }
 
+// The kernel attributes a launch needs (16-CTA clusters are an opt-in; dynamic
+// shared memory above 48 KB too), set once per device and kernel: setting them
+// costs host time on every launch otherwise.
+template <int THREADS>
+cudaError_t ensure_attributes(size_t smem) {
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static size_t smem_set[kMaxDev] = {};
+  static bool wide_set[kMaxDev] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDev) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(mu);
+  if (!wide_set[dev]) {
+    e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    wide_set[dev] = true;
+  }
+  if (smem > smem_set[dev]) {
+    e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResidentMaxSmem);
+    if (e != cudaSuccess) return e;
+    smem_set[dev] = kResidentMaxSmem;
+  }
+  return cudaSuccess;
+}
+
 template <int THREADS>
 cudaError_t launch_resident_t(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
                               size_t smem, cudaStream_t st) {
-  if (csize > 8) {  // 16-CTA clusters are an opt-in per kernel (and device)
-    cudaError_t e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
-                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-  }
-  cudaError_t e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_attributes<THREADS>(smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nlat * csize);

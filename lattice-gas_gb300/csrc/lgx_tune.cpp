@@ -32,6 +32,7 @@ namespace lgx {
 namespace {
 
 constexpr uint32_t kTuneSteps = 48;
+constexpr uint32_t kResidentTuneSteps = 128;  // the longest interval a batch launches
 constexpr size_t kTuneMaxWords = 4u << 20;  // per-plane words of all synthetic lattices
 
 std::mutex g_mu;
@@ -144,11 +145,13 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
       const uint32_t warps = cs * th / 32;
       if (warps > nchunks || warps * 16 < nchunks || !resident_fits(dm, cs)) continue;
       float us = 0;
+      // one launch of a full interval, as the batch runs it
       ResidentArgs ra{(const LatDesc*)descs, (const ResSched*)sched, 0, (const uint64_t*)base,
-                      kTuneSteps};
+                      kResidentTuneSteps};
       const size_t smem = resident_smem_bytes(dm, cs);
       cudaError_t r =
           time_it([&]() { return launch_resident(ra, n, cs, th, smem, s.st); }, &us);
+      us *= (float)kTuneSteps / (float)kResidentTuneSteps;
       if (r != cudaSuccess) {
         cudaGetLastError();  // a cluster shape this device cannot place: skip it
         continue;

@@ -7,7 +7,8 @@ Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
 `sweep` (the 64-lattice transport sweep as one batch), `transport` (one
 transport::measure at --size, density 0.22), `fill` (init_equilibrium on the
-device over the roofline case's geometry at 16384 x 8192).  --policy picks the sweep's batch
+device over the roofline case's geometry at 16384 x 8192), `tiny` (eight --size x
+--size lattices as one batch).  --policy picks the sweep's batch
 policy (under a profiler pass 1: the tuner's timings are not meaningful there, and
 without one it picks one launch per step for every class of this sweep).  --mode
 picks the step
@@ -26,7 +27,7 @@ from lattice_gas import workloads as W  # noqa: E402
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="wake",
-                    choices=["wake", "big", "sweep", "transport", "fill"])
+                    choices=["wake", "big", "sweep", "transport", "fill", "tiny"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--policy", type=int, default=0,
                     help="batch policy for the sweep: 0 tuned, 1 one launch per step, 2 resident")
@@ -34,6 +35,13 @@ def main():
     ap.add_argument("--mode", type=int, default=1)
     ap.add_argument("--depth", type=int, default=4)
     a = ap.parse_args()
+    if a.case == "tiny":
+        # --size x --size lattices (8 of them) as one batch under --policy
+        lats = [LG.GpuLattice(a.size, a.size, True, i) for i in range(8)]
+        b = LG.Batch(lats, a.policy)
+        b.advance(a.steps)
+        print("tiny: 8 x %d^2, %d steps, policy %d, plan %s" % (a.size, a.steps, a.policy, b.plan))
+        return
     if a.case == "fill":
         wl = W.roofline_case(w=16384, h=8192, n_circles=50)
         g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
