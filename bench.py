@@ -374,6 +374,33 @@ def bench_transport(LG, cpu: bool):
     return out
 
 
+def bench_byte_path(LG, W, steps: int, cpu_rate):
+    """The reference's own CPU update (byte per cell, its random stream, bands of
+    ceil(h / threads) rows, src/lattice.rs:222-364) run on the device on the wake
+    run, 16 bands as the reference on 16 host threads: the path whose golden
+    checksums (tests/golden.rs) the device reproduces.  Beside it the same update
+    on the host cores (the CPU baseline of this line)."""
+    wl = W.wake_run(steps=steps)
+    lat = LG.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
+    lat.load(wl.cells)
+    lat.advance(50)
+    t0 = time.perf_counter()
+    lat.advance(steps)
+    lat.store()
+    dt = time.perf_counter() - t0
+    out = {"workload": "wake run 4096x2304, byte-per-cell update with the reference's random "
+                       "stream, 16 bands, %d steps" % steps,
+           "value": round(wl.sites * steps / dt / 1e9, 2), "unit": UNIT,
+           "note": "the parity path: each band's draws come from one serial generator, so "
+                   "every 128-cell segment jumps its band's state ahead and walks its cells "
+                   "in order; the bitplane step is the throughput path"}
+    if cpu_rate:
+        out["cpu_reference"] = round(cpu_rate / 1e9, 4)
+        out["speedup_vs_cpu"] = round(wl.sites * steps / dt / cpu_rate, 1)
+    lat.close()
+    return out
+
+
 def bench_served(LG, W, n: int, budget: int):
     """The request stream: Poisson arrivals at 200/s, sizes 128x128..4096x2048,
     1k..50k steps, sampling every 50..500 steps with 8..32 blocks, obstacle none
@@ -553,12 +580,13 @@ def run_gb300(args, world, rank, local):
                                      "update (GpuLattice's shader) restated in C, %d threads"
                                      % (bsteps, bdt, threads)}
 
-    batched = served = big = transport = None
+    batched = served = big = transport = byte_path = None
     if not args.no_patterns:
         batched = bench_batched(LG, W, args.sweep_steps)
         served = bench_served(LG, W, args.requests, args.budget_mib << 20)
         big = bench_roofline_case(LG, W, args.big_steps)
         transport = bench_transport(LG, rank == 0 and world == 1 and not args.no_cpu)
+        byte_path = bench_byte_path(LG, W, 2000, rate if cpu else None)
     lop3_peak = LG.probe_int_rate(0)
     alu_achieved = STEP_ALU_WARP_INSTR * 32 / (step_ms * 1e-3)
 
@@ -599,6 +627,7 @@ def run_gb300(args, world, rank, local):
         "served": served,
         "roofline_case": big,
         "transport": transport,
+        "byte_path": byte_path,
         "device": g.device_name(),
     }
     print(json.dumps(line), flush=True)
