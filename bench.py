@@ -384,16 +384,19 @@ def bench_byte_path(LG, W, steps: int, cpu_rate):
     lat = LG.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
     lat.load(wl.cells)
     lat.advance(50)
-    t0 = time.perf_counter()
-    lat.advance(steps)
-    lat.store()
-    dt = time.perf_counter() - t0
+    dt = float("inf")
+    for _ in range(3):
+        t0 = time.perf_counter()
+        lat.advance(steps)
+        lat.store()
+        dt = min(dt, time.perf_counter() - t0)
     out = {"workload": "wake run 4096x2304, byte-per-cell update with the reference's random "
-                       "stream, 16 bands, %d steps" % steps,
+                       "stream, 16 bands, %d steps and a read-back, best of 3" % steps,
            "value": round(wl.sites * steps / dt / 1e9, 2), "unit": UNIT,
            "note": "the parity path: each band's draws come from one serial generator, so "
-                   "every 128-cell segment jumps its band's state ahead and walks its cells "
-                   "in order; the bitplane step is the throughput path"}
+                   "every 64-cell segment jumps its band's state ahead (a jump polynomial) "
+                   "and walks its cells in order, one xorshift64* step per cell; the "
+                   "bitplane step is the throughput path"}
     if cpu_rate:
         out["cpu_reference"] = round(cpu_rate / 1e9, 4)
         out["speedup_vs_cpu"] = round(wl.sites * steps / dt / cpu_rate, 1)
@@ -586,7 +589,7 @@ def run_gb300(args, world, rank, local):
         served = bench_served(LG, W, args.requests, args.budget_mib << 20)
         big = bench_roofline_case(LG, W, args.big_steps)
         transport = bench_transport(LG, rank == 0 and world == 1 and not args.no_cpu)
-        byte_path = bench_byte_path(LG, W, 2000, rate if cpu else None)
+        byte_path = bench_byte_path(LG, W, 1000, rate if cpu else None)
     lop3_peak = LG.probe_int_rate(0)
     alu_achieved = STEP_ALU_WARP_INSTR * 32 / (step_ms * 1e-3)
 

@@ -8,14 +8,31 @@
 // serial generator (src/lattice.rs:270-285).  Its golden tests pin that stream
 // bit for bit.  This file runs the same stream on the device.
 //
-// The draws are sequential within a band, so a thread takes a segment of one
-// row and first jumps the band's generator to the segment's draw index.  The
-// generator's state update is linear over GF(2), x -> M x, so k steps are M^k x;
-// with the 32 matrices M^(2^i) (columns precomputed on the host) a jump is at
-// most 32 matrix-vector products.  The draw index of every segment is fixed:
-// it counts the non-obstacle cells of the band before the segment, and
-// obstacles never move, so those offsets are computed once when cells are
-// loaded.  The inflow is the same with one stream and 3 or 4 draws per cell.
+// The draws are sequential within a band, so a thread takes a 64-cell segment
+// of one row and first jumps the band's generator to the segment's draw index.
+// That index counts the band's non-obstacle cells before the segment, and
+// obstacles never move, so it is fixed when cells are loaded; the host stores
+// it as the jump polynomial z^k mod P (lgx_rng.cuh), and each block folds the
+// first 64 states of its bands' generators into tables over 4-bit chunks of
+// the polynomial, so a jump is 16 shared-memory lookups.
+//
+// A block stages a tile of rows (rows y0-1 .. y0+R) in shared memory with
+// asynchronous copies, all in flight at once; each segment sits in its own
+// 80-byte slot (15 pad bytes, the left halo byte, 64 cells; the right halo is
+// the byte after the cells).  Five 16-byte chunks per slot is an odd count, so
+// the lanes of a warp, one segment each, read their 16-byte chunks from
+// distinct banks.  A thread walks its segment 16 cells at a time: one chunk per
+// row, the neighbours by funnel shifts, the six arrival bits gathered for four
+// cells at once.  Results go to a padded output tile and out with coalesced
+// stores.
+//
+// The inflow re-seed after the step (src/lattice.rs:270-285) draws from one
+// serial stream, 3 or 4 draws per non-obstacle cell of the leftmost columns,
+// and depends only on that stream and the obstacles, so it is fused: every
+// inflow cell has its own jump polynomial, the host passes the stream's first
+// 64 states with the launch, and the block's threads draw the tile's inflow
+// cells while its rows are in flight, into the output tile, where the
+// collision results leave them be.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -32,110 +49,323 @@
 
 namespace {
 
-using lgx::jump_ahead;
+using lgx::jump_entry;
+using lgx::jump_poly;
 using lgx::rng_seed;
 using lgx::xorshift;
 
-constexpr uint32_t kSeg = 128;     // cells per thread segment
-constexpr int kJumps = 32;         // the first 32 jump matrices: offsets below 2^32
+constexpr uint32_t kSeg = 64;             // cells per thread segment
+constexpr uint32_t kThreads = 256;        // largest block
+constexpr uint32_t kMaxRows = 8;          // rows per tile
+constexpr uint32_t kSlot = kSeg + 16;     // input slot: 15 pad bytes, left halo, cells
+constexpr uint32_t kOutPitch = kSeg + 4;  // output slot: 17 words
+constexpr uint32_t kMaxStride = 30;       // outcomes per state in the padded table
+constexpr uint32_t kLutBytes = 128 * kMaxStride;
+static_assert((kSlot / 16) % 2 == 1 && (kOutPitch / 4) % 2 == 1, "odd pitches");
+static_assert(kLutBytes % 16 == 0, "tile alignment");
 constexpr uint8_t kSolid = 0x80, kRest = 0x40;
 constexpr uint64_t kMul = lgx::kRngMul;
+constexpr int kChunk = 4;                            // bits per jump-table chunk
+constexpr uint32_t kTab = (64 / kChunk) << kChunk;  // entries per generator's table
 
 struct ByteStepArgs {
   const uint8_t* old;
   uint8_t* out;
-  const uint8_t* table;  // n_states * stride outcomes
+  const uint8_t* table;  // 128 * stride outcomes
   uint32_t stride;
-  uint32_t w, h, band;  // band: rows per generator
-  uint32_t segs_per_row;
-  const uint32_t* seg_off;  // draw index of each segment within its band
-  const uint64_t* jump;
-  uint64_t base_seed;       // seed ^ steps * 0x9E3779B97F4A7C15
-};
-
-struct ByteInletArgs {
-  uint8_t* cells;
-  uint32_t w, h, cols;
-  const uint32_t* row_off;  // draws before row y
-  const uint64_t* jump;
-  uint64_t seed;            // seed ^ steps * 0xD1B54A32D192ED03 (steps after the step)
+  uint32_t w, h, band;   // band: rows per generator
+  uint32_t segs;         // segments per row
+  uint32_t cols, rows;   // tile: segments and rows
+  uint32_t tiles_c;      // tiles across a row
+  uint32_t nbands;       // band tables per block
+  const uint64_t* poly;  // per segment: z^k mod P, k its first draw within the band
+  uint64_t base_seed;    // seed ^ steps * 0x9E3779B97F4A7C15
+  // the inflow re-seed
+  uint32_t inlet_cols;
+  const uint64_t* inlet_poly;  // per row and inflow column: z^k mod P, k the draws before it
   uint32_t t[7];
   int rest;
+  uint64_t inlet_states[64];  // the stream's first 64 states (seed ^ steps after the step
+                              // * 0xD1B54A32D192ED03)
 };
 
-// One row segment of the fused propagate-then-collide gather
-// (src/lattice.rs:324-364).
-__global__ void __launch_bounds__(128) lgx_byte_step_kernel(const ByteStepArgs p) {
-  __shared__ uint64_t jump[kJumps * 64];
-  __shared__ uint8_t table[128 * 30];
-  for (uint32_t i = threadIdx.x; i < kJumps * 64; i += blockDim.x) jump[i] = p.jump[i];
-  const uint32_t tsize = 128u * p.stride;
-  for (uint32_t i = threadIdx.x; i < tsize; i += blockDim.x) table[i] = p.table[i];
-  __syncthreads();
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= p.h * p.segs_per_row) return;
-  const uint32_t y = s / p.segs_per_row;
-  const uint32_t x0 = (s - y * p.segs_per_row) * kSeg;
-  const uint32_t x1 = min(x0 + kSeg, p.w);
-  const uint32_t b = y / p.band;
-  uint64_t st = jump_ahead(rng_seed(p.base_seed ^ ((uint64_t)(b + 1) << 32)), p.seg_off[s], jump);
+__host__ __device__ __forceinline__ uint32_t in_row_bytes(uint32_t cols) {
+  return cols * kSlot + 16;
+}
 
-  // Column offsets to the neighbour a particle arrives from: direction d takes
-  // from the neighbour in the opposite direction (src/hex.rs:36-41).
-  const bool odd = y & 1u;
-  const int DXE[6] = {1, 0, -1, -1, -1, 0};
-  const int DXO[6] = {1, 1, 0, -1, 0, 1};
-  const int DY[6] = {0, 1, 1, 0, -1, -1};
-  const int OPP[6] = {3, 4, 5, 0, 1, 2};
-  int sdx[6];
-  const uint8_t* srow[6];
-  for (int d = 0; d < 6; ++d) {
-    const int bk = OPP[d];
-    sdx[d] = odd ? DXO[bk] : DXE[bk];
-    int sy = (int)y + DY[bk];
-    if (sy < 0) sy += (int)p.h;
-    if (sy >= (int)p.h) sy -= (int)p.h;
-    srow[d] = p.old + (size_t)sy * p.w;
+// Band tables, the band generators' states, the collision table, the input
+// tile, the output tile.
+size_t step_smem_bytes(uint32_t cols, uint32_t rows, uint32_t nbands) {
+  return (size_t)nbands * (kTab + 64) * 8 + kLutBytes + (size_t)(rows + 2) * in_row_bytes(cols) +
+         ((size_t)rows * cols * kOutPitch + 15) / 16 * 16;
+}
+
+// Row y - 1 of the lattice, periodic, for y in 0 .. h + 1.
+__device__ __forceinline__ uint32_t wrap_row(uint32_t y, uint32_t h) {
+  return y == 0 ? h - 1 : (y - 1 >= h ? y - 1 - h : y - 1);
+}
+
+__device__ __forceinline__ uint32_t lds32(const uint8_t* p) {
+  return *reinterpret_cast<const uint32_t*>(p);
+}
+
+__device__ __forceinline__ uint4 lds128(const uint8_t* p) {
+  return *reinterpret_cast<const uint4*>(p);
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Four cells of row y from the words of rows y-1 (u), y (m) and y+1 (d) at
+// their columns, with the words on either side (p, n).  Direction d arrives
+// from the neighbour in the opposite direction (src/hex.rs:36-41): bit 0 from
+// (x-1, y), bit 3 from (x+1, y); from row y-1 bits 1 and 2, from row y+1 bits
+// 5 and 4, at columns (x-1, x) on even rows and (x, x+1) on odd rows.  Then
+// bounce-back on obstacles, and on other cells the padded table's outcome for
+// one draw of the band's generator (src/lattice.rs:324-364).
+template <bool ODD>
+__device__ __forceinline__ uint32_t gather4(uint32_t pu, uint32_t wu, uint32_t nu, uint32_t pm,
+                                            uint32_t wm, uint32_t nm, uint32_t pd, uint32_t wd,
+                                            uint32_t nd) {
+  uint32_t a = (__funnelshift_l(pm, wm, 8) & 0x01010101u) |
+               (__funnelshift_r(wm, nm, 8) & 0x08080808u) | (wm & 0x40404040u);
+  if (ODD)
+    a |= (wu & 0x02020202u) | (__funnelshift_r(wu, nu, 8) & 0x04040404u) |
+         (__funnelshift_r(wd, nd, 8) & 0x10101010u) | (wd & 0x20202020u);
+  else
+    a |= (__funnelshift_l(pu, wu, 8) & 0x02020202u) | (wu & 0x04040404u) |
+         (wd & 0x10101010u) | (__funnelshift_l(pd, wd, 8) & 0x20202020u);
+  return a;
+}
+
+// The state of cell B of four (bit 7 of each byte of `a` is clear).
+template <int B>
+__device__ __forceinline__ uint32_t state_byte(uint32_t a) {
+  return a >> (8 * B) & 0xFFu;
+}
+
+__device__ __forceinline__ uint32_t draw_k(uint64_t& st, uint32_t stride) {
+  st = xorshift(st);
+  return __umulhi((uint32_t)((st * kMul) >> 32), stride);
+}
+
+template <int B>
+__device__ __forceinline__ uint32_t cell_out(uint32_t a, uint32_t wm, uint32_t bounce, uint64_t& st,
+                                             const uint8_t* lut, uint32_t stride) {
+  if (wm >> (8 * B + 7) & 1u) return bounce >> (8 * B) & 0xFFu;
+  const uint32_t k = draw_k(st, stride);
+  return lut[state_byte<B>(a) * stride + k];
+}
+
+__device__ __forceinline__ uint32_t bounce4(uint32_t a) {
+  // the six moving bits turned by half a circle
+  const uint32_t m = a & 0x3F3F3F3Fu;
+  return 0x80808080u | (a & 0x40404040u) | ((m << 3) & 0x38383838u) | ((m >> 3) & 0x07070707u);
+}
+
+template <bool ODD>
+__device__ __forceinline__ uint32_t step4(uint32_t pu, uint32_t wu, uint32_t nu, uint32_t pm,
+                                          uint32_t wm, uint32_t nm, uint32_t pd, uint32_t wd,
+                                          uint32_t nd, uint64_t& st, const uint8_t* lut,
+                                          uint32_t stride) {
+  const uint32_t a = gather4<ODD>(pu, wu, nu, pm, wm, nm, pd, wd, nd);
+  if (!(wm & 0x80808080u)) {
+    uint32_t res = 0;
+    uint32_t k;
+    k = draw_k(st, stride);
+    res = lut[state_byte<0>(a) * stride + k];
+    k = draw_k(st, stride);
+    res |= (uint32_t)lut[state_byte<1>(a) * stride + k] << 8;
+    k = draw_k(st, stride);
+    res |= (uint32_t)lut[state_byte<2>(a) * stride + k] << 16;
+    k = draw_k(st, stride);
+    res |= (uint32_t)lut[state_byte<3>(a) * stride + k] << 24;
+    return res;
   }
-  const uint8_t* row = p.old + (size_t)y * p.w;
-  uint8_t* orow = p.out + (size_t)y * p.w;
-  for (uint32_t x = x0; x < x1; ++x) {
-    const uint8_t here = __ldg(row + x);
-    uint8_t state = here & kRest;
-    for (int d = 0; d < 6; ++d) {
-      int sx = (int)x + sdx[d];
-      if (sx < 0) sx += (int)p.w;
-      if (sx >= (int)p.w) sx -= (int)p.w;
-      state |= __ldg(srow[d] + sx) & (uint8_t)(1u << d);
-    }
-    uint8_t o;
-    if (here & kSolid) {
-      const uint8_t m = state & 0x3F;
-      o = kSolid | (state & kRest) | (uint8_t)(((m << 3) | (m >> 3)) & 0x3F);
+  const uint32_t bo = bounce4(a);
+  return cell_out<0>(a, wm, bo, st, lut, stride) | cell_out<1>(a, wm, bo, st, lut, stride) << 8 |
+         cell_out<2>(a, wm, bo, st, lut, stride) << 16 | cell_out<3>(a, wm, bo, st, lut, stride) << 24;
+}
+
+// The staged word for cells x .. x+3 of a segment: the collision results,
+// except on non-obstacle inflow cells, whose sample is already staged.
+__device__ __forceinline__ void put4(uint32_t* dst, uint32_t res, uint32_t x, uint32_t wm,
+                                     uint32_t inlet_cols) {
+  if (x < inlet_cols) {
+    const uint32_t n = inlet_cols - x;
+    uint32_t keep = ((~wm & 0x80808080u) >> 7) * 0xFFu;
+    if (n < 4) keep &= (1u << (8 * n)) - 1;
+    res = (res & ~keep) | (*dst & keep);
+  }
+  *dst = res;
+}
+
+// One thread's segment: `len` cells of row y, 16 at a time, from the input
+// slots of rows y-1, y, y+1 into its output slot.
+template <bool ODD>
+__device__ __forceinline__ void walk(const uint8_t* up, const uint8_t* mid, const uint8_t* dn,
+                                     uint8_t* o, uint32_t first, uint32_t len, uint64_t st,
+                                     const uint8_t* lut, uint32_t stride, uint32_t inlet_cols) {
+  uint32_t pu = lds32(up + 12), pm = lds32(mid + 12), pd = lds32(dn + 12);
+  uint4 cu = lds128(up + 16), cm = lds128(mid + 16), cd = lds128(dn + 16);
+  for (uint32_t g = 0; g < len; g += 16) {
+    const uint4 xu = lds128(up + 32 + g), xm = lds128(mid + 32 + g), xd = lds128(dn + 32 + g);
+    uint32_t* og = reinterpret_cast<uint32_t*>(o + g);
+    const uint32_t r0 = step4<ODD>(pu, cu.x, cu.y, pm, cm.x, cm.y, pd, cd.x, cd.y, st, lut, stride);
+    const uint32_t r1 = step4<ODD>(cu.x, cu.y, cu.z, cm.x, cm.y, cm.z, cd.x, cd.y, cd.z, st, lut, stride);
+    const uint32_t r2 = step4<ODD>(cu.y, cu.z, cu.w, cm.y, cm.z, cm.w, cd.y, cd.z, cd.w, st, lut, stride);
+    const uint32_t r3 = step4<ODD>(cu.z, cu.w, xu.x, cm.z, cm.w, xm.x, cd.z, cd.w, xd.x, st, lut, stride);
+    if (first + g < inlet_cols) {
+      put4(og, r0, first + g, cm.x, inlet_cols);
+      put4(og + 1, r1, first + g + 4, cm.y, inlet_cols);
+      put4(og + 2, r2, first + g + 8, cm.z, inlet_cols);
+      put4(og + 3, r3, first + g + 12, cm.w, inlet_cols);
     } else {
-      st = xorshift(st);
-      const uint32_t r = (uint32_t)((st * kMul) >> 32);
-      const uint32_t k = (uint32_t)(((uint64_t)r * p.stride) >> 32);
-      o = table[state * p.stride + k];
+      og[0] = r0;
+      og[1] = r1;
+      og[2] = r2;
+      og[3] = r3;
     }
-    orow[x] = o;
+    pu = cu.w;
+    pm = cm.w;
+    pd = cd.w;
+    cu = xu;
+    cm = xm;
+    cd = xd;
   }
 }
 
-// The inflow re-seed of the leftmost columns, one thread per row, each
-// jumping the step's single generator to the row's first draw
-// (src/lattice.rs:270-285, Equilibrium::sample at src/lattice.rs:102-115).
-__global__ void __launch_bounds__(128) lgx_byte_inlet_kernel(const ByteInletArgs p) {
-  __shared__ uint64_t jump[kJumps * 64];
-  for (uint32_t i = threadIdx.x; i < kJumps * 64; i += blockDim.x) jump[i] = p.jump[i];
+__global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_constant__ ByteStepArgs p) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  const uint32_t tc = blockIdx.x % p.tiles_c, tr = blockIdx.x / p.tiles_c;
+  const uint32_t y0 = tr * p.rows;
+  const uint32_t R = min(p.rows, p.h - y0);
+  const uint32_t s0 = tc * p.cols;
+  const uint32_t C = min(p.cols, p.segs - s0);
+  const uint32_t c0 = s0 * kSeg;
+  const uint32_t ncols = min(C * kSeg, p.w - c0);
+  const uint32_t b0 = y0 / p.band, nb = (y0 + R - 1) / p.band - b0 + 1;
+  const uint32_t RB = C * kSlot + 16;  // input row bytes
+
+  uint64_t* tab = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* states = tab + p.nbands * kTab;
+  uint8_t* lut = reinterpret_cast<uint8_t*>(states + p.nbands * 64);
+  uint8_t* in = lut + kLutBytes;
+  uint8_t* out = in + (p.rows + 2) * in_row_bytes(p.cols);
+
+  // rows y0-1 .. y0+R of the tile's columns, and the collision table, in flight together
+  const uint32_t in_rows = R + 2;
+  for (uint32_t r = 0; r < in_rows; ++r) {
+    const uint32_t gy = wrap_row(y0 + r, p.h);
+    const uint8_t* row = p.old + (size_t)gy * p.w + c0;
+    uint8_t* dst = in + r * RB + 16;
+    if ((p.w & 15u) == 0) {
+      for (uint32_t k = tid; k < (ncols >> 4); k += nt)
+        cp_async16(dst + (k >> 2) * kSlot + (k & 3u) * 16, row + k * 16);
+    } else if ((p.w & 3u) == 0) {
+      for (uint32_t k = tid; k < (ncols >> 2); k += nt)
+        cp_async4(dst + (k >> 4) * kSlot + (k & 15u) * 4, row + k * 4);
+    } else {
+      for (uint32_t x = tid; x < ncols; x += nt) dst[(x / kSeg) * kSlot + x % kSeg] = __ldg(row + x);
+    }
+  }
+  // halo bytes at the tile's two edges when it is narrower than a row (the
+  // others are copied from neighbouring slots once the tile has landed)
+  const uint32_t len_last = ncols - (C - 1) * kSeg;
+  if (p.tiles_c > 1) {
+    for (uint32_t i = tid; i < in_rows * 2; i += nt) {
+      const uint32_t r = i >> 1, gy = wrap_row(y0 + r, p.h);
+      const uint8_t* row = p.old + (size_t)gy * p.w;
+      if (i & 1u)
+        in[r * RB + (C - 1) * kSlot + 16 + len_last] = __ldg(row + (c0 + ncols == p.w ? 0 : c0 + ncols));
+      else
+        in[r * RB + 15] = __ldg(row + (c0 ? c0 - 1 : p.w - 1));
+    }
+  }
+  for (uint32_t i = tid; i < 32u * p.stride; i += nt) cp_async4(lut + i * 4, p.table + i * 4);
+  // the first 64 states of each band's generator
+  if (tid < nb) {
+    uint64_t x = rng_seed(p.base_seed ^ ((uint64_t)(b0 + tid + 1) << 32));
+    for (int j = 0; j < 64; ++j) {
+      states[tid * 64 + j] = x;
+      x = xorshift(x);
+    }
+  }
+  // the inflow cells of the tile, into the output tile
+  if (c0 < p.inlet_cols) {
+    const uint32_t n_in = min(p.inlet_cols, c0 + ncols) - c0;
+    for (uint32_t i = tid; i < R * n_in; i += nt) {
+      const uint32_t r = i / n_in, x = i - r * n_in;
+      const size_t cell = (size_t)(y0 + r) * p.w + c0 + x;
+      if (__ldg(p.old + cell) & kSolid) continue;
+      const uint64_t pk = __ldg(p.inlet_poly + (size_t)(y0 + r) * p.inlet_cols + c0 + x);
+      uint64_t st = 0;
+#pragma unroll
+      for (int j = 0; j < 64; ++j)
+        if (pk >> j & 1u) st ^= p.inlet_states[j];
+      out[(r * C + x / kSeg) * kOutPitch + x % kSeg] = lgx::equilibrium_sample(p.t, p.rest != 0, st);
+    }
+  }
+  cp_async_wait_all();
   __syncthreads();
-  const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x;
-  if (y >= p.h) return;
-  uint64_t st = jump_ahead(rng_seed(p.seed), p.row_off[y], jump);
-  uint8_t* row = p.cells + (size_t)y * p.w;
-  for (uint32_t x = 0; x < p.cols; ++x) {
-    if (row[x] & kSolid) continue;
-    row[x] = lgx::equilibrium_sample(p.t, p.rest != 0, st);
+  for (uint32_t i = tid; i < nb * kTab; i += nt)
+    tab[i] = jump_entry<kChunk>(states + (i / kTab) * 64, i % kTab);
+  // halo bytes between slots; across the row's ends when the tile spans it
+  for (uint32_t r = 0; r < in_rows; ++r) {
+    uint8_t* row = in + r * RB;
+    for (uint32_t s = tid; s < C; s += nt) {
+      uint8_t* slot = row + s * kSlot;
+      if (s > 0)
+        slot[15] = slot[16 + kSeg - 1 - kSlot];
+      else if (p.tiles_c == 1)
+        slot[15] = row[(C - 1) * kSlot + 16 + len_last - 1];
+      if (s + 1 < C)
+        slot[16 + kSeg] = slot[kSlot + 16];
+      else if (p.tiles_c == 1)
+        slot[16 + len_last] = row[16];
+    }
+  }
+  __syncthreads();
+
+  const uint32_t r = tid / C, s = tid - r * C;
+  if (r < R) {
+    const uint32_t y = y0 + r;
+    const uint32_t first = c0 + s * kSeg, len = min(kSeg, p.w - first);
+    uint64_t st = jump_poly<kChunk>(__ldg(p.poly + (size_t)y * p.segs + s0 + s),
+                                    tab + (y / p.band - b0) * kTab);
+    const uint8_t* up = in + r * RB + s * kSlot;
+    uint8_t* o = out + (r * C + s) * kOutPitch;
+    if (y & 1u)
+      walk<true>(up, up + RB, up + 2 * RB, o, first, len, st, lut, p.stride, p.inlet_cols);
+    else
+      walk<false>(up, up + RB, up + 2 * RB, o, first, len, st, lut, p.stride, p.inlet_cols);
+  }
+  __syncthreads();
+  for (uint32_t rr = 0; rr < R; ++rr) {
+    const uint8_t* src = out + rr * C * kOutPitch;
+    uint8_t* row = p.out + (size_t)(y0 + rr) * p.w + c0;
+    if ((p.w & 3u) == 0) {
+      for (uint32_t j = tid; j < (ncols >> 2); j += nt)
+        reinterpret_cast<uint32_t*>(row)[j] = lds32(src + (j >> 4) * kOutPitch + (j & 15u) * 4);
+    } else {
+      for (uint32_t x = tid; x < ncols; x += nt) row[x] = src[(x / kSeg) * kOutPitch + x % kSeg];
+    }
   }
 }
 
@@ -181,6 +411,23 @@ void build_table(bool rest, std::vector<uint8_t>* data, uint32_t* stride) {
   *stride = st;
 }
 
+// The step kernel's dynamic shared memory limit, raised once per device to
+// the largest tile plan_tiles can make.
+cudaError_t ensure_step_attributes(int device) {
+  static bool done[64] = {};
+  if (device >= 0 && device < 64 && done[device]) return cudaSuccess;
+  size_t most = 0;
+  for (uint32_t r = 1; r <= kMaxRows; ++r)
+    most = std::max(most, step_smem_bytes(kThreads / r, r, r));
+  cudaError_t e = cudaFuncSetAttribute(
+      lgx_byte_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(lgx_byte_step_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess && device >= 0 && device < 64) done[device] = true;
+  return e;
+}
+
 int cuda_fail(cudaError_t e, const char* what) {
   lgx::set_error(std::string(what) + ": " + cudaGetErrorString(e));
   return LGX_ERR_CUDA;
@@ -198,6 +445,9 @@ struct lgx_byte_lattice {
   int device = 0;
   cudaStream_t stream = nullptr;
   uint32_t w = 0, h = 0, threads = 1, band = 0, inlet_cols = 0, segs_per_row = 0;
+  // step tiles: segments and rows per block, tiles across a row, band tables
+  uint32_t tile_cols = 0, tile_rows = 0, tiles_c = 0, tiles = 0, nbands = 0, block = 0;
+  size_t smem = 0;
   bool rest = true;
   float density = 0, ux = 0, uy = 0;
   uint64_t seed = 0, steps = 0;
@@ -206,9 +456,8 @@ struct lgx_byte_lattice {
   int cur = 0;
   uint8_t* table = nullptr;
   uint32_t stride = 0;
-  uint64_t* jump = nullptr;
-  uint32_t* seg_off = nullptr;
-  uint32_t* row_off = nullptr;
+  uint64_t* seg_poly = nullptr;
+  uint64_t* inlet_poly = nullptr;
   // coarse-graining and counting go through the bitplane kernels
   lgx::Dims dm{};
   uint32_t* planes = nullptr;
@@ -226,43 +475,68 @@ namespace {
 void free_bytes(lgx_byte_lattice* L) {
   cudaSetDevice(L->device);
   if (L->stream) cudaStreamSynchronize(L->stream);
-  void* ptrs[] = {L->cells[0], L->cells[1], L->table, L->jump, L->seg_off, L->row_off,
-                  L->planes,   L->solid,    L->anysolid, L->counter, L->field, L->sums};
+  void* ptrs[] = {L->cells[0], L->cells[1], L->table,    L->seg_poly, L->inlet_poly, L->planes,
+                  L->solid,    L->anysolid, L->counter, L->field,    L->sums};
   for (void* p : ptrs) cudaFree(p);
   if (L->stream) cudaStreamDestroy(L->stream);
   delete L;
 }
 
-// Draw offsets of every segment and of every inflow row, from the obstacles
-// in `cells` (host copy).
+// The jump polynomial of every segment's first draw within its band, and of
+// every inflow cell's first draw in the inflow stream (row-major over the
+// leftmost columns, 3 or 4 draws per non-obstacle cell), from the obstacles in
+// `cells` (host copy).
 int build_offsets(lgx_byte_lattice* L, const uint8_t* cells) {
+  static const uint64_t q = lgx::rng_charpoly();
+  if (!q) {
+    lgx::set_error("the generator's characteristic polynomial failed its check");
+    return LGX_ERR_STATE;
+  }
   const uint32_t w = L->w, h = L->h;
-  std::vector<uint32_t> seg((size_t)h * L->segs_per_row), row(h, 0);
-  uint64_t count = 0;
+  const uint32_t icols = std::max(L->inlet_cols, 1u);
+  std::vector<uint64_t> seg((size_t)h * L->segs_per_row), inl((size_t)h * icols, 1);
+  uint64_t pk = 1;
   for (uint32_t y = 0; y < h; ++y) {
-    if (y % L->band == 0) count = 0;
+    if (y % L->band == 0) pk = 1;
     for (uint32_t s = 0; s < L->segs_per_row; ++s) {
-      seg[(size_t)y * L->segs_per_row + s] = (uint32_t)count;
+      seg[(size_t)y * L->segs_per_row + s] = pk;
       const uint32_t x1 = std::min(w, (s + 1) * kSeg);
-      for (uint32_t x = s * kSeg; x < x1; ++x) count += !(cells[(size_t)y * w + x] & kSolid);
-    }
-    if (count >= (1ull << 32)) {
-      lgx::set_error("a band has more than 2^32 fluid cells");
-      return LGX_ERR_ARG;
+      for (uint32_t x = s * kSeg; x < x1; ++x)
+        if (!(cells[(size_t)y * w + x] & kSolid)) pk = lgx::poly_mulz(pk, q);
     }
   }
   const uint32_t per = L->rest ? 4u : 3u;
-  uint64_t draws = 0;
-  for (uint32_t y = 0; y < h; ++y) {
-    row[y] = (uint32_t)draws;
-    for (uint32_t x = 0; x < L->inlet_cols; ++x) draws += per * !(cells[(size_t)y * w + x] & kSolid);
-  }
-  LGX_CUDA(cudaMemcpyAsync(L->seg_off, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice,
+  pk = 1;
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < L->inlet_cols; ++x) {
+      inl[(size_t)y * icols + x] = pk;
+      if (!(cells[(size_t)y * w + x] & kSolid))
+        for (uint32_t i = 0; i < per; ++i) pk = lgx::poly_mulz(pk, q);
+    }
+  LGX_CUDA(cudaMemcpyAsync(L->seg_poly, seg.data(), seg.size() * 8, cudaMemcpyHostToDevice,
                            L->stream));
-  LGX_CUDA(cudaMemcpyAsync(L->row_off, row.data(), row.size() * 4, cudaMemcpyHostToDevice,
+  LGX_CUDA(cudaMemcpyAsync(L->inlet_poly, inl.data(), inl.size() * 8, cudaMemcpyHostToDevice,
                            L->stream));
   LGX_CUDA(cudaStreamSynchronize(L->stream));
   return LGX_OK;
+}
+
+// Step tiles: a block takes up to 256 segments, as whole rows (up to 8) when a
+// row has fewer, and as many band tables as its rows meet.
+void plan_tiles(lgx_byte_lattice* L) {
+  const uint32_t segs = L->segs_per_row;
+  L->tile_cols = std::min(segs, kThreads);
+  L->tile_rows = std::min(std::min(kMaxRows, kThreads / L->tile_cols), L->h);
+  L->tiles_c = (segs + L->tile_cols - 1) / L->tile_cols;
+  const uint32_t tiles_r = (L->h + L->tile_rows - 1) / L->tile_rows;
+  L->tiles = L->tiles_c * tiles_r;
+  L->nbands = 1;
+  for (uint32_t t = 0; t < tiles_r; ++t) {
+    const uint32_t y0 = t * L->tile_rows, y1 = std::min(L->h, y0 + L->tile_rows) - 1;
+    L->nbands = std::max(L->nbands, y1 / L->band - y0 / L->band + 1);
+  }
+  L->block = std::min(kThreads, (L->tile_cols * L->tile_rows + 31) / 32 * 32);
+  L->smem = step_smem_bytes(L->tile_cols, L->tile_rows, L->nbands);
 }
 
 }  // namespace
@@ -312,23 +586,27 @@ int lgx_byte_create(size_t w, size_t h, float density, float ux, float uy, size_
   L->dm = lgx::make_dims(L->w, L->h, 0);
   std::vector<uint8_t> table;
   build_table(L->rest, &table, &L->stride);
-  std::vector<uint64_t> jumps = lgx::build_jumps();
-  jumps.resize((size_t)kJumps * 64);
+  if (L->stride > kMaxStride) {
+    lgx::set_error("collision table wider than the kernel's");
+    delete L;
+    return LGX_ERR_STATE;
+  }
+  plan_tiles(L);
   const size_t cells = w * h, total = L->dm.total;
   cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&L->cells[0], cells);
   if (e == cudaSuccess) e = cudaMalloc(&L->cells[1], cells);
   if (e == cudaSuccess) e = cudaMalloc(&L->table, table.size());
-  if (e == cudaSuccess) e = cudaMalloc(&L->jump, jumps.size() * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&L->seg_off, (size_t)L->h * L->segs_per_row * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&L->row_off, (size_t)L->h * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&L->seg_poly, (size_t)L->h * L->segs_per_row * 8);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&L->inlet_poly, (size_t)L->h * std::max(L->inlet_cols, 1u) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&L->planes, total * 7 * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->solid, total * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->anysolid, ((total + 31) / 32) * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->counter, 8);
   if (e == cudaSuccess) e = cudaMemset(L->cells[0], 0, cells);
   if (e == cudaSuccess) e = cudaMemcpy(L->table, table.data(), table.size(), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(L->jump, jumps.data(), jumps.size() * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = ensure_step_attributes(L->device);
   if (e != cudaSuccess) {
     const int rc = e == cudaErrorMemoryAllocation ? LGX_ERR_ALLOC : LGX_ERR_CUDA;
     lgx::set_error(std::string("lgx_byte_create: ") + cudaGetErrorString(e));
@@ -409,7 +687,6 @@ int lgx_byte_advance(lgx_byte_lattice* L, uint64_t n) {
     return LGX_ERR_ARG;
   }
   LGX_CUDA(cudaSetDevice(L->device));
-  const uint32_t nseg = L->h * L->segs_per_row;
   for (uint64_t i = 0; i < n; ++i) {
     ByteStepArgs a;
     a.old = L->cells[L->cur];
@@ -419,28 +696,23 @@ int lgx_byte_advance(lgx_byte_lattice* L, uint64_t n) {
     a.w = L->w;
     a.h = L->h;
     a.band = L->band;
-    a.segs_per_row = L->segs_per_row;
-    a.seg_off = L->seg_off;
-    a.jump = L->jump;
+    a.segs = L->segs_per_row;
+    a.cols = L->tile_cols;
+    a.rows = L->tile_rows;
+    a.tiles_c = L->tiles_c;
+    a.nbands = L->nbands;
+    a.poly = L->seg_poly;
     a.base_seed = L->seed ^ (L->steps * 0x9E3779B97F4A7C15ull);
-    lgx_byte_step_kernel<<<(nseg + 127) / 128, 128, 0, L->stream>>>(a);
+    a.inlet_cols = L->inlet_cols;
+    a.inlet_poly = L->inlet_poly;
+    uint64_t x = rng_seed(L->seed ^ ((L->steps + 1) * 0xD1B54A32D192ED03ull));
+    for (int j = 0; j < 64; ++j, x = xorshift(x)) a.inlet_states[j] = x;
+    memcpy(a.t, L->thresh, sizeof(a.t));
+    a.rest = L->rest ? 1 : 0;
+    lgx_byte_step_kernel<<<L->tiles, L->block, L->smem, L->stream>>>(a);
     LGX_CUDA(cudaGetLastError());
     L->cur ^= 1;
     L->steps += 1;
-    if (L->inlet_cols) {
-      ByteInletArgs b;
-      b.cells = L->cells[L->cur];
-      b.w = L->w;
-      b.h = L->h;
-      b.cols = L->inlet_cols;
-      b.row_off = L->row_off;
-      b.jump = L->jump;
-      b.seed = L->seed ^ (L->steps * 0xD1B54A32D192ED03ull);
-      memcpy(b.t, L->thresh, sizeof(b.t));
-      b.rest = L->rest ? 1 : 0;
-      lgx_byte_inlet_kernel<<<(L->h + 127) / 128, 128, 0, L->stream>>>(b);
-      LGX_CUDA(cudaGetLastError());
-    }
   }
   LGX_CUDA(cudaStreamSynchronize(L->stream));
   return LGX_OK;

@@ -49,6 +49,81 @@ __device__ __forceinline__ uint64_t jump_ahead(uint64_t x, uint64_t k, const uin
   return x;
 }
 
+// Jump polynomials (Haramoto, Matsumoto, L'Ecuyer, Panneton and Nishimura,
+// "Efficient jump ahead for F2-linear random number generators", 2008).  With
+// P(z) = z^64 + q(z) the characteristic polynomial of M, P(M) = 0, so
+// M^k = p_k(M) with p_k = z^k mod P, and M^k x = xor of M^j x over the set
+// coefficients j of p_k.  When many jumps start from the same x (every segment
+// of one band), the 64 states M^j x are shared and folded into tables over
+// B-bit chunks of p_k, T[c][n] = xor over the set bits b of n of M^(Bc+b) x;
+// a jump is then 64/B table lookups, and p_k is one 64-bit word.
+//
+// Host: q, the low 64 coefficients of P, from the Berlekamp-Massey algorithm
+// (Massey, 1969) over one state bit's sequence, checked on every basis vector
+// (M^64 e = q(M) e).  Returns 0 if the check fails.
+inline uint64_t rng_charpoly() {
+  constexpr int N = 128;
+  int s[N];
+  uint64_t x = 1;
+  for (int t = 0; t < N; ++t, x = xorshift(x)) s[t] = (int)(x & 1);
+  int C[N + 1] = {1}, B[N + 1] = {1}, T[N + 1];
+  int L = 0, m = 1;
+  for (int n = 0; n < N; ++n) {
+    int d = s[n];
+    for (int i = 1; i <= L; ++i) d ^= C[i] & s[n - i];
+    if (!d) {
+      ++m;
+      continue;
+    }
+    for (int i = 0; i <= N; ++i) T[i] = C[i];
+    for (int i = 0; i + m <= N; ++i) C[i + m] ^= B[i];
+    if (2 * L <= n) {
+      L = n + 1 - L;
+      for (int i = 0; i <= N; ++i) B[i] = T[i];
+      m = 1;
+    } else {
+      ++m;
+    }
+  }
+  if (L != 64) return 0;
+  uint64_t q = 0;
+  for (int j = 0; j < 64; ++j) q |= (uint64_t)C[64 - j] << j;
+  for (int e = 0; e < 64; ++e) {
+    uint64_t v = 1ull << e, acc = 0;
+    for (int j = 0; j < 64; ++j, v = xorshift(v))
+      if (q >> j & 1) acc ^= v;
+    if (acc != v) return 0;
+  }
+  return q;
+}
+
+// p * z mod P: one more generator step.
+__host__ __device__ __forceinline__ uint64_t poly_mulz(uint64_t p, uint64_t q) {
+  return (p << 1) ^ ((p >> 63) ? q : 0ull);
+}
+
+// Entry e = c * 2^B + n of the chunk tables of the states M^j x, j < 64, held
+// in `states`.
+template <int B>
+__device__ __forceinline__ uint64_t jump_entry(const uint64_t* states, uint32_t e) {
+  const uint64_t* s = states + (e >> B) * B;
+  uint64_t v = 0;
+#pragma unroll
+  for (int b = 0; b < B; ++b)
+    if (e >> b & 1u) v ^= s[b];
+  return v;
+}
+
+// M^k x for p = z^k mod P, from the chunk tables of x.
+template <int B>
+__device__ __forceinline__ uint64_t jump_poly(uint64_t p, const uint64_t* tab) {
+  uint64_t r = 0;
+#pragma unroll
+  for (int c = 0; c < 64 / B; ++c)
+    r ^= tab[(c << B) + (uint32_t)((p >> (B * c)) & ((1u << B) - 1))];
+  return r;
+}
+
 // Host: columns of M^(2^i), i < kJumpBits.
 inline std::vector<uint64_t> build_jumps() {
   auto apply = [](const uint64_t* cols, uint64_t v) {

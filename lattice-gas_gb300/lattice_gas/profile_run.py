@@ -8,7 +8,8 @@ Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 `sweep` (the 64-lattice transport sweep as one batch), `transport` (one
 transport::measure at --size, density 0.22), `fill` (init_equilibrium on the
 device over the roofline case's geometry at 16384 x 8192), `tiny` (eight --size x
---size lattices as one batch).  --policy picks the sweep's batch
+--size lattices as one batch), `bytes` (the wake run on the reference's
+byte-per-cell update, 16 bands).  --policy picks the sweep's batch
 policy (under a profiler pass 1: the tuner's timings are not meaningful there, and
 without one it picks one launch per step for every class of this sweep).  --mode
 picks the step
@@ -27,7 +28,7 @@ from lattice_gas import workloads as W  # noqa: E402
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="wake",
-                    choices=["wake", "big", "sweep", "transport", "fill", "tiny"])
+                    choices=["wake", "big", "sweep", "transport", "fill", "tiny", "bytes"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--policy", type=int, default=0,
                     help="batch policy for the sweep: 0 tuned, 1 one launch per step, 2 resident")
@@ -41,6 +42,15 @@ def main():
         b = LG.Batch(lats, a.policy)
         b.advance(a.steps)
         print("tiny: 8 x %d^2, %d steps, policy %d, plan %s" % (a.size, a.steps, a.policy, b.plan))
+        return
+    if a.case == "bytes":
+        wl = W.wake_run()
+        lat = LG.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
+        lat.load(wl.cells)
+        lat.advance(a.steps)
+        print("bytes: %d x %d, %d steps, %d particles" % (wl.w, wl.h, a.steps,
+                                                           lat.total_particles()))
+        lat.close()
         return
     if a.case == "fill":
         wl = W.roofline_case(w=16384, h=8192, n_circles=50)

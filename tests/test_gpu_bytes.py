@@ -55,6 +55,9 @@ def test_golden_output_on_the_device(LG, O, case):
     (64, 64, 8, 0, False),      # six-direction rule
     (1000, 40, 1, 70, True),    # one band, many segments per row
     (48, 48, 48, 0, True),      # a band per row
+    (16640, 8, 3, 20, True),    # rows wider than one tile: two tiles across, word loads
+    (16390, 6, 2, 5, False),    # two tiles across, byte loads, a 6-cell last segment
+    (200, 30, 30, 0, True),     # four segments and eight rows per tile, eight bands in it
 ])
 def test_device_byte_path_matches_the_oracle(LG, O, w, h, threads, inlet, rest):
     cells = np.zeros(w * h, np.uint8)
