@@ -29,10 +29,12 @@
 // The inflow re-seed after the step (src/lattice.rs:270-285) draws from one
 // serial stream, 3 or 4 draws per non-obstacle cell of the leftmost columns,
 // and depends only on that stream and the obstacles, so it is fused: every
-// inflow cell has its own jump polynomial, the host passes the stream's first
-// 64 states with the launch, and the block's threads draw the tile's inflow
-// cells while its rows are in flight, into the output tile, where the
-// collision results leave them be.
+// inflow cell (or, for inflows wider than 64 columns, every group of 8 cells
+// of a row, to bound the table) has its own jump polynomial, the host passes
+// the stream's first 64 states with the launch, and the block's threads draw
+// the tile's inflow cells while its rows are in flight, into the output tile,
+// where the collision results leave them be.  Many short draws finish sooner
+// than a few long ones: this phase runs beside the tile's loads.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -60,6 +62,8 @@ constexpr uint32_t kMaxRows = 8;          // rows per tile
 constexpr uint32_t kSlot = kSeg + 16;     // input slot: 15 pad bytes, left halo, cells
 constexpr uint32_t kOutPitch = kSeg + 4;  // output slot: 17 words
 constexpr uint32_t kMaxStride = 30;       // outcomes per state in the padded table
+constexpr uint32_t kInGroupWide = 8;      // inflow cells per jump polynomial, wide inflows
+constexpr uint32_t kInNarrow = 64;        // inflows up to this wide: one polynomial a cell
 constexpr uint32_t kLutBytes = 128 * kMaxStride;
 static_assert((kSlot / 16) % 2 == 1 && (kOutPitch / 4) % 2 == 1, "odd pitches");
 static_assert(kLutBytes % 16 == 0, "tile alignment");
@@ -81,8 +85,8 @@ struct ByteStepArgs {
   const uint64_t* poly;  // per segment: z^k mod P, k its first draw within the band
   uint64_t base_seed;    // seed ^ steps * 0x9E3779B97F4A7C15
   // the inflow re-seed
-  uint32_t inlet_cols;
-  const uint64_t* inlet_poly;  // per row and inflow column: z^k mod P, k the draws before it
+  uint32_t inlet_cols, inlet_group, inlet_groups;  // cells per group, groups per row
+  const uint64_t* inlet_poly;  // per row and inflow group: z^k mod P, k the draws before it
   uint32_t t[7];
   int rest;
   uint64_t inlet_states[64];  // the stream's first 64 states (seed ^ steps after the step
@@ -250,6 +254,33 @@ __device__ __forceinline__ void walk(const uint8_t* up, const uint8_t* mid, cons
   }
 }
 
+// The inflow samples of a tile's rows y0 .. y0+R-1 and columns c0 .. (up to the
+// inflow's edge), G cells of a row per task, into the output tile.
+template <uint32_t G>
+__device__ __forceinline__ void inflow_tile(const ByteStepArgs& p, uint8_t* out, uint32_t y0,
+                                            uint32_t R, uint32_t C, uint32_t c0, uint32_t ncols,
+                                            uint32_t tid, uint32_t nt) {
+  const uint32_t n_in = min(p.inlet_cols, c0 + ncols) - c0;
+  const uint32_t n_g = (n_in + G - 1) / G;
+  for (uint32_t i = tid; i < R * n_g; i += nt) {
+    const uint32_t r = i / n_g, x0 = (i - r * n_g) * G;
+    const uint32_t n = min(G, n_in - x0);
+    const uint8_t* cell = p.old + (size_t)(y0 + r) * p.w + c0 + x0;
+    if (G == 1 && (__ldg(cell) & kSolid)) continue;
+    const uint64_t pk = __ldg(p.inlet_poly + (size_t)(y0 + r) * p.inlet_groups + (c0 + x0) / G);
+    uint64_t st = 0;
+#pragma unroll
+    for (int j = 0; j < 64; ++j)
+      if (pk >> j & 1u) st ^= p.inlet_states[j];
+    for (uint32_t x = 0; x < n; ++x) {
+      if (G > 1 && (__ldg(cell + x) & kSolid)) continue;
+      const uint32_t xt = x0 + x;
+      out[(r * C + xt / kSeg) * kOutPitch + xt % kSeg] =
+          lgx::equilibrium_sample(p.t, p.rest != 0, st);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_constant__ ByteStepArgs p) {
   extern __shared__ __align__(16) uint8_t smem[];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
@@ -309,18 +340,10 @@ __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_co
   }
   // the inflow cells of the tile, into the output tile
   if (c0 < p.inlet_cols) {
-    const uint32_t n_in = min(p.inlet_cols, c0 + ncols) - c0;
-    for (uint32_t i = tid; i < R * n_in; i += nt) {
-      const uint32_t r = i / n_in, x = i - r * n_in;
-      const size_t cell = (size_t)(y0 + r) * p.w + c0 + x;
-      if (__ldg(p.old + cell) & kSolid) continue;
-      const uint64_t pk = __ldg(p.inlet_poly + (size_t)(y0 + r) * p.inlet_cols + c0 + x);
-      uint64_t st = 0;
-#pragma unroll
-      for (int j = 0; j < 64; ++j)
-        if (pk >> j & 1u) st ^= p.inlet_states[j];
-      out[(r * C + x / kSeg) * kOutPitch + x % kSeg] = lgx::equilibrium_sample(p.t, p.rest != 0, st);
-    }
+    if (p.inlet_group == 1)
+      inflow_tile<1>(p, out, y0, R, C, c0, ncols, tid, nt);
+    else
+      inflow_tile<kInGroupWide>(p, out, y0, R, C, c0, ncols, tid, nt);
   }
   cp_async_wait_all();
   __syncthreads();
@@ -472,6 +495,17 @@ struct lgx_byte_lattice {
 
 namespace {
 
+// Inflow cells per jump polynomial, and groups per row (at least one, for the
+// allocation).
+uint32_t inlet_group(const lgx_byte_lattice* L) {
+  return L->inlet_cols <= kInNarrow ? 1u : kInGroupWide;
+}
+
+uint32_t inlet_groups(const lgx_byte_lattice* L) {
+  const uint32_t g = inlet_group(L);
+  return std::max((L->inlet_cols + g - 1) / g, 1u);
+}
+
 void free_bytes(lgx_byte_lattice* L) {
   cudaSetDevice(L->device);
   if (L->stream) cudaStreamSynchronize(L->stream);
@@ -483,7 +517,7 @@ void free_bytes(lgx_byte_lattice* L) {
 }
 
 // The jump polynomial of every segment's first draw within its band, and of
-// every inflow cell's first draw in the inflow stream (row-major over the
+// every inflow group's first draw in the inflow stream (row-major over the
 // leftmost columns, 3 or 4 draws per non-obstacle cell), from the obstacles in
 // `cells` (host copy).
 int build_offsets(lgx_byte_lattice* L, const uint8_t* cells) {
@@ -493,8 +527,8 @@ int build_offsets(lgx_byte_lattice* L, const uint8_t* cells) {
     return LGX_ERR_STATE;
   }
   const uint32_t w = L->w, h = L->h;
-  const uint32_t icols = std::max(L->inlet_cols, 1u);
-  std::vector<uint64_t> seg((size_t)h * L->segs_per_row), inl((size_t)h * icols, 1);
+  const uint32_t groups = inlet_groups(L), gs = inlet_group(L);
+  std::vector<uint64_t> seg((size_t)h * L->segs_per_row), inl((size_t)h * groups, 1);
   uint64_t pk = 1;
   for (uint32_t y = 0; y < h; ++y) {
     if (y % L->band == 0) pk = 1;
@@ -509,7 +543,7 @@ int build_offsets(lgx_byte_lattice* L, const uint8_t* cells) {
   pk = 1;
   for (uint32_t y = 0; y < h; ++y)
     for (uint32_t x = 0; x < L->inlet_cols; ++x) {
-      inl[(size_t)y * icols + x] = pk;
+      if (x % gs == 0) inl[(size_t)y * groups + x / gs] = pk;
       if (!(cells[(size_t)y * w + x] & kSolid))
         for (uint32_t i = 0; i < per; ++i) pk = lgx::poly_mulz(pk, q);
     }
@@ -599,7 +633,7 @@ int lgx_byte_create(size_t w, size_t h, float density, float ux, float uy, size_
   if (e == cudaSuccess) e = cudaMalloc(&L->table, table.size());
   if (e == cudaSuccess) e = cudaMalloc(&L->seg_poly, (size_t)L->h * L->segs_per_row * 8);
   if (e == cudaSuccess)
-    e = cudaMalloc(&L->inlet_poly, (size_t)L->h * std::max(L->inlet_cols, 1u) * 8);
+    e = cudaMalloc(&L->inlet_poly, (size_t)L->h * inlet_groups(L) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&L->planes, total * 7 * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->solid, total * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->anysolid, ((total + 31) / 32) * 4);
@@ -704,6 +738,8 @@ int lgx_byte_advance(lgx_byte_lattice* L, uint64_t n) {
     a.poly = L->seg_poly;
     a.base_seed = L->seed ^ (L->steps * 0x9E3779B97F4A7C15ull);
     a.inlet_cols = L->inlet_cols;
+    a.inlet_group = inlet_group(L);
+    a.inlet_groups = inlet_groups(L);
     a.inlet_poly = L->inlet_poly;
     uint64_t x = rng_seed(L->seed ^ ((L->steps + 1) * 0xD1B54A32D192ED03ull));
     for (int j = 0; j < 64; ++j, x = xorshift(x)) a.inlet_states[j] = x;
