@@ -91,3 +91,40 @@ def test_restart_and_thread_invariance_of_conserved_quantities(LG, O):
             if expected is None:
                 expected = after
             assert after == expected
+
+
+def test_full_size_wake_run_on_the_byte_path(LG, O):
+    """4096 x 2304, the full-size wake run on the reference's byte stream (16 bands, the
+    plate, walls, an 8-column inflow): the device equals the oracle's Lattice::step after
+    1, 4 and 12 steps, and the obstacles and walls stay in place."""
+    from lattice_gas import workloads as W
+    wl = W.wake_run()
+    lat = LG.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
+    lat.load(wl.cells)
+    ref = O.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
+    ref.set_cells(wl.cells)
+    solid = (np.asarray(wl.cells) & 0x80) != 0
+    for n in (1, 3, 8):
+        lat.advance(n)
+        ref.advance(n)
+        got = lat.store()
+        assert np.array_equal(got, ref.cells), "differs in %d cells" % int((got != ref.cells).sum())
+        assert np.array_equal((got & 0x80) != 0, solid)
+    assert lat.total_particles() == ref.total_particles()
+
+
+def test_full_size_fill_then_step_on_the_byte_path(LG, O):
+    """The wake run's geometry filled on the device (init_equilibrium), then 5 steps: the
+    same cells as the oracle's fill and steps."""
+    from lattice_gas import workloads as W
+    wl = W.wake_run()
+    lat = LG.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
+    lat.load(wl.cells)
+    lat.init_equilibrium()
+    ref = O.Lattice(wl.w, wl.h, wl.density, wl.inflow, wl.inlet_cols, wl.rest, 16, wl.seed)
+    ref.set_cells(wl.cells)
+    ref.init_equilibrium()
+    assert np.array_equal(lat.store(), ref.cells)
+    lat.advance(5)
+    ref.advance(5)
+    assert np.array_equal(lat.store(), ref.cells)
