@@ -380,6 +380,86 @@ def bench_transport(LG, cpu: bool):
     return out
 
 
+# The reference's GPU benchmark matrix (benches/speed.rs:480-592) and its figures on
+# an Apple M3 Pro through Metal (benches/baseline.txt:21-29), Mcell/s: context, not a
+# target (other hardware, other API).
+REFERENCE_MATRIX = [
+    ("step/gpu/2048x1280/one-per-submit", 16692.3),
+    ("step/gpu/2048x1280/batched", 79234.4),
+    ("step/gpu/256x256/batched", 9428.9),
+    ("step/gpu/4096x2048/batched", 93454.4),
+    ("step/gpu/2048x1280/batched+inlet", 76372.2),
+    ("step/gpu/2048x1280/batched+inlet+sample", 70812.7),
+    ("field/gpu/sample/2048x1280", 20465.0),
+    ("lattice/gpu/store/2048x1280", 2611.4),
+    ("lattice/gpu/total-particles/2048x1280", 17646.6),
+]
+
+
+def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
+    """Each case of the reference's GPU benchmark group through this engine's
+    GpuLattice, set up as benches/speed.rs does (density 0.22, speed 0.4, 20x20 blocks,
+    seed 0x5EED, cells from Lattice::init_equilibrium) and timed its way
+    (benches/speed.rs:150-193): warm up, then the best of `samples` samples of about
+    `sample_s` seconds each. Every call waits for the device, as the reference's
+    submit-and-wait does. Throughput in Gcell/s (cell updates, or cells processed)."""
+    D, S, BLOCK, SEED = 0.22, 0.4, 20, 0x5EED
+
+    def seeded(w, h):
+        cells = np.zeros(w * h, np.uint8)
+        LG.init_equilibrium(cells, D, S, 0.0, True, SEED)
+        g = LG.GpuLattice(w, h, True, SEED)
+        g.load(cells)
+        return g
+
+    def rate(body, cells_per_iter):
+        t0, n = time.perf_counter(), 0
+        while time.perf_counter() - t0 < sample_s or n < 3:
+            body()
+            n += 1
+        per = (time.perf_counter() - t0) / n
+        iters = max(1, int(round(sample_s / per)))
+        best = float("inf")
+        for _ in range(samples):
+            t = time.perf_counter()
+            for _ in range(iters):
+                body()
+            best = min(best, (time.perf_counter() - t) / iters)
+        return cells_per_iter / best / 1e9
+
+    bw, bh = 2048, 1280
+    out = []
+    g = seeded(bw, bh)
+    got = [rate(lambda: g.advance(1), bw * bh), rate(lambda: g.advance(100), bw * bh * 100)]
+    g.close()
+    g = seeded(256, 256)
+    got.append(rate(lambda: g.advance(100), 256 * 256 * 100))
+    g.close()
+    g = seeded(4096, 2048)
+    got.append(rate(lambda: g.advance(100), 4096 * 2048 * 100))
+    g.close()
+    g = seeded(bw, bh)
+    g.set_inlet(8, D, (S, 0.0), True)
+    got.append(rate(lambda: g.advance(100), bw * bh * 100))
+    g.attach_field(BLOCK, BLOCK)
+    got.append(rate(lambda: g.advance_sampling(100, 5, 0.2), bw * bh * 100))
+    g.close()
+    g = seeded(bw, bh)
+    g.attach_field(BLOCK, BLOCK)
+    got.append(rate(lambda: g.sample_field(0.2), bw * bh))
+    buf = np.zeros(bw * bh, np.uint8)
+    got.append(rate(lambda: g.store(buf), bw * bh))
+    got.append(rate(lambda: g.total_particles(), bw * bh))
+    g.close()
+    for (name, ref), v in zip(REFERENCE_MATRIX, got):
+        out.append({"case": name, "value": round(v, 2), "reference_m3pro_metal": round(ref / 1e3, 3),
+                    "ratio": round(v * 1e3 / ref, 1)})
+    return {"unit": "Gcell/s", "cases": out,
+            "note": "the reference's own GPU cases (benches/speed.rs) on this engine, best of "
+                    "%d samples of ~%.1f s; its M3 Pro Metal figures (benches/baseline.txt) are "
+                    "other hardware, for context" % (samples, sample_s)}
+
+
 def bench_byte_path(LG, W, steps: int, cpu_rate):
     """The reference's own CPU update (byte per cell, its random stream, bands of
     ceil(h / threads) rows, src/lattice.rs:222-364) run on the device on the wake
@@ -589,13 +669,14 @@ def run_gb300(args, world, rank, local):
                                      "update (GpuLattice's shader) restated in C, %d threads"
                                      % (bsteps, bdt, threads)}
 
-    batched = served = big = transport = byte_path = None
+    batched = served = big = transport = byte_path = matrix = None
     if not args.no_patterns:
         batched = bench_batched(LG, W, args.sweep_steps)
         served = bench_served(LG, W, args.requests, args.budget_mib << 20)
         big = bench_roofline_case(LG, W, args.big_steps)
         transport = bench_transport(LG, rank == 0 and world == 1 and not args.no_cpu)
         byte_path = bench_byte_path(LG, W, 1000, rate if cpu else None)
+        matrix = bench_reference_matrix(LG)
     lop3_peak = LG.probe_int_rate(0)
     alu_achieved = STEP_ALU_WARP_INSTR * 32 / (step_ms * 1e-3)
 
@@ -637,6 +718,7 @@ def run_gb300(args, world, rank, local):
         "roofline_case": big,
         "transport": transport,
         "byte_path": byte_path,
+        "reference_matrix": matrix,
         "device": g.device_name(),
     }
     print(json.dumps(line), flush=True)

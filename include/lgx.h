@@ -87,12 +87,23 @@ int lgx_advance_sampling(lgx_lattice *lat, uint64_t n, uint64_t sample_every, fl
  * tail.  WAVE runs up to 128 steps per cooperative launch of a persistent
  * kernel (each block owns a fixed range of words and waits, with a bounded
  * spin, only for the blocks owning the rows next to its own).  TEMPORAL: see
- * lgx_set_temporal_depth.  AUTO (default) uses whichever of SINGLE, WAVE and
- * TEMPORAL with depth 4 or 8 a tuner measured fastest for the lattice's size
- * class (timed on a scratch lattice of the same shape at its first advance,
- * cached for the process; lgx_get_step_plan).  Results are identical in every
- * mode. */
-enum { LGX_STEP_AUTO = 0, LGX_STEP_SINGLE = 1, LGX_STEP_WAVE = 2, LGX_STEP_TEMPORAL = 3 };
+ * lgx_set_temporal_depth.  GRAPH runs advances of 8 steps or more, sampling
+ * every 16 steps or less often, as a batch of this lattice alone (lgx_batch_*;
+ * other advances take SINGLE's path): intervals replayed from captured CUDA
+ * graphs, or the resident kernel for a small lattice, on the lattice's own
+ * stream; for lattices that do not fill the GPU, where one launch per step
+ * is bound by the host's launch rate.  AUTO (default) uses whichever of
+ * SINGLE, WAVE, TEMPORAL with depth 4 or 8 and (below one full wave of step
+ * blocks) GRAPH a tuner measured fastest for the lattice's size class (timed
+ * on a scratch lattice of the same shape at its first advance, cached for the
+ * process; lgx_get_step_plan).  Results are identical in every mode. */
+enum {
+  LGX_STEP_AUTO = 0,
+  LGX_STEP_SINGLE = 1,
+  LGX_STEP_WAVE = 2,
+  LGX_STEP_TEMPORAL = 3,
+  LGX_STEP_GRAPH = 4
+};
 int lgx_set_step_mode(lgx_lattice *lat, int mode);
 /* TEMPORAL: runs of k steps (k = 4 or 8, lgx_set_temporal_depth) in one pass
  * over HBM, the intermediate steps kept in registers (lattices at least 64
@@ -107,6 +118,7 @@ typedef struct lgx_step_plan {
   float single_us;         /* one launch per step, with that shape */
   float single1_us, single2_us;  /* one launch per step, one and two chunks per warp */
   float wave_us, temporal4_us, temporal8_us;
+  float graph_us;          /* the one-lattice batch (GRAPH) */
 } lgx_step_plan;
 int lgx_get_step_plan(lgx_lattice *lat, lgx_step_plan *out);
 /* GpuLattice::sample_field (src/gpu.rs:710-721). */

@@ -109,4 +109,10 @@ typedef cudaError_t (*BatchStepHook)(void* ctx, cudaStream_t st, const uint64_t*
                                      uint32_t k_after);
 int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx, bool per_step);
 
+// lgx_batch_create_ex, with the batch's work on `stream` when it is not null
+// (a member lattice's own stream, borrowed: the batch neither creates nor
+// destroys it, so events recorded on that stream bracket the batch's work).
+int batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream_t stream,
+                 lgx_batch** out);
+
 }  // namespace lgx

@@ -70,6 +70,7 @@ int cuda_fail(cudaError_t e, const char* what) {
 struct lgx_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
+  bool own_stream = true;  // false: a member lattice's stream, borrowed
   std::vector<lgx_lattice*> lats;
   std::vector<lgx::LatDesc> descs;
   lgx::LatDesc* d_descs = nullptr;
@@ -79,6 +80,7 @@ struct lgx_batch {
   uint32_t nblocks = 0;
   uint32_t rest_blocks = 0;     // leading per-step blocks, those of rest-particle lattices
   uint32_t items_per_step = 0;  // inlet draw items of one step, all lattices
+  uint64_t item0_len = 1;       // the interval length d_item0 holds the prefix for
   uint32_t field_blocks = 0;
   std::vector<uint32_t*> inlet_bufs;
   std::vector<GraphEntry> graphs;
@@ -166,7 +168,7 @@ void free_batch(lgx_batch* b) {
   cudaFree(b->d_base);
   for (auto& ev : b->ev)
     if (ev) cudaEventDestroy(ev);
-  if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->stream && b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
 }
 
@@ -346,10 +348,19 @@ int batch_set_step_hook(lgx_batch* b, BatchStepHook fn, void* ctx, bool per_step
 extern "C" {
 
 int lgx_batch_create(lgx_lattice* const* lats, size_t n, lgx_batch** out) {
-  return lgx_batch_create_ex(lats, n, LGX_BATCH_AUTO, out);
+  return lgx::batch_create(lats, n, LGX_BATCH_AUTO, nullptr, out);
 }
 
 int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batch** out) {
+  return lgx::batch_create(lats, n, policy, nullptr, out);
+}
+
+}  // extern "C"
+
+// A batch whose work runs on `stream` (a member lattice's own stream, which it
+// neither creates nor destroys), or on a stream of its own when that is null.
+int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream_t stream,
+                      lgx_batch** out) {
   if (policy != LGX_BATCH_AUTO && policy != LGX_BATCH_PER_STEP && policy != LGX_BATCH_RESIDENT) {
     lgx::set_error("lgx_batch_create_ex: unknown policy");
     return LGX_ERR_ARG;
@@ -450,7 +461,12 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
     b->classes.push_back(rc);
   }
   lats = b->lats.data();
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (stream) {
+    b->stream = stream;
+    b->own_stream = false;
+  } else if (e == cudaSuccess) {
+    e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
@@ -497,6 +513,8 @@ int lgx_batch_create_ex(lgx_lattice* const* lats, size_t n, int policy, lgx_batc
   return LGX_OK;
 }
 
+extern "C" {
+
 int lgx_batch_destroy(lgx_batch* b) {
   if (b) free_batch(b);
   return LGX_OK;
@@ -510,7 +528,8 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
   LGX_CUDA(cudaSetDevice(b->device));
   // Field and block tables were laid out at creation; pending work on a
   // member's own stream finishes first.
-  for (lgx_lattice* l : b->lats) LGX_CUDA(cudaStreamSynchronize(l->stream));
+  for (lgx_lattice* l : b->lats)
+    if (l->stream != b->stream) LGX_CUDA(cudaStreamSynchronize(l->stream));
   int rc = setup_descs(b, alpha);
   if (rc) return rc;
   // The inlet draws of an interval are laid out per lattice as [k][h][iw][7];
@@ -529,13 +548,14 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
       len = p2;
       sample = every > 0 && (since + len >= every || len == left);
     }
-    if (b->items_per_step) {
-      // prefix for this interval length
+    if (b->items_per_step && b->item0_len != len) {
+      // prefix for this interval length (kept on the device while it repeats)
       std::vector<uint32_t> item0(b->lats.size() + 1, 0);
       for (size_t i = 0; i < b->lats.size(); ++i)
         item0[i + 1] = item0[i] + (uint32_t)len * b->lats[i]->dm.h * b->lats[i]->dm.iw;
       LGX_CUDA(cudaMemcpyAsync(b->d_item0, item0.data(), item0.size() * 4,
                                cudaMemcpyHostToDevice, b->stream));
+      b->item0_len = len;
     }
     cudaGraphExec_t ex = nullptr;
     rc = graph_for(b, (uint32_t)len, sample, &ex);

@@ -49,8 +49,13 @@ struct lgx_lattice {
   int auto_mode = LGX_STEP_SINGLE;
   uint32_t auto_depth = 0;
   uint32_t auto_words = 0;        // chunks per warp of the single-step kernel
-  float auto_us[6] = {0, 0, 0, 0, 0, 0};  // single (best, 1, 2 chunks), wave, temporal 4, 8
+  float auto_us[7] = {0, 0, 0, 0, 0, 0, 0};  // single (best, 1, 2 chunks), wave, temporal 4,
+                                              // 8, graph
   uint32_t step_words = 0;        // a pinned kernel shape (0: by size, or the tuner's)
+  // LGX_STEP_GRAPH: a batch of this lattice alone, whose work runs on the
+  // lattice's stream; made at first use, dropped when the inlet or the field
+  // (which a batch lays out when it is made) changes
+  lgx_batch* solo = nullptr;
   uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
   uint32_t* done = nullptr;  // [wave_grid] published step per CTA
   uint32_t* error = nullptr; // timeout flag

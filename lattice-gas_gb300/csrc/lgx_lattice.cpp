@@ -14,6 +14,7 @@
 #include <string>
 
 #include "../../include/lgx.h"
+#include "lgx_batch.hpp"
 #include "lgx_handle.hpp"
 #include "lgx_profile.hpp"
 #include "lgx_tune.hpp"
@@ -78,8 +79,15 @@ int check_lat(lgx_lattice* lat) {
   return LGX_OK;
 }
 
+// The one-lattice batch of LGX_STEP_GRAPH, if made.
+void drop_solo(lgx_lattice* lat) {
+  if (lat->solo) lgx_batch_destroy(lat->solo);
+  lat->solo = nullptr;
+}
+
 void free_lattice(lgx_lattice* lat) {
   cudaSetDevice(lat->device);
+  drop_solo(lat);  // before the stream it borrows
   if (lat->stream) cudaStreamSynchronize(lat->stream);
   cudaFree(lat->planes[0]);
   cudaFree(lat->planes[1]);
@@ -242,7 +250,7 @@ int resolve_auto(lgx_lattice* lat) {
     // the tuner could not run here (e.g. no room for its scratch lattice): the
     // reference's own launch pattern, one kernel per step
     cudaGetLastError();
-    p = lgx::StepPlan{LGX_STEP_SINGLE, 0, 0, 0, 0, 0, 0, 0, 0};
+    p = lgx::StepPlan{LGX_STEP_SINGLE, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   }
   lat->auto_mode = p.mode;
   lat->auto_depth = p.depth;
@@ -253,8 +261,34 @@ int resolve_auto(lgx_lattice* lat) {
   lat->auto_us[3] = p.wave_us;
   lat->auto_us[4] = p.temporal4_us;
   lat->auto_us[5] = p.temporal8_us;
+  lat->auto_us[6] = p.graph_us;
   lat->auto_resolved = true;
   return LGX_OK;
+}
+
+// LGX_STEP_GRAPH: runs of at least this many steps, sampling no more often
+// than every kGraphMinEvery steps, go through the lattice's one-lattice batch
+// (captured CUDA graphs, or the resident kernel for a small lattice); other
+// runs take one launch per step.  A batch launches one graph per sampling
+// interval, which costs about as much as 10-15 single-step launches save.
+constexpr uint64_t kGraphMinSteps = 8;
+constexpr uint64_t kGraphMinEvery = 16;
+
+int advance_graph(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
+  if (!lat->solo) {
+    lgx_lattice* one[1] = {lat};
+    const int rc = lgx::batch_create(one, 1, LGX_BATCH_AUTO, lat->stream, &lat->solo);
+    if (rc) {
+      lat->solo = nullptr;
+      return rc;
+    }
+  }
+  uint64_t k0 = 0, k1 = 0, g = 0;
+  lgx_batch_launch_count(lat->solo, &k0, &g);
+  const int rc = lgx_batch_advance_sampling(lat->solo, n, every, alpha);
+  lgx_batch_launch_count(lat->solo, &k1, &g);
+  lat->launches += k1 - k0;
+  return rc;
 }
 
 int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
@@ -439,6 +473,7 @@ int lgx_set_inlet(lgx_lattice* lat, size_t cols, float density, float ux, float 
   if (rc) return rc;
   lat->dm = lgx::make_dims(lat->dm.w, lat->dm.h, (uint32_t)std::min<size_t>(cols, lat->dm.w));
   lgx::equilibrium_thresholds(density, ux, uy, rest != 0, lat->thresh);
+  drop_solo(lat);  // its inlet buffers were sized for the old inlet
   lat->inlet_valid = 0;  // draws depend on the thresholds
   return LGX_OK;
 }
@@ -451,6 +486,7 @@ int lgx_attach_field(lgx_lattice* lat, size_t bx, size_t by) {
     return LGX_ERR_ARG;
   }
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  drop_solo(lat);  // its block tables were laid out for the old field
   cudaFree(lat->field);
   cudaFree(lat->sums);
   cudaFree(lat->vort);  // sized for the old block grid
@@ -532,6 +568,18 @@ int lgx_advance(lgx_lattice* lat, uint64_t n) { return lgx_advance_sampling(lat,
 int lgx_advance_sampling(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
   int rc = check_lat(lat);
   if (rc) return rc;
+  int mode = lat->step_mode;
+  if (mode == LGX_STEP_AUTO && n > 0) {
+    rc = resolve_auto(lat);
+    if (rc) return rc;
+    mode = lat->auto_mode;
+  }
+  if (mode == LGX_STEP_GRAPH && n >= kGraphMinSteps && (every == 0 || every >= kGraphMinEvery)) {
+    rc = advance_graph(lat, n, every, alpha);
+    if (rc == LGX_OK || lat->step_mode == LGX_STEP_GRAPH) return rc;
+    // AUTO: no one-lattice batch here (e.g. no memory for it); one launch per step
+    cudaGetLastError();
+  }
   rc = enqueue_steps(lat, n, every, alpha);
   if (rc) return rc;
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
@@ -540,7 +588,7 @@ int lgx_advance_sampling(lgx_lattice* lat, uint64_t n, uint64_t every, float alp
 
 int lgx_set_step_mode(lgx_lattice* lat, int mode) {
   if (!lat || (mode != LGX_STEP_AUTO && mode != LGX_STEP_SINGLE && mode != LGX_STEP_WAVE &&
-               mode != LGX_STEP_TEMPORAL)) {
+               mode != LGX_STEP_TEMPORAL && mode != LGX_STEP_GRAPH)) {
     lgx::set_error("lgx_set_step_mode: bad handle or mode");
     return LGX_ERR_ARG;
   }
@@ -566,6 +614,7 @@ int lgx_get_step_plan(lgx_lattice* lat, lgx_step_plan* out) {
   out->wave_us = lat->auto_us[3];
   out->temporal4_us = lat->auto_us[4];
   out->temporal8_us = lat->auto_us[5];
+  out->graph_us = lat->auto_us[6];
   return LGX_OK;
 }
 

@@ -174,12 +174,28 @@ float time_mode(lgx_lattice* t, int mode, uint32_t depth, float est_us) {
   k = std::min<uint64_t>(std::max<uint64_t>(k, 8), 512);
   k = (k + 7) / 8 * 8;
   float ms = 0;
-  if (lgx_advance(t, 8) || lgx_timing_mark(t, 0) || lgx_advance(t, k) || lgx_timing_mark(t, 1) ||
+  // GRAPH captures a graph per new interval length: a first run of k steps
+  // keeps that capture out of the timed one
+  if (lgx_advance(t, 8) || (mode == LGX_STEP_GRAPH && lgx_advance(t, k)) ||
+      lgx_timing_mark(t, 0) || lgx_advance(t, k) || lgx_timing_mark(t, 1) ||
       lgx_timing_elapsed(t, 0, 1, &ms)) {
     cudaGetLastError();
     return -1;
   }
   return ms * 1e3f / (float)k;
+}
+
+// Lattices up to one full wave of the single-step kernel's blocks (six
+// resident 256-word blocks per SM) are offered the one-lattice batch: below
+// that the GPU is not full, and one launch per step runs at the host's launch
+// rate rather than the kernel's.
+uint32_t graph_max_words(int device) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (uint32_t)sms * 6u * 256u;
 }
 
 }  // namespace
@@ -199,7 +215,7 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
   lgx_lattice* t = nullptr;
   int rc = lgx_create(w, h, rest ? 1 : 0, 0x7E57ull, &t);
   if (rc) return rc;
-  StepPlan p{LGX_STEP_SINGLE, 0, 1, 0, 0, 0, 0, 0, 0};
+  StepPlan p{LGX_STEP_SINGLE, 0, 1, 0, 0, 0, 0, 0, 0, 0};
   const float est = time_mode(t, LGX_STEP_SINGLE, 0, 0);
   for (uint32_t words : {1u, 2u}) {  // the single-step kernel's two shapes
     t->step_words = words;
@@ -216,6 +232,10 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
     const float t8 = time_mode(t, LGX_STEP_TEMPORAL, 8, p.single_us);
     p.temporal4_us = t4 > 0 ? t4 : 0;
     p.temporal8_us = t8 > 0 ? t8 : 0;
+  }
+  if (dm.total <= graph_max_words(device)) {
+    const float g = time_mode(t, LGX_STEP_GRAPH, 0, p.single_us);
+    p.graph_us = g > 0 ? g : 0;
   }
   lgx_destroy(t);
   if (p.single_us <= 0) {
@@ -236,6 +256,11 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
     best = p.temporal8_us;
     p.mode = LGX_STEP_TEMPORAL;
     p.depth = 8;
+  }
+  if (p.graph_us > 0 && p.graph_us < best) {
+    best = p.graph_us;
+    p.mode = LGX_STEP_GRAPH;
+    p.depth = 0;
   }
   std::lock_guard<std::mutex> g(g_mu);
   g_step_plans[key] = p;

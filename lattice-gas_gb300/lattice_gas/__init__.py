@@ -88,7 +88,7 @@ class StepPlan(C.Structure):
     _fields_ = [("mode", C.c_int), ("depth", C.c_uint32), ("words", C.c_uint32),
                 ("single_us", C.c_float), ("single1_us", C.c_float), ("single2_us", C.c_float),
                 ("wave_us", C.c_float), ("temporal4_us", C.c_float),
-                ("temporal8_us", C.c_float)]
+                ("temporal8_us", C.c_float), ("graph_us", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -332,7 +332,7 @@ class GpuLattice:
     def advance_sampling(self, n, sample_every, alpha):
         _check(lib().lgx_advance_sampling(self._h, int(n), int(sample_every), float(alpha)))
 
-    STEP_AUTO, STEP_SINGLE, STEP_WAVE, STEP_TEMPORAL = 0, 1, 2, 3
+    STEP_AUTO, STEP_SINGLE, STEP_WAVE, STEP_TEMPORAL, STEP_GRAPH = 0, 1, 2, 3, 4
 
     def set_step_mode(self, mode: int):
         _check(lib().lgx_set_step_mode(self._h, int(mode)))
