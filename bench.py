@@ -396,6 +396,17 @@ REFERENCE_MATRIX = [
 ]
 
 
+# The reference's host-side cases of the same file (benches/speed.rs:606-681) that
+# this engine runs on the device, with its M3 Pro figures in ns per call
+# (benches/baseline.txt:31-32, 41, 42); cells per call where it counts them.
+REFERENCE_HOST_ROWS = [
+    ("field/vorticity/2048x1280", 8909.5, 0),
+    ("field/mean-velocity/2048x1280", 4751.6, 0),
+    ("lattice/init-equilibrium/2048x1280", 17224694.4, 2048 * 1280),
+    ("transport/measure/64", 626022417.0, 0),
+]
+
+
 def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
     """Each case of the reference's GPU benchmark group through this engine's
     GpuLattice, set up as benches/speed.rs does (density 0.22, speed 0.4, 20x20 blocks,
@@ -454,10 +465,37 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
     for (name, ref), v in zip(REFERENCE_MATRIX, got):
         out.append({"case": name, "value": round(v, 2), "reference_m3pro_metal": round(ref / 1e3, 3),
                     "ratio": round(v * 1e3 / ref, 1)})
-    return {"unit": "Gcell/s", "cases": out,
+
+    def ns(body):  # rate() gives calls per ns for one unit per call
+        return 1.0 / rate(body, 1.0)
+
+    host = []
+    g = seeded(bw, bh)
+    g.attach_field(BLOCK, BLOCK)
+    g.advance_sampling(100, 5, 0.2)
+    times = [ns(lambda: g.vorticity()), ns(lambda: g.mean_velocity())]
+    g.close()
+    lat = LG.Lattice(bw, bh, D, (S, 0.0), 8, True, 16, SEED)
+    times.append(ns(lambda: lat.init_equilibrium()))
+    lat.close()
+    best = float("inf")
+    for _ in range(3):
+        t = time.perf_counter()
+        LG.transport_measure([D], rest=True, seed=SEED, size=64)
+        best = min(best, time.perf_counter() - t)
+    times.append(best * 1e9)
+    for (name, ref_ns, n), t in zip(REFERENCE_HOST_ROWS, times):
+        row = {"case": name, "ns_per_call": round(t, 1), "reference_m3pro_cpu_ns": ref_ns,
+               "ratio": round(ref_ns / t, 2)}
+        if n:
+            row["gcell_per_s"] = round(n / t, 2)
+        host.append(row)
+    return {"unit": "Gcell/s", "cases": out, "host_cases_on_device": host,
             "note": "the reference's own GPU cases (benches/speed.rs) on this engine, best of "
                     "%d samples of ~%.1f s; its M3 Pro Metal figures (benches/baseline.txt) are "
-                    "other hardware, for context" % (samples, sample_s)}
+                    "other hardware, for context. host_cases_on_device: its CPU cases that "
+                    "this engine runs on the device (ns per call, each call a launch and a "
+                    "read-back; ratio = reference time / this time)" % (samples, sample_s)}
 
 
 def bench_byte_path(LG, W, steps: int, cpu_rate):

@@ -130,19 +130,60 @@ __global__ void __launch_bounds__(256) lgx_vorticity_kernel(const float* __restr
 
 // Field::mean_velocity (src/render.rs:146-161): the f32 sums run in block
 // order, as the reference adds them, so one thread adds them all.
-__global__ void lgx_mean_velocity_kernel(const float* __restrict__ ux,
-                                         const float* __restrict__ uy,
-                                         const float* __restrict__ sol, uint32_t nb,
-                                         float* __restrict__ out) {
-  float sx = 0.0f, sy = 0.0f, n = 0.0f;
-  for (uint32_t k = 0; k < nb; ++k)
-    if (sol[k] < 0.5f) {
-      sx = __fadd_rn(sx, ux[k]);
-      sy = __fadd_rn(sy, uy[k]);
-      n = __fadd_rn(n, 1.0f);
+// Field::mean_velocity (src/render.rs:146-161): the f32 sums in block order,
+// as the reference adds them, so one thread adds.  The block stages a chunk at
+// a time in shared memory with all its threads, each non-solid block's
+// velocity as it is and each solid block's as -0.0: adding -0.0 leaves every
+// f32 unchanged in round-to-nearest (x + -0 = x, +0 + -0 = +0, -0 + -0 = -0),
+// so the adding thread's sums are the reference's with no test in its loop,
+// and it reads four values per shared load.  The reference's count n adds 1.0f
+// per non-solid block: the exact count up to 2^24, where it stops growing; the
+// block counts with a reduction and rounds the same way.
+constexpr uint32_t kMeanChunk = 4096;  // blocks per staged chunk (32 KB)
+
+__global__ void __launch_bounds__(1024) lgx_mean_velocity_kernel(
+    const float* __restrict__ ux, const float* __restrict__ uy, const float* __restrict__ sol,
+    uint32_t nb, float* __restrict__ out) {
+  __shared__ float4 s_ux[kMeanChunk / 4], s_uy[kMeanChunk / 4];
+  __shared__ unsigned long long s_count;
+  float* fx = reinterpret_cast<float*>(s_ux);
+  float* fy = reinterpret_cast<float*>(s_uy);
+  if (threadIdx.x == 0) s_count = 0;
+  float sx = 0.0f, sy = 0.0f;
+  uint32_t mine = 0;
+  for (uint32_t c0 = 0; c0 < nb; c0 += kMeanChunk) {
+    const uint32_t len = min(kMeanChunk, nb - c0);
+    const uint32_t padded = (len + 7) & ~7u;
+    for (uint32_t k = threadIdx.x; k < padded; k += blockDim.x) {
+      const bool fluid = k < len && sol[c0 + k] < 0.5f;
+      fx[k] = fluid ? ux[c0 + k] : -0.0f;
+      fy[k] = fluid ? uy[c0 + k] : -0.0f;
+      mine += fluid ? 1u : 0u;
     }
-  out[0] = n == 0.0f ? 0.0f : __fdiv_rn(sx, n);
-  out[1] = n == 0.0f ? 0.0f : __fdiv_rn(sy, n);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (uint32_t q = 0; q < padded / 4; q += 2) {
+        const float4 a0 = s_ux[q], a1 = s_ux[q + 1], b0 = s_uy[q], b1 = s_uy[q + 1];
+        sx = __fadd_rn(sx, a0.x); sy = __fadd_rn(sy, b0.x);
+        sx = __fadd_rn(sx, a0.y); sy = __fadd_rn(sy, b0.y);
+        sx = __fadd_rn(sx, a0.z); sy = __fadd_rn(sy, b0.z);
+        sx = __fadd_rn(sx, a0.w); sy = __fadd_rn(sy, b0.w);
+        sx = __fadd_rn(sx, a1.x); sy = __fadd_rn(sy, b1.x);
+        sx = __fadd_rn(sx, a1.y); sy = __fadd_rn(sy, b1.y);
+        sx = __fadd_rn(sx, a1.z); sy = __fadd_rn(sy, b1.z);
+        sx = __fadd_rn(sx, a1.w); sy = __fadd_rn(sy, b1.w);
+      }
+    }
+    __syncthreads();
+  }
+  atomicAdd(&s_count, (unsigned long long)mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned long long c = s_count;
+    const float n = c <= (1ull << 24) ? (float)c : 16777216.0f;
+    out[0] = n == 0.0f ? 0.0f : __fdiv_rn(sx, n);
+    out[1] = n == 0.0f ? 0.0f : __fdiv_rn(sy, n);
+  }
 }
 
 cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
@@ -156,7 +197,7 @@ cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint3
 }
 
 cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cudaStream_t st) {
-  lgx_mean_velocity_kernel<<<1, 1, 0, st>>>(field, field + nb, field + 3 * nb, nb, out);
+  lgx_mean_velocity_kernel<<<1, 1024, 0, st>>>(field, field + nb, field + 3 * nb, nb, out);
   return cudaGetLastError();
 }
 

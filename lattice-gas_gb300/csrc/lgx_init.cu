@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "lgx_internal.hpp"
@@ -212,6 +213,33 @@ __global__ void __launch_bounds__(kThreads) lgx_fill_sample_kernel(const FillArg
   }
 }
 
+// The jump matrices M^(2^i), i < kFillJumps, on the current device: built and
+// copied once per device for the process (24 KB).
+cudaError_t device_jumps(const uint64_t** out) {
+  static std::mutex mu;
+  static const uint64_t* table[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(mu);
+  if (!table[dev]) {
+    std::vector<uint64_t> jumps = build_jumps();
+    jumps.resize((size_t)kFillJumps * 64);
+    void* p = nullptr;
+    e = cudaMalloc(&p, jumps.size() * sizeof(uint64_t));
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(p, jumps.data(), jumps.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return e;
+    }
+    table[dev] = (const uint64_t*)p;
+  }
+  *out = table[dev];
+  return cudaSuccess;
+}
+
 }  // namespace
 
 cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st) {
@@ -232,21 +260,15 @@ cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st) {
   const uint32_t grid = (uint32_t)((p.nseg + p.per_block - 1) / p.per_block);
   p.s0 = rng_seed(f.seed);
 
-  std::vector<uint64_t> jumps = build_jumps();
-  jumps.resize((size_t)kFillJumps * 64);
-  void* scratch = nullptr;
-  const size_t jbytes = jumps.size() * sizeof(uint64_t);
-  cudaError_t e = cudaMallocAsync(&scratch, jbytes + (size_t)grid * 8u, st);
+  cudaError_t e = device_jumps(&p.jump);
   if (e != cudaSuccess) return e;
-  p.jump = (const uint64_t*)scratch;
-  p.blk = (unsigned long long*)((char*)scratch + jbytes);
-  e = cudaMemcpyAsync(scratch, jumps.data(), jbytes, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) {
-    lgx_fill_count_kernel<<<grid, kThreads, 0, st>>>(p);
-    lgx_fill_sample_kernel<<<grid, kThreads, 0, st>>>(p);
-    e = cudaGetLastError();
-  }
-  // the pageable copy above has left the host vector before returning
+  void* scratch = nullptr;
+  e = cudaMallocAsync(&scratch, (size_t)grid * 8u, st);
+  if (e != cudaSuccess) return e;
+  p.blk = (unsigned long long*)scratch;
+  lgx_fill_count_kernel<<<grid, kThreads, 0, st>>>(p);
+  lgx_fill_sample_kernel<<<grid, kThreads, 0, st>>>(p);
+  e = cudaGetLastError();
   const cudaError_t e2 = cudaFreeAsync(scratch, st);
   return e != cudaSuccess ? e : e2;
 }
