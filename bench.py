@@ -407,6 +407,22 @@ REFERENCE_HOST_ROWS = [
 ]
 
 
+# The reference's CPU step cases (benches/speed.rs:409-476: the byte-per-cell
+# Lattice::step, one step per call) and its M3 Pro figures in Mcell/s
+# (benches/baseline.txt:13-20); this engine runs the same stream on the device.
+# (w, h, bands, rest, inlet columns, plate); tN is the reference's 12 threads.
+REFERENCE_CPU_STEP_ROWS = [
+    ("step/512x512/t1", 458.7, (512, 512, 1, True, 0, False)),
+    ("step/512x512/tN", 1505.6, (512, 512, 12, True, 0, False)),
+    ("step/512x512/t1/no-rest", 463.3, (512, 512, 1, False, 0, False)),
+    ("step/512x512/tN/plate", 1502.8, (512, 512, 12, True, 0, True)),
+    ("step/512x512/tN/inlet", 1290.9, (512, 512, 12, True, 8, False)),
+    ("step/2048x1280/t1", 248.4, (2048, 1280, 1, True, 0, False)),
+    ("step/2048x1280/tN", 1844.0, (2048, 1280, 12, True, 0, False)),
+    ("step/2048x64/tN", 1061.7, (2048, 64, 12, True, 0, False)),
+]
+
+
 def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
     """Each case of the reference's GPU benchmark group through this engine's
     GpuLattice, set up as benches/speed.rs does (density 0.22, speed 0.4, 20x20 blocks,
@@ -490,12 +506,31 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
         if n:
             row["gcell_per_s"] = round(n / t, 2)
         host.append(row)
+    steps = []
+    for name, ref, (w, h, bands, rest, inlet, plate) in REFERENCE_CPU_STEP_ROWS:
+        cells = np.zeros(w * h, np.uint8)
+        if plate:  # benches/speed.rs:334-341, the binary's plate scaled to the lattice
+            yc = np.float32(h) * LG.SQRT3_2 / np.float32(2.0)
+            size = np.float32(h) * np.float32(173.0) / np.float32(1280.0)
+            x0 = np.float32(w) / np.float32(5.0)
+            LG.add_box(cells, w, h, x0, x0 + np.float32(4.0), yc - size / np.float32(2.0),
+                       yc + size / np.float32(2.0))
+        lat = LG.Lattice(w, h, D, (S, 0.0), inlet, rest, bands, SEED)
+        lat.load(cells)
+        lat.init_equilibrium()
+        v = rate(lambda: lat.advance(1), w * h)
+        lat.close()
+        steps.append({"case": name, "value": round(v, 2), "reference_m3pro_cpu": round(ref / 1e3, 4),
+                      "ratio": round(v * 1e3 / ref, 1)})
     return {"unit": "Gcell/s", "cases": out, "host_cases_on_device": host,
+            "byte_step_cases_on_device": steps,
             "note": "the reference's own GPU cases (benches/speed.rs) on this engine, best of "
                     "%d samples of ~%.1f s; its M3 Pro Metal figures (benches/baseline.txt) are "
                     "other hardware, for context. host_cases_on_device: its CPU cases that "
                     "this engine runs on the device (ns per call, each call a launch and a "
-                    "read-back; ratio = reference time / this time)" % (samples, sample_s)}
+                    "read-back; ratio = reference time / this time). byte_step_cases_on_device: "
+                    "its CPU byte-per-cell step cases, the same random stream run by this "
+                    "engine's device byte path, one step and a wait per call" % (samples, sample_s)}
 
 
 def bench_byte_path(LG, W, steps: int, cpu_rate):
