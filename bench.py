@@ -458,6 +458,7 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
     out = []
     g = seeded(bw, bh)
     got = [rate(lambda: g.advance(1), bw * bh), rate(lambda: g.advance(100), bw * bh * 100)]
+    plan = g.step_plan
     g.close()
     g = seeded(256, 256)
     got.append(rate(lambda: g.advance(100), 256 * 256 * 100))
@@ -524,6 +525,8 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
                       "ratio": round(v * 1e3 / ref, 1)})
     return {"unit": "Gcell/s", "cases": out, "host_cases_on_device": host,
             "byte_step_cases_on_device": steps,
+            "step_plan_2048x1280": {k: (round(v, 3) if isinstance(v, float) else v)
+                                    for k, v in plan.items()},
             "note": "the reference's own GPU cases (benches/speed.rs) on this engine, best of "
                     "%d samples of ~%.1f s; its M3 Pro Metal figures (benches/baseline.txt) are "
                     "other hardware, for context. host_cases_on_device: its CPU cases that "
