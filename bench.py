@@ -404,6 +404,8 @@ REFERENCE_HOST_ROWS = [
     ("field/mean-velocity/2048x1280", 4751.6, 0),
     ("lattice/init-equilibrium/2048x1280", 17224694.4, 2048 * 1280),
     ("transport/measure/64", 626022417.0, 0),
+    ("lattice/total-particles/2048x1280", 44570.5, 2048 * 1280),
+    ("lattice/mean-velocity/2048x1280", 501249.2, 2048 * 1280),
 ]
 
 
@@ -501,6 +503,10 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
         LG.transport_measure([D], rest=True, seed=SEED, size=64)
         best = min(best, time.perf_counter() - t)
     times.append(best * 1e9)
+    lat = LG.Lattice(bw, bh, D, (S, 0.0), 0, True, 12, SEED)  # benches/speed.rs:334-346
+    lat.init_equilibrium()
+    times += [ns(lambda: lat.total_particles()), ns(lambda: lat.mean_velocity())]
+    lat.close()
     for (name, ref_ns, n), t in zip(REFERENCE_HOST_ROWS, times):
         row = {"case": name, "ns_per_call": round(t, 1), "reference_m3pro_cpu_ns": ref_ns,
                "ratio": round(ref_ns / t, 2)}

@@ -132,6 +132,12 @@ int lgx_field_vorticity(lgx_lattice *lat, float *w, size_t n_blocks);
 /* Field::mean_velocity (src/render.rs:146-161): the mean of the blocks whose solid
  * fraction is below one half, summed in block order as the reference does. */
 int lgx_field_mean_velocity(lgx_lattice *lat, float *ux, float *uy);
+/* Lattice::mean_velocity (src/lattice.rs:286-294) of this lattice's cells, on the
+ * device: momentum per particle over every site, obstacle sites included (the
+ * WITH_WALLS moments summed exactly, then Moments::velocity's f32 arithmetic).
+ * The reference applies it to a GpuLattice's cells after store
+ * (src/gpu.rs:1439-1446); here it needs no copy. */
+int lgx_mean_velocity(lgx_lattice *lat, float *ux, float *uy);
 /* New: the exact integer block sums (FLUID view, src/moments.rs:37-74) of the
  * most recent sample: mass, px2 (half units), py2 (units of sqrt(3)/2), and
  * the count of obstacle cells.  n_blocks must be bw*bh. */
@@ -374,6 +380,8 @@ int lgx_byte_read_field(lgx_byte_lattice *lat, float *ux, float *uy, float *rho,
                         size_t n_blocks);
 /* Lattice::total_particles (src/lattice.rs:299-312). */
 int lgx_byte_total_particles(lgx_byte_lattice *lat, uint64_t *out);
+/* Lattice::mean_velocity (src/lattice.rs:286-294), on the device. */
+int lgx_byte_mean_velocity(lgx_byte_lattice *lat, float *ux, float *uy);
 int lgx_byte_steps(lgx_byte_lattice *lat, uint64_t *out);
 
 /* ---- host-side lattice setup (src/lattice.rs, src/hex.rs) ---------------- */

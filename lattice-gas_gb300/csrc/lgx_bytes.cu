@@ -47,6 +47,7 @@
 
 #include "../../include/lgx.h"
 #include "lgx_internal.hpp"
+#include "lgx_reduce.cuh"
 #include "lgx_rng.cuh"
 
 namespace {
@@ -392,6 +393,51 @@ __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_co
   }
 }
 
+// The WITH_WALLS moments of byte cells, read 8 cells per 64-bit word: bit d of
+// every byte is counted by one popcount, and mass = sum, px2 and py2 weight the
+// six moving bits by CX2 and CY2 (src/hex.rs, src/moments.rs:37-74); bit 7,
+// the obstacle flag, is not a particle (src/lattice.rs:299-312).  out[0..2]:
+// mass, px2, py2 as 64-bit two's-complement sums.
+__global__ void __launch_bounds__(256) lgx_byte_moments_kernel(const uint8_t* __restrict__ cells,
+                                                               size_t n,
+                                                               unsigned long long* out) {
+  constexpr unsigned long long kBit0 = 0x0101010101010101ull;
+  long long mass = 0, px2 = 0, py2 = 0;
+  const uint64_t* w = reinterpret_cast<const uint64_t*>(cells);
+  const size_t nw = n / 8;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nw;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t x = __ldg(w + i);
+    int c[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) c[d] = __popcll(x & (kBit0 << d));
+    mass += c[0] + c[1] + c[2] + c[3] + c[4] + c[5] + c[6];
+    px2 += 2 * c[0] + c[1] - c[2] - 2 * c[3] - c[4] + c[5];
+    py2 += c[1] + c[2] - c[4] - c[5];
+  }
+  if (blockIdx.x == 0 && threadIdx.x < n - nw * 8) {  // the last n % 8 cells
+    const uint32_t x = cells[nw * 8 + threadIdx.x];
+    int c[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) c[d] = (x >> d) & 1u;
+    mass += c[0] + c[1] + c[2] + c[3] + c[4] + c[5] + c[6];
+    px2 += 2 * c[0] + c[1] - c[2] - 2 * c[3] - c[4] + c[5];
+    py2 += c[1] + c[2] - c[4] - c[5];
+  }
+  long long v[3] = {mass, px2, py2};
+  lgx::block_add<3>(v, out);
+}
+
+cudaError_t launch_byte_moments(const uint8_t* cells, size_t n, unsigned long long* out,
+                                cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  size_t blocks = (n / 8 + 255) / 256;
+  blocks = std::max<size_t>(1, std::min<size_t>(blocks, 152 * 2));
+  lgx_byte_moments_kernel<<<(unsigned)blocks, 256, 0, st>>>(cells, n, out);
+  return cudaGetLastError();
+}
+
 // Host: the padded collision table (src/collision.rs:161-188).
 void build_table(bool rest, std::vector<uint8_t>* data, uint32_t* stride) {
   static const int CX2[6] = {2, 1, -1, -2, -1, 1}, CY2[6] = {0, 1, 1, 0, -1, -1};
@@ -637,7 +683,7 @@ int lgx_byte_create(size_t w, size_t h, float density, float ux, float uy, size_
   if (e == cudaSuccess) e = cudaMalloc(&L->planes, total * 7 * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->solid, total * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->anysolid, ((total + 31) / 32) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&L->counter, 8);
+  if (e == cudaSuccess) e = cudaMalloc(&L->counter, 4 * 8);  // count, then the three moments
   if (e == cudaSuccess) e = cudaMemset(L->cells[0], 0, cells);
   if (e == cudaSuccess) e = cudaMemcpy(L->table, table.data(), table.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = ensure_step_attributes(L->device);
@@ -828,12 +874,31 @@ int lgx_byte_total_particles(lgx_byte_lattice* L, uint64_t* out) {
     return LGX_ERR_ARG;
   }
   LGX_CUDA(cudaSetDevice(L->device));
-  LGX_CUDA(lgx::launch_pack(L->cells[L->cur], L->dm, L->planes, L->solid, L->anysolid, L->stream));
-  LGX_CUDA(lgx::launch_count(L->planes, L->dm, L->counter, L->stream));
-  unsigned long long v = 0;
-  LGX_CUDA(cudaMemcpyAsync(&v, L->counter, 8, cudaMemcpyDeviceToHost, L->stream));
+  LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1, L->stream));
+  unsigned long long local = 0;
+  unsigned long long* v = lgx::host_result_words();
+  if (!v) v = &local;
+  LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 8, cudaMemcpyDeviceToHost, L->stream));
   LGX_CUDA(cudaStreamSynchronize(L->stream));
-  *out = v;
+  *out = *v;
+  return LGX_OK;
+}
+
+// Lattice::mean_velocity (src/lattice.rs:286-294): the WITH_WALLS moments of
+// every cell, then Moments::velocity.
+int lgx_byte_mean_velocity(lgx_byte_lattice* L, float* ux, float* uy) {
+  if (!L || !ux || !uy) {
+    lgx::set_error("null argument");
+    return LGX_ERR_ARG;
+  }
+  LGX_CUDA(cudaSetDevice(L->device));
+  LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1, L->stream));
+  unsigned long long local[3];
+  unsigned long long* v = lgx::host_result_words();
+  if (!v) v = local;
+  LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost, L->stream));
+  LGX_CUDA(cudaStreamSynchronize(L->stream));
+  lgx::moments_velocity((int64_t)v[0], (int64_t)v[1], (int64_t)v[2], ux, uy);
   return LGX_OK;
 }
 

@@ -5,6 +5,7 @@
 // field (sample_block in lgx_step_impl.cuh).
 #include "lgx_device.cuh"
 #include "lgx_internal.hpp"
+#include "lgx_reduce.cuh"
 #include "lgx_step_impl.cuh"
 
 namespace lgx {
@@ -35,8 +36,29 @@ __global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restri
     for (int d = 0; d < 7; ++d) c += __popc(__ldg(a + d * S + g) & m);
     acc += c;
   }
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-  if ((threadIdx.x & 31u) == 0 && acc) atomicAdd(out, acc);
+  long long v[1] = {(long long)acc};
+  block_add<1>(v, out);
+}
+
+// Lattice mass and momentum, obstacle sites included: per word the popcounts
+// of the seven planes weighted by CX2 and CY2 (src/hex.rs), summed exactly.
+__global__ void __launch_bounds__(256) lgx_moments_kernel(const uint32_t* __restrict__ a, Dims dm,
+                                                          unsigned long long* out) {
+  long long mass = 0, px2 = 0, py2 = 0;
+  const size_t S = dm.total;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < dm.total;
+       g += gridDim.x * blockDim.x) {
+    const uint32_t j = g % dm.wpr;
+    const uint32_t m = (j == dm.lastword) ? dm.tail : 0xffffffffu;
+    int c[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) c[d] = __popc(__ldg(a + d * S + g) & m);
+    mass += c[0] + c[1] + c[2] + c[3] + c[4] + c[5] + c[6];
+    px2 += 2 * c[0] + c[1] - c[2] - 2 * c[3] - c[4] + c[5];
+    py2 += c[1] + c[2] - c[4] - c[5];
+  }
+  long long v[3] = {mass, px2, py2};
+  block_add<3>(v, out);
 }
 
 // Bytes -> planes: one warp per lattice word; lane k reads column 32 j + k and
@@ -201,6 +223,16 @@ cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cu
   return cudaGetLastError();
 }
 
+cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long* out,
+                           cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  uint32_t blocks = (dm.total + 255) / 256;
+  if (blocks > 304) blocks = 304;  // two blocks per SM, grid-stride beyond
+  lgx_moments_kernel<<<blocks, 256, 0, st>>>(a, dm, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st) {
   const uint32_t nb = s.bw * s.bh;
   if (nb == 0) return cudaSuccess;
@@ -213,7 +245,7 @@ cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* 
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   uint32_t blocks = (dm.total + 255) / 256;
-  if (blocks > 1216) blocks = 1216;  // 152 SMs x 8 resident blocks, grid-stride beyond
+  if (blocks > 304) blocks = 304;  // two blocks per SM, grid-stride beyond
   lgx_count_kernel<<<blocks, 256, 0, st>>>(a, dm, out);
   return cudaGetLastError();
 }

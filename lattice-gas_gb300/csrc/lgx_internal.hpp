@@ -112,6 +112,17 @@ cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint3
 cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
                          cudaStream_t st);
+// The WITH_WALLS moments of every cell (src/moments.rs:37-74, 126-138): out[0..2] =
+// mass, px2, py2 as 64-bit two's-complement sums.
+cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long* out,
+                           cudaStream_t st);
+// Moments::velocity (src/moments.rs:91-97): momentum per particle in f32, (0, 0)
+// for no particles.
+void moments_velocity(int64_t mass, int64_t px2, int64_t py2, float* ux, float* uy);
+// Eight page-locked 64-bit words for this host thread, for results of a few
+// bytes read back by a call that synchronises before it returns (a copy to
+// pageable memory goes through a staging copy); null if none could be had.
+unsigned long long* host_result_words();
 // Byte cells (w*h, row-major) <-> planes + solid + anysolid.
 cudaError_t launch_pack(const uint8_t* cells, const Dims& dm, uint32_t* planes, uint32_t* solid,
                         uint32_t* anysolid, cudaStream_t st);

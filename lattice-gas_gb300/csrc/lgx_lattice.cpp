@@ -435,7 +435,8 @@ int lgx_create(size_t w, size_t h, int rest, uint64_t seed, lgx_lattice** out) {
   if (e == cudaSuccess) e = cudaMalloc(&lat->solid, total * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&lat->anysolid, ((total + 31) / 32) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&lat->cells, w * h);
-  if (e == cudaSuccess) e = cudaMalloc(&lat->counter, sizeof(unsigned long long));
+  // the particle count, then the three WITH_WALLS moments
+  if (e == cudaSuccess) e = cudaMalloc(&lat->counter, 4 * sizeof(unsigned long long));
   for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&lat->ev[i]);
   if (e == cudaSuccess) e = cudaMemsetAsync(lat->planes[0], 0, total * 7 * 4, lat->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(lat->planes[1], 0, total * 7 * 4, lat->stream);
@@ -701,7 +702,9 @@ int lgx_field_mean_velocity(lgx_lattice* lat, float* ux, float* uy) {
   const size_t nb = (size_t)lat->bw * lat->bh;
   LGX_CUDA(lgx::launch_mean_velocity(lat->field, (uint32_t)nb, d + nb, lat->stream));
   lat->launches += 1;
-  float v[2];
+  float local[2];
+  float* v = (float*)lgx::host_result_words();
+  if (!v) v = local;
   LGX_CUDA(cudaMemcpyAsync(v, d + nb, 8, cudaMemcpyDeviceToHost, lat->stream));
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
   *ux = v[0];
@@ -788,12 +791,33 @@ int lgx_total_particles(lgx_lattice* lat, uint64_t* out) {
     lgx::set_error("null output");
     return LGX_ERR_ARG;
   }
-  unsigned long long v = 0;
+  unsigned long long local = 0;
+  unsigned long long* v = lgx::host_result_words();
+  if (!v) v = &local;
   LGX_CUDA(lgx::launch_count(lat->planes[lat->cur], lat->dm, lat->counter, lat->stream));
   lat->launches += 1;
-  LGX_CUDA(cudaMemcpyAsync(&v, lat->counter, sizeof(v), cudaMemcpyDeviceToHost, lat->stream));
+  LGX_CUDA(cudaMemcpyAsync(v, lat->counter, sizeof(*v), cudaMemcpyDeviceToHost, lat->stream));
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
-  *out = v;
+  *out = *v;
+  return LGX_OK;
+}
+
+int lgx_mean_velocity(lgx_lattice* lat, float* ux, float* uy) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!ux || !uy) {
+    lgx::set_error("lgx_mean_velocity: null output");
+    return LGX_ERR_ARG;
+  }
+  unsigned long long local[3];
+  unsigned long long* v = lgx::host_result_words();
+  if (!v) v = local;
+  LGX_CUDA(lgx::launch_moments(lat->planes[lat->cur], lat->dm, lat->counter + 1, lat->stream));
+  lat->launches += 1;
+  LGX_CUDA(cudaMemcpyAsync(v, lat->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost,
+                           lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  lgx::moments_velocity((int64_t)v[0], (int64_t)v[1], (int64_t)v[2], ux, uy);
   return LGX_OK;
 }
 

@@ -9,6 +9,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <cuda_runtime.h>
+
 #include "../../include/lgx.h"
 #include "lgx_internal.hpp"
 
@@ -16,6 +18,37 @@ namespace lgx {
 namespace {
 
 constexpr float kSqrt3_2 = 0.8660254f;
+
+}  // namespace
+
+// Moments::velocity (src/moments.rs:91-97), in the reference's f32 order:
+// (px2 as f32 * 0.5) / m and (py2 as f32 * SQRT3_2) / m with m = mass as f32.
+void moments_velocity(int64_t mass, int64_t px2, int64_t py2, float* ux, float* uy) {
+  if (mass == 0) {
+    *ux = 0.0f;
+    *uy = 0.0f;
+    return;
+  }
+  const float m = (float)mass;
+  *ux = (float)px2 * 0.5f / m;
+  *uy = (float)py2 * kSqrt3_2 / m;
+}
+
+unsigned long long* host_result_words() {
+  thread_local unsigned long long* words = nullptr;
+  thread_local bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, 8 * sizeof(unsigned long long), cudaHostAllocPortable) == cudaSuccess)
+      words = (unsigned long long*)p;
+    else
+      cudaGetLastError();
+  }
+  return words;
+}
+
+namespace {
 constexpr float kCXF[6] = {1.0f, 0.5f, -0.5f, -1.0f, -0.5f, 0.5f};
 constexpr float kCYF[6] = {0.0f, kSqrt3_2, kSqrt3_2, 0.0f, -kSqrt3_2, -kSqrt3_2};
 constexpr uint8_t kSolid = 0x80;

@@ -140,6 +140,7 @@ def lib():
         _sig(L, "lgx_row_ux", vp, f32p, sz)
         _sig(L, "lgx_field_vorticity", vp, f32p, sz)
         _sig(L, "lgx_field_mean_velocity", vp, f32p, f32p)
+        _sig(L, "lgx_mean_velocity", vp, f32p, f32p)
         _sig(L, "lgx_column_uy", vp, f32p, sz)
         _sig(L, "lgx_line_sums", vp, i32p, sz, i32p, sz)
         _sig(L, "lgx_steps", vp, C.POINTER(C.c_uint64))
@@ -175,6 +176,7 @@ def lib():
         _sig(L, "lgx_byte_sample_field", vp, C.c_float)
         _sig(L, "lgx_byte_read_field", vp, f32p, f32p, f32p, f32p, sz)
         _sig(L, "lgx_byte_total_particles", vp, C.POINTER(C.c_uint64))
+        _sig(L, "lgx_byte_mean_velocity", vp, C.POINTER(C.c_float), C.POINTER(C.c_float))
         _sig(L, "lgx_byte_steps", vp, C.POINTER(C.c_uint64))
         _sig(L, "lgx_batch_create", C.POINTER(vp), sz, C.POINTER(vp))
         _sig(L, "lgx_batch_create_ex", C.POINTER(vp), sz, C.c_int, C.POINTER(vp))
@@ -291,6 +293,13 @@ class GpuLattice:
         """Field::mean_velocity (src/render.rs:146-161) of the attached field."""
         ux, uy = C.c_float(), C.c_float()
         _check(lib().lgx_field_mean_velocity(self._h, C.byref(ux), C.byref(uy)))
+        return np.float32(ux.value), np.float32(uy.value)
+
+    def lattice_mean_velocity(self):
+        """Lattice::mean_velocity (src/lattice.rs:286-294) of this lattice's cells: momentum
+        per particle over every site, obstacle sites included."""
+        ux, uy = C.c_float(), C.c_float()
+        _check(lib().lgx_mean_velocity(self._h, C.byref(ux), C.byref(uy)))
         return np.float32(ux.value), np.float32(uy.value)
 
     @property
@@ -457,6 +466,12 @@ class Lattice:
         v = C.c_uint64()
         _check(lib().lgx_byte_total_particles(self._h, C.byref(v)))
         return int(v.value)
+
+    def mean_velocity(self):
+        """Lattice::mean_velocity (src/lattice.rs:286-294), on the device."""
+        ux, uy = C.c_float(), C.c_float()
+        _check(lib().lgx_byte_mean_velocity(self._h, C.byref(ux), C.byref(uy)))
+        return np.float32(ux.value), np.float32(uy.value)
 
     @property
     def steps(self) -> int:

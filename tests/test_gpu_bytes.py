@@ -128,3 +128,26 @@ def test_full_size_fill_then_step_on_the_byte_path(LG, O):
     lat.advance(5)
     ref.advance(5)
     assert np.array_equal(lat.store(), ref.cells)
+
+
+@pytest.mark.parametrize("w,h,threads,inlet,rest", [(300, 64, 3, 40, True), (129, 18, 5, 8, False),
+                                                    (2048, 1280, 12, 8, True)])
+def test_lattice_mean_velocity_on_the_device(LG, O, w, h, threads, inlet, rest):
+    """Lattice::mean_velocity (src/lattice.rs:286-294) of the device byte lattice and of
+    a bitplane lattice holding the same cells equals the oracle's, bit for bit; an
+    empty lattice gives (0, 0)."""
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, w / 3.0, h * 0.4, min(w, h) / 6.0)
+    LG.init_equilibrium(cells, 0.3, 0.15, 0.05, rest, 7 + w)
+    lat = LG.Lattice(w, h, 0.3, (0.15, 0.0), inlet, rest, threads, 11)
+    lat.load(cells)
+    lat.advance(17)
+    ref = O.Lattice(w, h, 0.3, (0.15, 0.0), inlet, rest, threads, 11)
+    ref.set_cells(lat.store())
+    want = [np.float32(v).view(np.uint32) for v in ref.mean_velocity()]
+    assert [np.float32(v).view(np.uint32) for v in lat.mean_velocity()] == want
+    g = LG.GpuLattice(w, h, rest, 3)
+    g.load(lat.store())
+    assert [np.float32(v).view(np.uint32) for v in g.lattice_mean_velocity()] == want
+    g.load(np.zeros(w * h, np.uint8))
+    assert g.lattice_mean_velocity() == (0.0, 0.0)
