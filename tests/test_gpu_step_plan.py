@@ -23,8 +23,12 @@ def test_auto_picks_the_fastest_timed_mode(LG, w, h):
     chosen = {1: p["single_us"], 2: p["wave_us"],
               3: p["temporal4_us"] if p["depth"] == 4 else p["temporal8_us"],
               4: p["graph_us"]}[p["mode"]]
-    assert chosen == min(t for t in (p["single_us"], p["wave_us"], p["temporal4_us"],
-                                     p["temporal8_us"], p["graph_us"]) if t > 0)
+    others = min(t for t in (p["single_us"], p["wave_us"], p["temporal4_us"],
+                             p["temporal8_us"]) if t > 0)
+    if p["mode"] == 4:  # graph replays win ties within 5%
+        assert chosen < 1.05 * others
+    else:
+        assert chosen == others and not (0 < p["graph_us"] < 1.05 * others)
     assert g.step_plan == p  # cached for the size class
 
 
