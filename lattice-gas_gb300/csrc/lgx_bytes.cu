@@ -533,6 +533,7 @@ struct lgx_byte_lattice {
   uint32_t* solid = nullptr;
   uint32_t* anysolid = nullptr;
   unsigned long long* counter = nullptr;
+  unsigned long long* fill_scratch = nullptr;  // the equilibrium fill's block counts
   bool has_field = false;
   uint32_t bx = 0, by = 0, bw = 0, bh = 0;
   float* field = nullptr;
@@ -556,7 +557,7 @@ void free_bytes(lgx_byte_lattice* L) {
   cudaSetDevice(L->device);
   if (L->stream) cudaStreamSynchronize(L->stream);
   void* ptrs[] = {L->cells[0], L->cells[1], L->table,    L->seg_poly, L->inlet_poly, L->planes,
-                  L->solid,    L->anysolid, L->counter, L->field,    L->sums};
+                  L->solid,    L->anysolid, L->counter, L->field,    L->sums, L->fill_scratch};
   for (void* p : ptrs) cudaFree(p);
   if (L->stream) cudaStreamDestroy(L->stream);
   delete L;
@@ -744,6 +745,8 @@ int lgx_byte_init_equilibrium(lgx_byte_lattice* L) {
   f.seed = L->seed ^ 0xA5A51234ull;
   f.rest = L->rest;
   memcpy(f.thresh, L->thresh, sizeof(f.thresh));
+  if (!L->fill_scratch) LGX_CUDA(cudaMalloc(&L->fill_scratch, lgx::kFillScratchBytes));
+  f.scratch = L->fill_scratch;
   LGX_CUDA(lgx::launch_equilibrium_fill(f, L->stream));
   LGX_CUDA(cudaStreamSynchronize(L->stream));
   return LGX_OK;

@@ -56,6 +56,7 @@ struct lgx_lattice {
   // lattice's stream; made at first use, dropped when the inlet or the field
   // (which a batch lays out when it is made) changes
   lgx_batch* solo = nullptr;
+  unsigned long long* fill_scratch = nullptr;  // the equilibrium fill's block counts
   uint32_t wave_grid = 0;    // co-resident CTAs; 0 until first used
   uint32_t* done = nullptr;  // [wave_grid] published step per CTA
   uint32_t* error = nullptr; // timeout flag
@@ -64,3 +65,8 @@ struct lgx_lattice {
   void* prof = nullptr;
   float* vort = nullptr;  // vorticity of the field, bw*bh, then the mean velocity (2)
 };
+
+// The equilibrium fill's scratch for this lattice, made at its first fill.
+inline cudaError_t ensure_fill_scratch(lgx_lattice* l) {
+  return l->fill_scratch ? cudaSuccess : cudaMalloc(&l->fill_scratch, lgx::kFillScratchBytes);
+}

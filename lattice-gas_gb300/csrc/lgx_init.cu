@@ -9,7 +9,8 @@
 // of walking the generator from the first cell.
 //
 // Cells are handled in words of 32 (a bitplane word, or 32 consecutive bytes),
-// 8 words per thread.  Two launches: the first counts the fluid cells of each
+// one word per thread, or 8 on fills large enough to give every SM several
+// blocks that way.  Two launches: the first counts the fluid cells of each
 // block's contiguous range of words; the second has each block add up the
 // counts of the blocks before it, then walk its range 256 segments at a time,
 // with a block-wide scan giving each thread the fluid cells before its segment.
@@ -26,13 +27,17 @@ namespace lgx {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr uint32_t kSegWords = 8;  // 32-cell words per thread
+constexpr uint32_t kSegWordsLarge = 8;  // 32-cell words per thread on large fills
+// Fills of fewer words than this take one word per thread: with eight, a
+// small lattice's few blocks run on a few SMs, each thread walking 256 cells.
+constexpr uint64_t kLargeFillWords = 152ull * 8 * 256 * kSegWordsLarge;
 constexpr int kFillJumps = 48;     // draw indices below 2^48
 
 struct FillArgs {
   EqFill f;
   uint64_t nwords;      // 32-cell words in cell order
-  uint64_t nseg;        // segments of kSegWords words
+  uint64_t nseg;        // segments of seg_words words
+  uint32_t seg_words;   // 32-cell words per thread
   uint64_t per_block;   // segments per block (a multiple of kThreads)
   uint64_t s0;          // generator state before the first draw
   unsigned long long* blk;  // fluid cells per block
@@ -69,8 +74,8 @@ __device__ __forceinline__ uint32_t fluid_mask(const FillArgs& p, uint64_t wd) {
 
 __device__ __forceinline__ uint32_t segment_count(const FillArgs& p, uint64_t seg) {
   uint32_t c = 0;
-  const uint64_t w0 = seg * kSegWords;
-  const uint64_t w1 = min(w0 + kSegWords, p.nwords);
+  const uint64_t w0 = seg * p.seg_words;
+  const uint64_t w1 = min(w0 + p.seg_words, p.nwords);
   for (uint64_t wd = w0; wd < w1; ++wd) c += __popc(fluid_mask(p, wd));
   return c;
 }
@@ -144,8 +149,8 @@ __global__ void __launch_bounds__(kThreads) lgx_fill_sample_kernel(const FillArg
     const uint32_t tile = block_scan(mine, &before, scan);
     if (seg < s1) {
       uint64_t st = jump_ahead(p.s0, (base + before) * per, jump);
-      const uint64_t w0 = seg * kSegWords;
-      const uint64_t w1 = min(w0 + kSegWords, p.nwords);
+      const uint64_t w0 = seg * p.seg_words;
+      const uint64_t w1 = min(w0 + p.seg_words, p.nwords);
       for (uint64_t wd = w0; wd < w1; ++wd) {
         uint32_t m = fluid_mask(p, wd);
         if (p.f.planes) {
@@ -252,7 +257,8 @@ cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st) {
   if (!f.planes && (reinterpret_cast<uintptr_t>(f.cells) & 15u)) return cudaErrorInvalidValue;
   if ((f.thresh_rows || f.thresh_cols) && (!f.planes || (f.thresh_rows && f.thresh_cols)))
     return cudaErrorInvalidValue;
-  p.nseg = (p.nwords + kSegWords - 1) / kSegWords;
+  p.seg_words = p.nwords >= kLargeFillWords ? kSegWordsLarge : 1u;
+  p.nseg = (p.nwords + p.seg_words - 1) / p.seg_words;
   // a few blocks per SM, each over a contiguous range of whole tiles
   const uint64_t tiles = (p.nseg + kThreads - 1) / kThreads;
   const uint64_t nblk = std::min<uint64_t>(tiles, 152u * 8u);
@@ -263,13 +269,17 @@ cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st) {
   cudaError_t e = device_jumps(&p.jump);
   if (e != cudaSuccess) return e;
   void* scratch = nullptr;
-  e = cudaMallocAsync(&scratch, (size_t)grid * 8u, st);
-  if (e != cudaSuccess) return e;
-  p.blk = (unsigned long long*)scratch;
+  if (f.scratch) {
+    p.blk = f.scratch;
+  } else {
+    e = cudaMallocAsync(&scratch, (size_t)grid * 8u, st);
+    if (e != cudaSuccess) return e;
+    p.blk = (unsigned long long*)scratch;
+  }
   lgx_fill_count_kernel<<<grid, kThreads, 0, st>>>(p);
   lgx_fill_sample_kernel<<<grid, kThreads, 0, st>>>(p);
   e = cudaGetLastError();
-  const cudaError_t e2 = cudaFreeAsync(scratch, st);
+  const cudaError_t e2 = scratch ? cudaFreeAsync(scratch, st) : cudaSuccess;
   return e != cudaSuccess ? e : e2;
 }
 

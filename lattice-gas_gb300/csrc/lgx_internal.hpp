@@ -152,7 +152,11 @@ struct EqFill {
   // in device memory, in place of `thresh`; at most one is set.
   const uint32_t* thresh_rows;
   const uint32_t* thresh_cols;
+  // Device scratch of kFillScratchBytes for the fill's per-block counts, kept by
+  // the caller across fills; null: allocated and freed around this fill.
+  unsigned long long* scratch;
 };
+constexpr size_t kFillScratchBytes = 152 * 8 * 8;  // one count per block, at most 1216 blocks
 cudaError_t launch_equilibrium_fill(const EqFill& f, cudaStream_t st);
 
 

@@ -99,6 +99,7 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->field);
   cudaFree(lat->sums);
   cudaFree(lat->prof);
+  cudaFree(lat->fill_scratch);
   cudaFree(lat->vort);
   cudaFree(lat->done);
   cudaFree(lat->error);
@@ -543,6 +544,8 @@ int lgx_init_equilibrium(lgx_lattice* lat, float density, float ux, float uy, ui
   f.seed = seed ^ 0xA5A51234ull;  // src/lattice.rs:198
   f.rest = lat->rest;
   lgx::equilibrium_thresholds(density, ux, uy, lat->rest, f.thresh);
+  LGX_CUDA(ensure_fill_scratch(lat));
+  f.scratch = lat->fill_scratch;
   LGX_CUDA(lgx::launch_equilibrium_fill(f, lat->stream));
   lat->launches += 2;
   LGX_CUDA(cudaStreamSynchronize(lat->stream));

@@ -156,6 +156,8 @@ int restart(Meas& m, uint64_t rep, lgx_lattice* l) {
     f.thresh_cols = m.d_thresh;
   else
     f.thresh_rows = m.d_thresh;
+  LGX_CUDA(ensure_fill_scratch(l));
+  f.scratch = l->fill_scratch;
   LGX_CUDA(lgx::launch_equilibrium_fill(f, l->stream));
   l->launches += 2;
   l->seed = s;
