@@ -376,7 +376,8 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     slot.owner = nullptr;
     slot.owner_cap = 0;
     const size_t cap = 2 * (size_t)total_blocks;
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&slot.owner, cap * 4, s->stream);
+    if (e == cudaSuccess)
+      e = cudaMallocFromPoolAsync((void**)&slot.owner, cap * 4, s->pool, s->stream);
     if (e == cudaSuccess) slot.owner_cap = cap;
   }
   std::vector<uint32_t*> owner(nch);
