@@ -110,6 +110,10 @@ def test_new_entry_points_refuse_bad_arguments(engine_lib):
     assert L.lgx_line_sums(None, None, 0, None, 0) == ARG
     assert L.lgx_init_equilibrium(None, 0.3, 0.0, 0.0, 1) == ARG
     assert L.lgx_byte_init_equilibrium(None) == ARG
+    fx, fy = C.c_float(), C.c_float()
+    assert L.lgx_mean_velocity(None, C.byref(fx), C.byref(fy)) == ARG
+    assert L.lgx_byte_mean_velocity(None, C.byref(fx), C.byref(fy)) == ARG
+    assert L.lgx_set_step_mode(None, 4) == ARG                    # LGX_STEP_GRAPH, no lattice
 
 
 @pytest.mark.skipif(_gpu_present(), reason="checks the no-device path")
