@@ -301,7 +301,22 @@ __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_co
   uint8_t* in = lut + kLutBytes;
   uint8_t* out = in + (p.rows + 2) * in_row_bytes(p.cols);
 
-  // rows y0-1 .. y0+R of the tile's columns, and the collision table, in flight together
+  // Launched with programmatic dependent launch: the collision table and the
+  // band generators' states depend on nothing the previous step writes, so
+  // they are under way while that step drains; its cells are read only after
+  // griddepcontrol.wait (the previous grid complete and its writes visible).
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  for (uint32_t i = tid; i < 32u * p.stride; i += nt) cp_async4(lut + i * 4, p.table + i * 4);
+  // the first 64 states of each band's generator
+  if (tid < nb) {
+    uint64_t x = rng_seed(p.base_seed ^ ((uint64_t)(b0 + tid + 1) << 32));
+    for (int j = 0; j < 64; ++j) {
+      states[tid * 64 + j] = x;
+      x = xorshift(x);
+    }
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  // rows y0-1 .. y0+R of the tile's columns, in flight together
   const uint32_t in_rows = R + 2;
   for (uint32_t r = 0; r < in_rows; ++r) {
     const uint32_t gy = wrap_row(y0 + r, p.h);
@@ -328,15 +343,6 @@ __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_co
         in[r * RB + (C - 1) * kSlot + 16 + len_last] = __ldg(row + (c0 + ncols == p.w ? 0 : c0 + ncols));
       else
         in[r * RB + 15] = __ldg(row + (c0 ? c0 - 1 : p.w - 1));
-    }
-  }
-  for (uint32_t i = tid; i < 32u * p.stride; i += nt) cp_async4(lut + i * 4, p.table + i * 4);
-  // the first 64 states of each band's generator
-  if (tid < nb) {
-    uint64_t x = rng_seed(p.base_seed ^ ((uint64_t)(b0 + tid + 1) << 32));
-    for (int j = 0; j < 64; ++j) {
-      states[tid * 64 + j] = x;
-      x = xorshift(x);
     }
   }
   // the inflow cells of the tile, into the output tile
@@ -794,8 +800,17 @@ int lgx_byte_advance(lgx_byte_lattice* L, uint64_t n) {
     for (int j = 0; j < 64; ++j, x = xorshift(x)) a.inlet_states[j] = x;
     memcpy(a.t, L->thresh, sizeof(a.t));
     a.rest = L->rest ? 1 : 0;
-    lgx_byte_step_kernel<<<L->tiles, L->block, L->smem, L->stream>>>(a);
-    LGX_CUDA(cudaGetLastError());
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(L->tiles);
+    cfg.blockDim = dim3(L->block);
+    cfg.dynamicSmemBytes = L->smem;
+    cfg.stream = L->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    LGX_CUDA(cudaLaunchKernelEx(&cfg, lgx_byte_step_kernel, a));
     L->cur ^= 1;
     L->steps += 1;
   }
