@@ -46,6 +46,8 @@ def test_golden_output_on_the_device(LG, O, case):
     assert O.fnv1a(fb) == int(g["field"], 16)
     assert O.invariants(cells) == (g["mass"], g["px"], g["py"])
     assert lat.total_particles() == g["mass"]
+    ux, uy = lat.mean_velocity()  # tests/golden.rs:130, 217: the record's six decimals
+    assert abs(ux - g["ux"]) < 5e-7 and abs(uy - g["uy"]) < 5e-7
     assert lat.steps == case["steps"]
 
 
