@@ -46,17 +46,30 @@ def peaks():
     return 6800.0, "fallback"
 
 
-# From the ncu metric capture summarised in profiles/step_wake_run_pipes.md
-# (the wake run's lgx_step_kernel, two chunks per warp, one launch = one step):
-# DRAM bytes read + written per launch (cold cache under ncu; the 18 MB of
-# planes stay in L2 between steps of a timed run), and the ALU-pipe warp
-# instructions per launch, which do not depend on timing.
+# Figures from ncu captures of the wake run's lgx_step_kernel (one launch = one
+# step): DRAM bytes read + written per launch (cold cache under ncu; the 18 MB of
+# planes stay in L2 between steps of a timed run) and the ALU-pipe warp
+# instructions per launch, which do not depend on timing; and, for the roofline
+# case, DRAM bytes per site-update from a 16384 x 8192 capture of the same kernel
+# (the full 32768 x 16384 case scales with its sites).  They hold for the kernel
+# sources they were captured from: STEP_SOURCES hashed to CAPTURED_SOURCES_SHA.
+# When the sources differ the line says "stale": true.
 STEP_TRAFFIC_BYTES = 8419072 + 0
 STEP_ALU_WARP_INSTR = 3455811
-# Roofline-case DRAM bytes per site-update, from the 16384 x 8192 capture of the
-# same kernel (118.8 MB read + 72.7 MB written for 134.2 M sites); the full
-# 32768 x 16384 case scales with its sites.
 BIG_DRAM_BYTES_PER_SITE = (118769408 + 72740864) / (16384 * 8192)
+STEP_SOURCES = ("lgx_step.cu", "lgx_step_impl.cuh", "lgx_device.cuh",
+                os.path.join("generated", "collide.cuh"))
+CAPTURED_SOURCES_SHA = "unrecorded"
+
+
+def step_sources_sha() -> str:
+    """sha256 (16 hex digits) over the step kernel's source files, in order."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in STEP_SOURCES:
+        with open(os.path.join(ROOT, "lattice-gas_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 class ClockSampler:
@@ -199,11 +212,30 @@ def cpu_bitplane_rate(wl, seconds: float, threads: int, chunk: int = 20):
     return wl.sites * steps / dt, steps, dt
 
 
+def wake_config(steps: int, world: int) -> dict:
+    """The headline workload's config, the same for both arms."""
+    return {"workload": "wake_run: 4096x2304 FHP-III, plate at x=512 of 1/8 channel height, "
+                        "8-column inflow u=0.2, density 0.3, walls at rows 0 and h-1; 20000 "
+                        "steps, 32x32 blocks every 100 steps",
+            "w": 4096, "h": 2304, "lattice_steps_per_bench_step": steps,
+            "sample_every": 100, "block": 32,
+            "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": "replicas x%d" % world}
+
+
 def run_reference(args, world, rank):
+    """The reference's CPU update on the host's cores.  Nothing of the engine is
+    loaded: the cells come from the oracle's restatement of the reference's setup
+    (add_solid, init_equilibrium) and the step is the oracle's Lattice::step."""
     if rank != 0:
         return 0
-    from lattice_gas import workloads as W
-    wl = W.wake_run(steps=args.lattice_steps)
+    from types import SimpleNamespace
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    w, h, every = 4096, 2304, 100
+    wl = SimpleNamespace(w=w, h=h, rest=True, seed=0x5EED, density=0.3, inflow=(0.2, 0.0),
+                         inlet_cols=8, block=32, sample_every=every, alpha=1.0, sites=w * h,
+                         steps=args.lattice_steps, cells=O.wake_run_cells(w, h, 0.3, 0.2, 0x5EED))
     threads = os.cpu_count() or 1
     # each bench step: a bounded sample of the run (~2 s of the host's cores)
     for _ in range(args.warmup):
@@ -217,20 +249,19 @@ def run_reference(args, world, rank):
         total_steps += n
         total_t += dt
     value = wl.sites * total_steps / total_t / 1e9
+    sample = ("%d lattice steps of the wake run in %d samples of ~2 s (a bounded sample of the "
+              "20000-step run; the metric is a rate), byte-per-cell Lattice::step restated in C "
+              "(oracle/), %d threads, 32x32 field sampled every 100 steps"
+              % (total_steps, args.steps, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * total_t / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "wake_run 4096x2304 FHP-III, plate + inflow + walls, 32x32 "
-                               "blocks every 100 steps", "w": wl.w, "h": wl.h,
-                   "lattice_steps_per_bench_step": "bounded sample (~2 s of CPU work)",
-                   "l2": "n/a (CPU)"},
+        "config": wake_config(args.lattice_steps, world),
+        "sample": sample,
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
-                         "kind": "port",
-                         "sample": "%d lattice steps of the wake run in %d samples of ~2 s, "
-                                   "byte-per-cell Lattice::step restated in C (oracle/), "
-                                   "%d threads" % (total_steps, args.steps, threads)},
+                         "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -425,13 +456,28 @@ REFERENCE_CPU_STEP_ROWS = [
 ]
 
 
-def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
+STEP_MODE_NAMES = {1: "single", 2: "wave", 3: "temporal", 4: "graph"}
+
+
+def plan_name(plan: dict) -> str:
+    """The step mode the tuner picked, as words."""
+    name = STEP_MODE_NAMES.get(plan["mode"], str(plan["mode"]))
+    if plan["mode"] == 1:
+        name += " (%d chunk%s per warp)" % (plan["words"], "s" if plan["words"] > 1 else "")
+    elif plan["mode"] == 3:
+        name += " k=%d" % plan["depth"]
+    return name
+
+
+def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 7):
     """Each case of the reference's GPU benchmark group through this engine's
     GpuLattice, set up as benches/speed.rs does (density 0.22, speed 0.4, 20x20 blocks,
-    seed 0x5EED, cells from Lattice::init_equilibrium) and timed its way
-    (benches/speed.rs:150-193): warm up, then the best of `samples` samples of about
-    `sample_s` seconds each. Every call waits for the device, as the reference's
-    submit-and-wait does. Throughput in Gcell/s (cell updates, or cells processed)."""
+    seed 0x5EED, cells from Lattice::init_equilibrium): warm up, then `samples`
+    samples of about `sample_s` seconds each; the value is the median sample, with the
+    best beside it (the reference reports its best, benches/speed.rs:150-193). Every
+    call waits for the device, as the reference's submit-and-wait does. Throughput in
+    Gcell/s (cell updates, or cells processed); step cases name the step mode the
+    tuner picked for the lattice."""
     D, S, BLOCK, SEED = 0.22, 0.4, 20, 0x5EED
 
     def seeded(w, h):
@@ -448,31 +494,37 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
             n += 1
         per = (time.perf_counter() - t0) / n
         iters = max(1, int(round(sample_s / per)))
-        best = float("inf")
+        ts = []
         for _ in range(samples):
             t = time.perf_counter()
             for _ in range(iters):
                 body()
-            best = min(best, (time.perf_counter() - t) / iters)
-        return cells_per_iter / best / 1e9
+            ts.append((time.perf_counter() - t) / iters)
+        return cells_per_iter / statistics.median(ts) / 1e9, cells_per_iter / min(ts) / 1e9
 
     bw, bh = 2048, 1280
     out = []
+    modes = []
     g = seeded(bw, bh)
     got = [rate(lambda: g.advance(1), bw * bh), rate(lambda: g.advance(100), bw * bh * 100)]
     plan = g.step_plan
+    modes += ["single (one step per call)", plan_name(plan)]
     g.close()
     g = seeded(256, 256)
     got.append(rate(lambda: g.advance(100), 256 * 256 * 100))
+    modes.append(plan_name(g.step_plan))
     g.close()
     g = seeded(4096, 2048)
     got.append(rate(lambda: g.advance(100), 4096 * 2048 * 100))
+    modes.append(plan_name(g.step_plan))
     g.close()
     g = seeded(bw, bh)
     g.set_inlet(8, D, (S, 0.0), True)
     got.append(rate(lambda: g.advance(100), bw * bh * 100))
+    modes.append(plan_name(g.step_plan))
     g.attach_field(BLOCK, BLOCK)
     got.append(rate(lambda: g.advance_sampling(100, 5, 0.2), bw * bh * 100))
+    modes.append(plan_name(g.step_plan) + ", sampling every 5")
     g.close()
     g = seeded(bw, bh)
     g.attach_field(BLOCK, BLOCK)
@@ -480,13 +532,17 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
     buf = np.zeros(bw * bh, np.uint8)
     got.append(rate(lambda: g.store(buf), bw * bh))
     got.append(rate(lambda: g.total_particles(), bw * bh))
+    modes += [None, None, None]
     g.close()
-    for (name, ref), v in zip(REFERENCE_MATRIX, got):
-        out.append({"case": name, "value": round(v, 2), "reference_m3pro_metal": round(ref / 1e3, 3),
-                    "ratio": round(v * 1e3 / ref, 1)})
+    for (name, ref), (v, best), mode in zip(REFERENCE_MATRIX, got, modes):
+        row = {"case": name, "value": round(v, 2), "best": round(best, 2),
+               "reference_m3pro_metal": round(ref / 1e3, 3), "ratio": round(v * 1e3 / ref, 1)}
+        if mode:
+            row["step_mode"] = mode
+        out.append(row)
 
-    def ns(body):  # rate() gives calls per ns for one unit per call
-        return 1.0 / rate(body, 1.0)
+    def ns(body):  # rate() gives calls per ns for one unit per call (median sample)
+        return 1.0 / rate(body, 1.0)[0]
 
     host = []
     g = seeded(bw, bh)
@@ -525,7 +581,7 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
         lat = LG.Lattice(w, h, D, (S, 0.0), inlet, rest, bands, SEED)
         lat.load(cells)
         lat.init_equilibrium()
-        v = rate(lambda: lat.advance(1), w * h)
+        v = rate(lambda: lat.advance(1), w * h)[0]
         lat.close()
         steps.append({"case": name, "value": round(v, 2), "reference_m3pro_cpu": round(ref / 1e3, 4),
                       "ratio": round(v * 1e3 / ref, 1)})
@@ -533,8 +589,8 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 5):
             "byte_step_cases_on_device": steps,
             "step_plan_2048x1280": {k: (round(v, 3) if isinstance(v, float) else v)
                                     for k, v in plan.items()},
-            "note": "the reference's own GPU cases (benches/speed.rs) on this engine, best of "
-                    "%d samples of ~%.1f s; its M3 Pro Metal figures (benches/baseline.txt) are "
+            "note": "the reference's own GPU cases (benches/speed.rs) on this engine, median "
+                    "of %d samples of ~%.1f s (best beside it); its M3 Pro Metal figures (benches/baseline.txt) are "
                     "other hardware, for context. host_cases_on_device: its CPU cases that "
                     "this engine runs on the device (ns per call, each call a launch and a "
                     "read-back; ratio = reference time / this time). byte_step_cases_on_device: "
@@ -760,6 +816,7 @@ def run_gb300(args, world, rank, local):
         byte_path = bench_byte_path(LG, W, 1000, rate if cpu else None)
         matrix = bench_reference_matrix(LG)
     lop3_peak = LG.probe_int_rate(0)
+    src_sha = step_sources_sha()
     alu_achieved = STEP_ALU_WARP_INSTR * 32 / (step_ms * 1e-3)
 
     if rank != 0:
@@ -770,16 +827,15 @@ def run_gb300(args, world, rank, local):
         "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32 bitplanes (integer)",
         "data": "synthetic (seeded wake-run lattice built with the reference's primitives)",
-        "config": {"workload": "wake_run: 4096x2304 FHP-III, plate at x=512 of 1/8 channel "
-                               "height, 8-column inflow u=0.2, density 0.3, walls at rows 0 and "
-                               "h-1; 20000 steps, 32x32 blocks every 100 steps",
-                   "w": wl.w, "h": wl.h, "lattice_steps_per_bench_step": wl.steps,
-                   "sample_every": wl.sample_every, "block": wl.block,
-                   "l2": "flushed between timed steps (256 MiB write)",
-                   "parallelism": "replicas x%d" % world},
+        "config": wake_config(wl.steps, world),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": STEP_TRAFFIC_BYTES, "peak_kind": peak_kind,
+                     "ncu_figures": {"sources_sha": src_sha,
+                                     "captured_from_sha": CAPTURED_SOURCES_SHA,
+                                     "stale": src_sha != CAPTURED_SOURCES_SHA,
+                                     "covers": "traffic, int_pipe.alu_warp_instr_per_launch, "
+                                               "roofline_case.single.dram_GBps_from_ncu"},
                      "kernel": "lgx_step_kernel", "step_kernel_us": round(step_ms * 1e3, 3),
                      "algorithmic_bytes_per_launch": wl.sites * ALGO_BYTES_PER_SITE,
                      "note": "the step is integer-ALU bound, not HBM bound: see int_pipe",
@@ -821,7 +877,7 @@ def main():
     ap.add_argument("--sweep-steps", type=int, default=5000)
     ap.add_argument("--requests", type=int, default=256)
     ap.add_argument("--budget-mib", type=int, default=16384)
-    ap.add_argument("--big-steps", type=int, default=96)
+    ap.add_argument("--big-steps", type=int, default=2000)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

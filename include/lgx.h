@@ -185,18 +185,19 @@ int lgx_probe_int_rate(int op, double *ops_per_s);
 
 /* No counterpart in the reference.  One step of a lattice whose buffers the
  * caller owns, for callers that cannot let a library allocate device memory:
- * hosts that hand out every buffer from their own arena, work being recorded
- * into a CUDA graph (where cudaMalloc is not allowed), and loops that cannot
- * afford the synchronisation cudaMalloc/cudaFree imply.  Buffers, all device
- * memory: planes_in / planes_out hold 7 planes of ceil(w/32)*h words each,
- * plane-major, bit k of word y*ceil(w/32)+j being column 32j+k (planes_out
- * receives the step; it must not alias planes_in); solid has one plane of the
- * same shape, anysolid one bit per word of it (bit g%32 of word g/32 set when
- * solid word g is non-zero).  thresh are the inflow's seven 24-bit thresholds
+ * hosts that hand out every buffer from their own arena and treat any other
+ * allocation as a fault, and loops that cannot afford the synchronisation
+ * cudaMalloc/cudaFree imply.  Buffers, all device memory: planes_in /
+ * planes_out hold 7 planes of ceil(w/32)*h words each, plane-major, bit k of
+ * word y*ceil(w/32)+j being column 32j+k (planes_out receives the step; it
+ * must not alias planes_in); solid has one plane of the same shape, anysolid
+ * one bit per word of it (bit g%32 of word g/32 set when solid word g is
+ * non-zero).  thresh are the inflow's seven 24-bit thresholds
  * (lgx_equilibrium_thresholds), read only when inlet_cols > 0; seed and steps
- * (steps taken before this one) key the draws as lgx_advance does.  The work
- * is enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the
- * call returns without waiting.
+ * (steps taken before this one) key the draws as lgx_advance does.  w, h and
+ * inlet_cols above 2^32 - 1 are refused with LGX_ERR_ARG.  The work is
+ * enqueued on `stream` (a cudaStream_t, 0 for the default stream) and the call
+ * returns without waiting.
  *
  * The inflow's per-step draws, h * ceil(inlet_cols/32) * 7 words, go to one
  * scratch array of 262144 words (1 MiB) compiled into the library and held
@@ -205,8 +206,10 @@ int lgx_probe_int_rate(int op, double *ops_per_s);
  * before reading it, so calls whose work overlaps on the GPU (on different
  * streams, or on different host threads) race and must be ordered by the
  * caller.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture. */
+ * (cudaGetSymbolAddress) with that device current, and so does the first call
+ * after the device's context has been destroyed and made again (for instance
+ * by cudaDeviceReset), since the array may then sit at another address; make
+ * that first call before any stream capture. */
 int lgx_step_planes_noalloc(const uint32_t *planes_in, uint32_t *planes_out,
                             const uint32_t *solid, const uint32_t *anysolid, size_t w, size_t h,
                             int rest_particles, size_t inlet_cols, const uint32_t thresh[7],

@@ -4,7 +4,7 @@
 // Inputs: seven planes n[0..6] (six directions, then rest), the fair bit s2,
 // one-hot selectors s3[0..2] and s5[0..4].  Output: seven planes o[0..6].
 // Semantics (class pick by selector) follow the reference's known-answer
-// specification, src/gpu.rs:799-817; classes come from src/collision.rs:152-159.
+// specification, src/gpu.rs:799-817; classes come from src/collision.rs:62-69.
 #pragma once
 #include <stdint.h>
 

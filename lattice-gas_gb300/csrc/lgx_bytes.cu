@@ -4,7 +4,7 @@
 // different random stream than its GPU bitplanes do: one xorshift64*
 // generator per band of rows (bands of ceil(h / threads) rows), one draw per
 // non-obstacle cell in row-major order, and a padded lookup table
-// (src/collision.rs:161-210); the inflow re-seed after each step draws from one
+// (src/collision.rs:72-119); the inflow re-seed after each step draws from one
 // serial generator (src/lattice.rs:270-285).  Its golden tests pin that stream
 // bit for bit.  This file runs the same stream on the device.
 //
@@ -444,7 +444,7 @@ cudaError_t launch_byte_moments(const uint8_t* cells, size_t n, unsigned long lo
   return cudaGetLastError();
 }
 
-// Host: the padded collision table (src/collision.rs:161-188).
+// Host: the padded collision table (src/collision.rs:72-98).
 void build_table(bool rest, std::vector<uint8_t>* data, uint32_t* stride) {
   static const int CX2[6] = {2, 1, -1, -2, -1, 1}, CY2[6] = {0, 1, 1, 0, -1, -1};
   const int n = rest ? 128 : 64;

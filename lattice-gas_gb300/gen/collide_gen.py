@@ -1,6 +1,6 @@
 """Collision-circuit generator: momentum classes -> LOP3-mapped CUDA.
 
-The FHP rule is not hand-written.  As in the reference (src/collision.rs:152-159
+The FHP rule is not hand-written.  As in the reference (src/collision.rs:62-69
 enumerates the classes; src/gpu.rs:46-139 turns them into a Boolean circuit),
 every cell state is grouped with the states of equal mass and momentum, and a
 collision replaces a state by the member of its class that a random selector
@@ -41,7 +41,7 @@ REST = 6
 
 
 # ---------------------------------------------------------------------------
-# The rule (src/collision.rs:126-159)
+# The rule (src/collision.rs:37-69)
 # ---------------------------------------------------------------------------
 
 def invariants(s: int):
@@ -634,7 +634,7 @@ HEADER = """// Generated by lattice-gas_gb300/gen/collide_gen.py -- do not edit.
 // Inputs: seven planes n[0..6] (six directions, then rest), the fair bit s2,
 // one-hot selectors s3[0..2] and s5[0..4].  Output: seven planes o[0..6].
 // Semantics (class pick by selector) follow the reference's known-answer
-// specification, src/gpu.rs:799-817; classes come from src/collision.rs:152-159.
+// specification, src/gpu.rs:799-817; classes come from src/collision.rs:62-69.
 #pragma once
 #include <stdint.h>
 

@@ -449,3 +449,71 @@ uint64_t lgo_bp_total_particles(const lgo_bp *g) {
 
 uint64_t lgo_bp_steps(const lgo_bp *g) { return g->steps; }
 const uint32_t *lgo_bp_planes(const lgo_bp *g) { return g->a; }
+
+/* GpuLattice::steps is a public field (gpu.rs:471); a lattice loaded from a run
+ * that has already taken `steps` steps continues that run's random stream. */
+void lgo_bp_set_steps(lgo_bp *g, uint64_t steps) { g->steps = steps; }
+
+typedef struct {
+    lgo_bp *g;
+    const uint32_t *P;
+    long r0, r1; /* rows r0 .. r1-1 of the lattice, taken mod h */
+} window_job;
+
+static void *window_worker(void *arg) {
+    window_job *j = (window_job *)arg;
+    lgo_bp *g = j->g;
+    long h = (long)g->h;
+    for (long r = j->r0; r < j->r1; ++r) {
+        uint32_t y = (uint32_t)(((r % h) + h) % h);
+        for (uint32_t x = 0; x < (uint32_t)g->wpr; ++x)
+            step_word(g->a, g->b, g->solid, g->anysolid, j->P, g->rest, y, x);
+    }
+    return NULL;
+}
+
+/* n steps of the rows y0 .. y1-1 only, exactly as n full steps would leave them.
+ * A row depends on rows y-1, y, y+1 of the step before, so step s of n updates the
+ * window widened by n-1-s rows on each side; rows outside it go stale and are never
+ * read by the rows that matter.  For checking a sub-window of a lattice too large to
+ * step whole on the host.  Requires y1 - y0 + 2n <= h. */
+void lgo_bp_advance_window(lgo_bp *g, uint64_t n, size_t y0, size_t y1) {
+    for (uint64_t s = 0; s < n; ++s) {
+        uint32_t P[18];
+        lgo_bp_params(g->w, g->h, g->seed, g->steps, g->inlet_cols, g->thresh, P);
+        long halo = (long)(n - 1 - s);
+        long r0 = (long)y0 - halo, r1 = (long)y1 + halo;
+        size_t nt = g->threads ? g->threads : 1;
+        if (nt > 256) nt = 256;
+        long rows = r1 - r0;
+        long band = (rows + (long)nt - 1) / (long)nt;
+        window_job jobs[256];
+        pthread_t tid[256];
+        size_t nj = 0;
+        for (long r = r0; r < r1; r += band)
+            jobs[nj++] = (window_job){g, P, r, r + band < r1 ? r + band : r1};
+        if (nj == 1) window_worker(&jobs[0]);
+        else {
+            for (size_t i = 0; i < nj; ++i) pthread_create(&tid[i], NULL, window_worker, &jobs[i]);
+            for (size_t i = 0; i < nj; ++i) pthread_join(tid[i], NULL);
+        }
+        uint32_t *t = g->a;
+        g->a = g->b;
+        g->b = t;
+        g->steps += 1;
+    }
+}
+
+/* The cells of rows y0 .. y1-1 (lgo_bp_store restricted to a band). */
+void lgo_bp_store_rows(const lgo_bp *g, size_t y0, size_t y1, uint8_t *cells) {
+    size_t w = g->w, wpr = g->wpr, total = g->total;
+    for (size_t y = y0; y < y1; ++y)
+        for (size_t x = 0; x < w; ++x) {
+            size_t word = y * wpr + x / 32;
+            uint32_t k = (uint32_t)(x % 32);
+            uint8_t c = 0;
+            for (int d = 0; d < 7; ++d) c |= (uint8_t)(((g->a[d * total + word] >> k) & 1u) << d);
+            c |= (uint8_t)(((g->solid[word] >> k) & 1u) << 7);
+            cells[(y - y0) * w + x] = c;
+        }
+}

@@ -33,10 +33,10 @@ uint8_t lgo_reverse(uint8_t state);                                  /* hex.rs:4
 void lgo_site_position(size_t x, size_t y, float *px, float *py);     /* hex.rs:52 */
 /* Classes in the reference's BTreeMap order; states ascending within each.
  * Writes class sizes to sizes[] and members back to back to members[].
- * Returns the number of classes (collision.rs:152-159). */
+ * Returns the number of classes (collision.rs:62-69). */
 int lgo_classes(int rest, int *sizes, uint8_t *members);
-int lgo_table_stride(int rest);                                       /* collision.rs:172 */
-uint8_t lgo_table_apply(int rest, uint8_t state, uint32_t rand);      /* collision.rs:205 */
+int lgo_table_stride(int rest);                                       /* collision.rs:110-113 */
+uint8_t lgo_table_apply(int rest, uint8_t state, uint32_t rand);      /* collision.rs:115-119 */
 
 /* ---- RNG (src/rng.rs) ---------------------------------------------------- */
 uint64_t lgo_rng_seed(uint64_t seed);                                 /* rng.rs:9-15 */
@@ -134,6 +134,13 @@ uint64_t lgo_bp_total_particles(const lgo_bp *g);
 uint64_t lgo_bp_steps(const lgo_bp *g);
 /* Raw planes (7 * wpr * h words, plane-major) for word-level comparisons. */
 const uint32_t *lgo_bp_planes(const lgo_bp *g);
+/* Set the step counter (GpuLattice::steps, a public field, gpu.rs:471). */
+void lgo_bp_set_steps(lgo_bp *g, uint64_t steps);
+/* n steps of rows y0 .. y1-1 only (the window widened by the steps left on each
+ * side, so those rows end exact); y1 - y0 + 2n <= h. */
+void lgo_bp_advance_window(lgo_bp *g, uint64_t n, size_t y0, size_t y1);
+/* Cells of rows y0 .. y1-1, (y1 - y0) * w bytes. */
+void lgo_bp_store_rows(const lgo_bp *g, size_t y0, size_t y1, uint8_t *cells);
 
 /* ---- transport.rs ------------------------------------------------------- */
 /* row_ux / column_uy (transport.rs:51-91) of byte cells. */

@@ -118,6 +118,9 @@ def lib():
         _sig(L, "lgo_bp_total_particles", C.c_uint64, C.c_void_p)
         _sig(L, "lgo_bp_steps", C.c_uint64, C.c_void_p)
         _sig(L, "lgo_bp_planes", u32p, C.c_void_p)
+        _sig(L, "lgo_bp_set_steps", None, C.c_void_p, C.c_uint64)
+        _sig(L, "lgo_bp_advance_window", None, C.c_void_p, C.c_uint64, sz, sz)
+        _sig(L, "lgo_bp_store_rows", None, C.c_void_p, sz, sz, u8p)
         _lib = L
         return L
 
@@ -347,6 +350,20 @@ class BitplaneLattice:
         p = lib().lgo_bp_planes(self._p)
         return np.ctypeslib.as_array(p, shape=(7 * wpr * self.h,)).copy()
 
+    def set_steps(self, steps):
+        """Continue the random stream of a run that has taken `steps` steps."""
+        lib().lgo_bp_set_steps(self._p, int(steps))
+
+    def advance_window(self, n, y0, y1):
+        """n steps, exact on rows y0 .. y1-1 only (see lgo_bp_advance_window)."""
+        assert y1 - y0 + 2 * n <= self.h
+        lib().lgo_bp_advance_window(self._p, int(n), int(y0), int(y1))
+
+    def store_rows(self, y0, y1) -> np.ndarray:
+        out = np.zeros((y1 - y0) * self.w, np.uint8)
+        lib().lgo_bp_store_rows(self._p, int(y0), int(y1), ptr(out, C.c_uint8))
+        return out
+
 
 def column_wave_cells(w, h, density, u0, uy_col, rest, rng_seed):
     """Transverse-wave start (src/transport.rs:237-251)."""
@@ -401,3 +418,22 @@ def field_mean_velocity(ux, uy, sol):
     lib().lgo_field_mean_velocity(ptr(a, C.c_float), ptr(b, C.c_float), ptr(c, C.c_float), a.size,
                                   C.byref(mx), C.byref(my))
     return np.float32(mx.value), np.float32(my.value)
+
+
+def wake_run_cells(w=4096, h=2304, density=0.3, speed=0.2, seed=0x5EED):
+    """The wake run's starting cells built with the oracle's own setup: a plate one
+    eighth of the channel height at x = w/8, four columns thick (src/main.rs:582-588,
+    add_solid with a box on site_position), walls as solid rows 0 and h-1, then
+    Lattice::init_equilibrium (src/lattice.rs:197-208).  The same cells as the
+    engine's workload builder makes, for the CPU arm that must not load the engine."""
+    F = np.float32
+    cells = np.zeros(w * h, np.uint8)
+    yc = F(h) * SQRT3_2 / F(2.0)
+    half = F(h) * SQRT3_2 / F(16.0)
+    x0 = F(w // 8)
+    lib().lgo_add_box(ptr(cells, C.c_uint8), w, h, x0, x0 + F(4.0), yc - half, yc + half, 0)
+    cells[:w] = SOLID_BIT
+    cells[(h - 1) * w:] = SOLID_BIT
+    lib().lgo_cells_init_equilibrium(ptr(cells, C.c_uint8), cells.size, density, speed, 0.0, 1,
+                                     seed & (2**64 - 1))
+    return cells

@@ -2,9 +2,9 @@
 
 Reads the GOLDEN table and the CASES list from the reference's
 tests/golden.rs (lines 68-74 and 141-147) as text and writes them as JSON.
-Run in a container where the reference is mounted:
+Run where a checkout of the reference is present, giving its golden.rs:
 
-    python tests/golden/extract_golden.py /root/reference/tests/golden.rs
+    python tests/golden/extract_golden.py <reference checkout>/tests/golden.rs
 """
 import json
 import os
@@ -41,4 +41,6 @@ def main(path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/tests/golden.rs")
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_golden.py <path to the reference's tests/golden.rs>")
+    main(sys.argv[1])

@@ -1,7 +1,7 @@
 """A fixed run of one workload, for profilers (ncu) to attach to.
 
-    python lattice-gas_gb300/lattice_gas/profile_run.py --case wake --steps 60
-    python lattice-gas_gb300/lattice_gas/profile_run.py --case big --steps 20 --mode 1
+    python tests/profile_run.py --case wake --steps 60
+    python tests/profile_run.py --case big --steps 20 --mode 1
 
 Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
@@ -19,7 +19,8 @@ import argparse
 import os
 import sys
 
-sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                "lattice-gas_gb300"))
 
 import lattice_gas as LG  # noqa: E402
 from lattice_gas import workloads as W  # noqa: E402

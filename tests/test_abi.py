@@ -114,6 +114,23 @@ def test_new_entry_points_refuse_bad_arguments(engine_lib):
     assert L.lgx_mean_velocity(None, C.byref(fx), C.byref(fy)) == ARG
     assert L.lgx_byte_mean_velocity(None, C.byref(fx), C.byref(fy)) == ARG
     assert L.lgx_set_step_mode(None, 4) == ARG                    # LGX_STEP_GRAPH, no lattice
+    # the allocation-free step refuses sizes beyond 32 bits before any arithmetic on them
+    # (the buffer arguments are never touched on this path)
+    nz = [C.c_void_p(0x1000 * (i + 1)) for i in range(4)]
+    th = np.zeros(7, np.uint32).ctypes.data_as(C.POINTER(C.c_uint32))
+    step = L.lgx_step_planes_noalloc
+    step.restype = C.c_int
+    step.argtypes = [C.c_void_p] * 4 + [C.c_size_t, C.c_size_t, C.c_int, C.c_size_t,
+                                        C.POINTER(C.c_uint32), C.c_uint64, C.c_uint64,
+                                        C.c_void_p]
+    for w, h, cols in ((2 ** 32 + 64, 64, 0), (64, 2 ** 32 + 64, 0), (64, 64, 2 ** 32 + 8),
+                       (2 ** 64 - 1, 64, 0)):
+        assert step(*nz, w, h, 1, cols, th, 1, 0, None) == ARG, (w, h, cols)
+        assert b"32 bits" in L.lgx_last_error()
+    for w, h in ((64, 63), (4, 64)):
+        assert step(*nz, w, h, 1, 0, th, 1, 0, None) == ARG, (w, h)
+    assert step(None, *nz[1:], 64, 64, 1, 0, th, 1, 0, None) == ARG
+    assert step(nz[0], nz[0], nz[2], nz[3], 64, 64, 1, 0, th, 1, 0, None) == ARG  # aliased
 
 
 @pytest.mark.skipif(_gpu_present(), reason="checks the no-device path")

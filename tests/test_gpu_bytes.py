@@ -77,6 +77,49 @@ def test_device_byte_path_matches_the_oracle(LG, O, w, h, threads, inlet, rest):
         assert np.array_equal(got, ref.cells), "differs in %d cells" % int((got != ref.cells).sum())
 
 
+@pytest.mark.parametrize("threads", [1, 3])
+def test_periodic_box_on_the_byte_path(LG, O, threads):
+    """The plain CPU-runnable case on the device byte stream: a 256 x 128 periodic
+    FHP-III box, no obstacle, every channel Bernoulli(0.25) (Lattice::new(256, 128,
+    0.25, (0, 0), 0, true, T, seed) and init_equilibrium, filled on the device), 500
+    steps at T = 1 and T = 3 thread bands.  The device's cells equal the oracle's
+    Lattice::step bit for bit; the 8 x 8 field and the exact integer block sums formed
+    on the device equal the oracle's; mass and momentum are conserved exactly."""
+    w, h, seed, bs = 256, 128, 0x5EED, 8
+    lat = LG.Lattice(w, h, 0.25, (0.0, 0.0), 0, True, threads, seed)
+    lat.load(np.zeros(w * h, np.uint8))
+    lat.init_equilibrium()
+    ref = O.Lattice(w, h, 0.25, (0.0, 0.0), 0, True, threads, seed)
+    ref.init_equilibrium()
+    start = lat.store()
+    assert np.array_equal(start, ref.cells)
+    assert (start & 0x80).sum() == 0 and (start & 0x7F).any()
+    before = O.invariants(start)
+    lat.advance(500)
+    ref.advance(500)
+    got = lat.store()
+    assert np.array_equal(got, ref.cells), "differs in %d cells" % int((got != ref.cells).sum())
+    assert O.invariants(got) == before
+    assert lat.total_particles() == before[0] and lat.steps == 500
+    lat.attach_field(bs, bs)
+    lat.sample_field(1.0)
+    f = lat.read_field()
+    want = O.Field(w, h, bs, bs)
+    want.sample(ref.cells, w, h, 1.0)
+    for a, b in zip((f.ux, f.uy, f.rho, f.solid), (want.ux, want.uy, want.rho, want.solid)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    g = LG.GpuLattice(w, h, True, seed)
+    g.attach_field(bs, bs)
+    g.load(got)
+    g.sample_field(1.0)
+    sums = g.read_block_sums()
+    for a, b in zip(sums, O.block_sums(ref.cells, w, h, bs, bs)):
+        assert np.array_equal(a, b)
+    assert tuple(int(s.sum(dtype=np.int64)) for s in sums[:3]) == before
+    g.close()
+    lat.close()
+
+
 def test_restart_and_thread_invariance_of_conserved_quantities(LG, O):
     """tests/golden.rs:262-297 on the device: closed box, 1/2/3/5/8 bands."""
     for rest in (False, True):

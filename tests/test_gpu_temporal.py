@@ -67,6 +67,52 @@ def test_temporal_matches_the_oracle(LG, O):
     assert np.array_equal(g.store(), o.store())
 
 
+def test_roofline_case_as_stated_against_the_oracle_on_a_band(LG, O):
+    """The roofline case as stated: 32768 x 16384, 200 circles, 8-column inflow,
+    2,000 steps.  Temporal blocking (k = 4 and 8) gives the single-step kernel's
+    lattice after 2,000 steps, every cell; and a 1024-row band containing obstacles
+    and the inflow equals the oracle's over the last 64 steps: the oracle takes the
+    device's whole lattice after 1,936 steps and steps only the band (widened by the
+    steps left), which is exact on the band (lgo_bp_advance_window)."""
+    import os
+    from lattice_gas import workloads as W
+    wl = W.roofline_case()
+    n, tail, y0, y1 = 2000, 64, 7680, 8704
+    assert (wl.cells[y0 * wl.w:y1 * wl.w] & 0x80).any()
+    finals = {}
+    for mode, k in ((1, 0), (3, 4), (3, 8)):
+        g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
+        g.set_step_mode(mode)
+        if k:
+            g.set_temporal_depth(k)
+        g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)
+        g.load(wl.cells)
+        if mode == 1:
+            g.advance(n - tail)
+            o = O.BitplaneLattice(wl.w, wl.h, True, wl.seed, max(1, min(16, os.cpu_count() or 1)))
+            o.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)
+            o.load(g.store())
+            o.set_steps(n - tail)
+            o.advance_window(tail, y0, y1)
+            g.advance(tail)
+            band = o.store_rows(y0, y1)
+            del o
+            got = g.store()
+            assert np.array_equal(got[y0 * wl.w:y1 * wl.w], band), \
+                "the band differs from the oracle in %d cells" % int(
+                    (got[y0 * wl.w:y1 * wl.w] != band).sum())
+        else:
+            g.advance(n)
+            got = g.store()
+        assert g.steps == n
+        finals[k] = got
+        g.close()
+    for k in (4, 8):
+        assert np.array_equal(finals[0], finals[k]), \
+            "temporal k=%d differs from single steps in %d cells" % (
+                k, int((finals[0] != finals[k]).sum()))
+
+
 def test_full_size_roofline_case_temporal_equals_single(LG):
     """32768 x 16384 with 200 circles and the inflow, 24 steps: blocked (k = 8)
     against single steps, compared through the exact block sums and count."""

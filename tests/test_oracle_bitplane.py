@@ -219,3 +219,25 @@ def test_step_parameters(O):
     seed32 = (0x1234_5678_9ABC_DEF0 ^ (7 * 0x9E3779B97F4A7C15)) & 0xFFFFFFFF
     assert list(P[:11]) == [4, 32, seed32, 3, 3, 0xF, 128, 2, 40, 64, 2]
     assert list(P[11:]) == list(th)
+
+
+@pytest.mark.parametrize("y0,y1", [(20, 44), (0, 16), (50, 64)])
+def test_a_window_stepped_alone_equals_the_whole_lattice(O, y0, y1):
+    """The windowed advance (the check of a band of a lattice too large to step whole
+    on the host) leaves the band exactly as full steps do, including bands that
+    touch the periodic edge rows, with an obstacle, an inflow and a continued step
+    count."""
+    w, h, n = 200, 64, 12
+    cells = O.init_equilibrium_cells(np.zeros(w * h, np.uint8), 0.3, 0.2, 0.0, True, 5)
+    O.lib().lgo_add_circle(O.ptr(cells, O.C.c_uint8), w, h, 90.0, 30.0, 9.0)
+    full = O.BitplaneLattice(w, h, True, 0xABCDEF, 3)
+    part = O.BitplaneLattice(w, h, True, 0xABCDEF, 3)
+    for g in (full, part):
+        g.set_inlet(40, 0.3, (0.2, 0.0), True)
+        g.load(cells)
+        g.set_steps(17)
+    full.advance(n)
+    part.advance_window(n, y0, y1)
+    assert full.steps == part.steps == 17 + n
+    assert np.array_equal(full.store()[y0 * w:y1 * w], part.store_rows(y0, y1))
+    assert not np.array_equal(full.store(), part.store())   # the rest went stale

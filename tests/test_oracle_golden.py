@@ -2,7 +2,7 @@
 
 Pins: tests/golden.rs:141-147 (five exact FNV-1a checksums of cells and
 field, exact mass/momentum), tests/golden.rs:207-297 (behaviour, determinism,
-thread-count invariance), src/collision.rs:216-240, src/moments.rs:147-211,
+thread-count invariance), src/collision.rs:127-151, src/moments.rs:147-211,
 src/lattice.rs:396-559.
 """
 import json
