@@ -433,6 +433,7 @@ REFERENCE_MATRIX = [
 REFERENCE_HOST_ROWS = [
     ("field/vorticity/2048x1280", 8909.5, 0),
     ("field/mean-velocity/2048x1280", 4751.6, 0),
+    ("field/vorticity+mean-velocity/2048x1280 (one call)", 8909.5 + 4751.6, 0),
     ("lattice/init-equilibrium/2048x1280", 17224694.4, 2048 * 1280),
     ("transport/measure/64", 626022417.0, 0),
     ("lattice/total-particles/2048x1280", 44570.5, 2048 * 1280),
@@ -548,7 +549,8 @@ def bench_reference_matrix(LG, sample_s: float = 0.1, samples: int = 7):
     g = seeded(bw, bh)
     g.attach_field(BLOCK, BLOCK)
     g.advance_sampling(100, 5, 0.2)
-    times = [ns(lambda: g.vorticity()), ns(lambda: g.mean_velocity())]
+    times = [ns(lambda: g.vorticity()), ns(lambda: g.mean_velocity()),
+             ns(lambda: g.field_analyses())]
     g.close()
     lat = LG.Lattice(bw, bh, D, (S, 0.0), 8, True, 16, SEED)
     times.append(ns(lambda: lat.init_equilibrium()))

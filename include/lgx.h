@@ -132,6 +132,11 @@ int lgx_field_vorticity(lgx_lattice *lat, float *w, size_t n_blocks);
 /* Field::mean_velocity (src/render.rs:146-161): the mean of the blocks whose solid
  * fraction is below one half, summed in block order as the reference does. */
 int lgx_field_mean_velocity(lgx_lattice *lat, float *ux, float *uy);
+/* Both of the above in one launch and one read-back, for a caller that wants the
+ * two per frame (the reference computes them one after the other on the host,
+ * src/render.rs:127-161): w gets n_blocks = bw*bh vorticity values and (ux, uy)
+ * the mean velocity; w may be null, or ux and uy both null, not all three. */
+int lgx_field_analyses(lgx_lattice *lat, float *w, size_t n_blocks, float *ux, float *uy);
 /* Lattice::mean_velocity (src/lattice.rs:286-294) of this lattice's cells, on the
  * device: momentum per particle over every site, obstacle sites included (the
  * WITH_WALLS moments summed exactly, then Moments::velocity's f32 arithmetic).

@@ -131,41 +131,40 @@ __global__ void lgx_verify_kernel(uint32_t* out, uint32_t n) {
 
 }  // namespace
 
-// Field::vorticity (src/render.rs:127-143): on the block grid, dv/dx by a
-// one-sided difference at the first and last column and a central one
-// between, du/dy central with the rows periodic; f32 operations one by one,
-// rounded to nearest, as the reference's Rust (which never fuses).
-__global__ void __launch_bounds__(256) lgx_vorticity_kernel(const float* __restrict__ ux,
-                                                            const float* __restrict__ uy,
-                                                            uint32_t bw, uint32_t bh, float dx,
-                                                            float dy, float* __restrict__ out) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= bw * bh) return;
+// Field::vorticity (src/render.rs:127-143) of block k: on the block grid, dv/dx by a
+// one-sided difference at the first and last column and a central one between,
+// du/dy central with the rows periodic; f32 operations one by one, rounded to
+// nearest, as the reference's Rust (which never fuses).
+__device__ __forceinline__ float vorticity_at(const float* __restrict__ ux,
+                                              const float* __restrict__ uy, uint32_t k,
+                                              uint32_t bw, uint32_t bh, float dx, float dy) {
   const uint32_t j = k / bw, i = k - j * bw;
   const uint32_t ip = min(i + 1u, bw - 1u), im = i ? i - 1u : 0u;
   const uint32_t jp = j + 1u < bh ? j + 1u : 0u, jm = j ? j - 1u : bh - 1u;
   const float dvdx = __fdiv_rn(__fsub_rn(uy[j * bw + ip], uy[j * bw + im]),
                                __fmul_rn(__uint2float_rn(ip - im), dx));
   const float dudy = __fdiv_rn(__fsub_rn(ux[jp * bw + i], ux[jm * bw + i]), __fmul_rn(2.0f, dy));
-  out[k] = __fsub_rn(dvdx, dudy);
+  return __fsub_rn(dvdx, dudy);
 }
 
-// Field::mean_velocity (src/render.rs:146-161): the f32 sums run in block
-// order, as the reference adds them, so one thread adds them all.
-// Field::mean_velocity (src/render.rs:146-161): the f32 sums in block order,
-// as the reference adds them, so one thread adds.  The block stages a chunk at
-// a time in shared memory with all its threads, each non-solid block's
-// velocity as it is and each solid block's as -0.0: adding -0.0 leaves every
-// f32 unchanged in round-to-nearest (x + -0 = x, +0 + -0 = +0, -0 + -0 = -0),
-// so the adding thread's sums are the reference's with no test in its loop,
-// and it reads four values per shared load.  The reference's count n adds 1.0f
-// per non-solid block: the exact count up to 2^24, where it stops growing; the
-// block counts with a reduction and rounds the same way.
+// Field::mean_velocity (src/render.rs:146-161) by one block: the f32 sums run in
+// block order, as the reference adds them, so one thread adds them all.  The
+// block stages a chunk at a time in shared memory with all its threads, each
+// non-solid block's velocity as it is and each solid block's (and the padding's)
+// as -0.0: adding -0.0 leaves every f32 unchanged in round-to-nearest
+// (x + -0 = x, +0 + -0 = +0, -0 + -0 = -0), so the adding thread's sums are the
+// reference's with no test in its loop.  The adding thread reads 32 values of
+// each sum ahead of the adds that use them (two register sets), so the dependent
+// chain of f32 adds, not the shared-memory latency, sets its pace.  The
+// reference's count n adds 1.0f per non-solid block: the exact count up to 2^24,
+// where it stops growing; the block counts with a reduction and rounds the same way.
 constexpr uint32_t kMeanChunk = 4096;  // blocks per staged chunk (32 KB)
+constexpr uint32_t kAnalysisThreads = 256;
 
-__global__ void __launch_bounds__(1024) lgx_mean_velocity_kernel(
-    const float* __restrict__ ux, const float* __restrict__ uy, const float* __restrict__ sol,
-    uint32_t nb, float* __restrict__ out) {
+__device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux,
+                                                    const float* __restrict__ uy,
+                                                    const float* __restrict__ sol, uint32_t nb,
+                                                    float* __restrict__ out) {
   __shared__ float4 s_ux[kMeanChunk / 4], s_uy[kMeanChunk / 4];
   __shared__ unsigned long long s_count;
   float* fx = reinterpret_cast<float*>(s_ux);
@@ -175,7 +174,7 @@ __global__ void __launch_bounds__(1024) lgx_mean_velocity_kernel(
   uint32_t mine = 0;
   for (uint32_t c0 = 0; c0 < nb; c0 += kMeanChunk) {
     const uint32_t len = min(kMeanChunk, nb - c0);
-    const uint32_t padded = (len + 7) & ~7u;
+    const uint32_t padded = (len + 31u) & ~31u;
     for (uint32_t k = threadIdx.x; k < padded; k += blockDim.x) {
       const bool fluid = k < len && sol[c0 + k] < 0.5f;
       fx[k] = fluid ? ux[c0 + k] : -0.0f;
@@ -184,16 +183,33 @@ __global__ void __launch_bounds__(1024) lgx_mean_velocity_kernel(
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (uint32_t q = 0; q < padded / 4; q += 2) {
-        const float4 a0 = s_ux[q], a1 = s_ux[q + 1], b0 = s_uy[q], b1 = s_uy[q + 1];
-        sx = __fadd_rn(sx, a0.x); sy = __fadd_rn(sy, b0.x);
-        sx = __fadd_rn(sx, a0.y); sy = __fadd_rn(sy, b0.y);
-        sx = __fadd_rn(sx, a0.z); sy = __fadd_rn(sy, b0.z);
-        sx = __fadd_rn(sx, a0.w); sy = __fadd_rn(sy, b0.w);
-        sx = __fadd_rn(sx, a1.x); sy = __fadd_rn(sy, b1.x);
-        sx = __fadd_rn(sx, a1.y); sy = __fadd_rn(sy, b1.y);
-        sx = __fadd_rn(sx, a1.z); sy = __fadd_rn(sy, b1.z);
-        sx = __fadd_rn(sx, a1.w); sy = __fadd_rn(sy, b1.w);
+      const uint32_t nq = padded / 4u;  // float4s per sum, a multiple of 8
+      float4 a[8], b[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        a[i] = s_ux[i];
+        b[i] = s_uy[i];
+      }
+      for (uint32_t q = 0; q < nq; q += 8u) {
+        const uint32_t qn = q + 8u < nq ? q + 8u : q;  // the last round rereads its own
+        float4 na[8], nb4[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          na[i] = s_ux[qn + i];
+          nb4[i] = s_uy[qn + i];
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          sx = __fadd_rn(sx, a[i].x); sy = __fadd_rn(sy, b[i].x);
+          sx = __fadd_rn(sx, a[i].y); sy = __fadd_rn(sy, b[i].y);
+          sx = __fadd_rn(sx, a[i].z); sy = __fadd_rn(sy, b[i].z);
+          sx = __fadd_rn(sx, a[i].w); sy = __fadd_rn(sy, b[i].w);
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          a[i] = na[i];
+          b[i] = nb4[i];
+        }
       }
     }
     __syncthreads();
@@ -208,18 +224,35 @@ __global__ void __launch_bounds__(1024) lgx_mean_velocity_kernel(
   }
 }
 
-cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
-                             uint32_t by, float* out, cudaStream_t st) {
-  const uint32_t nb = bw * bh;
-  if (nb == 0) return cudaSuccess;
-  const float dx = (float)bx;
-  const float dy = __fmul_rn_host((float)by, 0.8660254f);
-  lgx_vorticity_kernel<<<(nb + 255) / 256, 256, 0, st>>>(field, field + nb, bw, bh, dx, dy, out);
-  return cudaGetLastError();
+// The field analyses of one field in one launch: block 0 forms the mean velocity
+// when `mean` is set, the other blocks the vorticity (one thread per field block)
+// when `vort` is set.
+__global__ void __launch_bounds__(kAnalysisThreads) lgx_field_analyses_kernel(
+    const float* __restrict__ ux, const float* __restrict__ uy, const float* __restrict__ sol,
+    uint32_t bw, uint32_t bh, float dx, float dy, float* __restrict__ vort,
+    float* __restrict__ mean) {
+  uint32_t b = blockIdx.x;
+  if (mean) {
+    if (b == 0) {
+      mean_velocity_block(ux, uy, sol, bw * bh, mean);
+      return;
+    }
+    b -= 1u;
+  }
+  const uint32_t k = b * kAnalysisThreads + threadIdx.x;
+  if (vort && k < bw * bh) vort[k] = vorticity_at(ux, uy, k, bw, bh, dx, dy);
 }
 
-cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cudaStream_t st) {
-  lgx_mean_velocity_kernel<<<1, 1024, 0, st>>>(field, field + nb, field + 3 * nb, nb, out);
+cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
+                                  uint32_t by, float* vort, float* mean, cudaStream_t st) {
+  const uint32_t nb = bw * bh;
+  const uint32_t blocks = (mean ? 1u : 0u) + (vort ? (nb + kAnalysisThreads - 1u) /
+                                                         kAnalysisThreads : 0u);
+  if (blocks == 0) return cudaSuccess;
+  const float dx = (float)bx;
+  const float dy = __fmul_rn_host((float)by, 0.8660254f);
+  lgx_field_analyses_kernel<<<blocks, kAnalysisThreads, 0, st>>>(
+      field, field + nb, field + 3 * nb, bw, bh, dx, dy, vort, mean);
   return cudaGetLastError();
 }
 

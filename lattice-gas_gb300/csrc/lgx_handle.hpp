@@ -64,6 +64,7 @@ struct lgx_lattice {
   // [3][w] and the device copy of the profile descriptor, one allocation
   void* prof = nullptr;
   float* vort = nullptr;  // vorticity of the field, bw*bh, then the mean velocity (2)
+  float* vort_host = nullptr;  // page-locked copy of the same, for the read-back
 };
 
 // The equilibrium fill's scratch for this lattice, made at its first fill.

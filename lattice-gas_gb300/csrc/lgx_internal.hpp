@@ -106,10 +106,10 @@ void temporal_tiling(const Dims& dm, uint32_t k, TemporalArgs* t);  // k steps p
 cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaStream_t st);
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
 // Field::vorticity and Field::mean_velocity of a field laid out ux | uy | rho |
-// sol (bw * bh each); out: bw * bh floats, or (mean ux, mean uy).
-cudaError_t launch_vorticity(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
-                             uint32_t by, float* out, cudaStream_t st);
-cudaError_t launch_mean_velocity(const float* field, uint32_t nb, float* out, cudaStream_t st);
+// sol (bw * bh each), in one launch: vort gets bw * bh floats and mean (mean ux,
+// mean uy); either may be null.
+cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
+                                  uint32_t by, float* vort, float* mean, cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
                          cudaStream_t st);
 // The WITH_WALLS moments of every cell (src/moments.rs:37-74, 126-138): out[0..2] =

@@ -101,6 +101,7 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->prof);
   cudaFree(lat->fill_scratch);
   cudaFree(lat->vort);
+  if (lat->vort_host) cudaFreeHost(lat->vort_host);
   cudaFree(lat->done);
   cudaFree(lat->error);
   for (auto& e : lat->ev)
@@ -492,9 +493,11 @@ int lgx_attach_field(lgx_lattice* lat, size_t bx, size_t by) {
   cudaFree(lat->field);
   cudaFree(lat->sums);
   cudaFree(lat->vort);  // sized for the old block grid
+  if (lat->vort_host) cudaFreeHost(lat->vort_host);
   lat->field = nullptr;
   lat->sums = nullptr;
   lat->vort = nullptr;
+  lat->vort_host = nullptr;
   lat->has_field = false;
   lat->bx = (uint32_t)bx;
   lat->by = (uint32_t)by;
@@ -662,57 +665,85 @@ int lgx_read_field(lgx_lattice* lat, float* ux, float* uy, float* rho, float* so
   return LGX_OK;
 }
 
-// The vorticity / mean-velocity buffer of the attached field.
+// The vorticity / mean-velocity buffers of the attached field: on the device, and
+// page-locked on the host so that the read-back is one DMA copy.
 static int field_scratch(lgx_lattice* lat, float** out) {
   if (!lat->has_field) {
     lgx::set_error("no field attached to this lattice");
     return LGX_ERR_STATE;
   }
-  if (!lat->vort) LGX_CUDA(cudaMalloc(&lat->vort, ((size_t)lat->bw * lat->bh + 2) * 4));
+  const size_t bytes = ((size_t)lat->bw * lat->bh + 2) * 4;
+  if (!lat->vort) LGX_CUDA(cudaMalloc(&lat->vort, bytes));
+  if (!lat->vort_host) LGX_CUDA(cudaHostAlloc((void**)&lat->vort_host, bytes,
+                                              cudaHostAllocDefault));
   *out = lat->vort;
+  return LGX_OK;
+}
+
+// Field::vorticity and/or Field::mean_velocity of the attached field: one launch,
+// one copy back of what was asked for (the two sit side by side on the device).
+static int field_analyses(lgx_lattice* lat, float* w, float* mx, float* my) {
+  float* d = nullptr;
+  int rc = field_scratch(lat, &d);
+  if (rc) return rc;
+  const size_t nb = (size_t)lat->bw * lat->bh;
+  const bool mean = mx != nullptr;
+  LGX_CUDA(lgx::launch_field_analyses(lat->field, lat->bw, lat->bh, lat->bx, lat->by,
+                                      w ? d : nullptr, mean ? d + nb : nullptr, lat->stream));
+  lat->launches += 1;
+  const size_t first = w ? 0 : nb, count = (w ? nb : 0) + (mean ? 2 : 0);
+  LGX_CUDA(cudaMemcpyAsync(lat->vort_host + first, d + first, count * 4, cudaMemcpyDeviceToHost,
+                           lat->stream));
+  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  if (w) memcpy(w, lat->vort_host, nb * 4);
+  if (mean) {
+    *mx = lat->vort_host[nb];
+    *my = lat->vort_host[nb + 1];
+  }
   return LGX_OK;
 }
 
 int lgx_field_vorticity(lgx_lattice* lat, float* w, size_t n_blocks) {
   int rc = check_lat(lat);
   if (rc) return rc;
-  float* d = nullptr;
-  rc = field_scratch(lat, &d);
-  if (rc) return rc;
-  const size_t nb = (size_t)lat->bw * lat->bh;
-  if (!w || n_blocks != nb) {
+  if (!lat->has_field) {
+    lgx::set_error("no field attached to this lattice");
+    return LGX_ERR_STATE;
+  }
+  if (!w || n_blocks != (size_t)lat->bw * lat->bh) {
     lgx::set_error("lgx_field_vorticity: need one value per field block");
     return LGX_ERR_ARG;
   }
-  LGX_CUDA(lgx::launch_vorticity(lat->field, lat->bw, lat->bh, lat->bx, lat->by, d,
-                                 lat->stream));
-  lat->launches += 1;
-  LGX_CUDA(cudaMemcpyAsync(w, d, nb * 4, cudaMemcpyDeviceToHost, lat->stream));
-  LGX_CUDA(cudaStreamSynchronize(lat->stream));
-  return LGX_OK;
+  return field_analyses(lat, w, nullptr, nullptr);
 }
 
 int lgx_field_mean_velocity(lgx_lattice* lat, float* ux, float* uy) {
   int rc = check_lat(lat);
   if (rc) return rc;
-  float* d = nullptr;
-  rc = field_scratch(lat, &d);
-  if (rc) return rc;
   if (!ux || !uy) {
     lgx::set_error("lgx_field_mean_velocity: null output");
     return LGX_ERR_ARG;
   }
-  const size_t nb = (size_t)lat->bw * lat->bh;
-  LGX_CUDA(lgx::launch_mean_velocity(lat->field, (uint32_t)nb, d + nb, lat->stream));
-  lat->launches += 1;
-  float local[2];
-  float* v = (float*)lgx::host_result_words();
-  if (!v) v = local;
-  LGX_CUDA(cudaMemcpyAsync(v, d + nb, 8, cudaMemcpyDeviceToHost, lat->stream));
-  LGX_CUDA(cudaStreamSynchronize(lat->stream));
-  *ux = v[0];
-  *uy = v[1];
-  return LGX_OK;
+  return field_analyses(lat, nullptr, ux, uy);
+}
+
+int lgx_field_analyses(lgx_lattice* lat, float* w, size_t n_blocks, float* ux, float* uy) {
+  int rc = check_lat(lat);
+  if (rc) return rc;
+  if (!lat->has_field) {
+    lgx::set_error("no field attached to this lattice");
+    return LGX_ERR_STATE;
+  }
+  if (w && n_blocks != (size_t)lat->bw * lat->bh) {
+    lgx::set_error("lgx_field_analyses: need one vorticity value per field block");
+    return LGX_ERR_ARG;
+  }
+  if ((ux == nullptr) != (uy == nullptr) || (!w && !ux)) {
+    lgx::set_error("lgx_field_analyses: ask for the vorticity, the mean velocity (both "
+                   "components) or both");
+    return LGX_ERR_ARG;
+  }
+  return field_analyses(lat, w, ux, uy);
 }
 
 int lgx_read_block_sums(lgx_lattice* lat, int32_t* mass, int32_t* px2, int32_t* py2,

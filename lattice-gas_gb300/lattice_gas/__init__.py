@@ -140,6 +140,7 @@ def lib():
         _sig(L, "lgx_row_ux", vp, f32p, sz)
         _sig(L, "lgx_field_vorticity", vp, f32p, sz)
         _sig(L, "lgx_field_mean_velocity", vp, f32p, f32p)
+        _sig(L, "lgx_field_analyses", vp, f32p, sz, f32p, f32p)
         _sig(L, "lgx_mean_velocity", vp, f32p, f32p)
         _sig(L, "lgx_column_uy", vp, f32p, sz)
         _sig(L, "lgx_line_sums", vp, i32p, sz, i32p, sz)
@@ -294,6 +295,15 @@ class GpuLattice:
         ux, uy = C.c_float(), C.c_float()
         _check(lib().lgx_field_mean_velocity(self._h, C.byref(ux), C.byref(uy)))
         return np.float32(ux.value), np.float32(uy.value)
+
+    def field_analyses(self):
+        """Field::vorticity and Field::mean_velocity together: one launch, one read-back."""
+        bx, by, bw, bh = self._field
+        out = np.zeros(bw * bh, np.float32)
+        ux, uy = C.c_float(), C.c_float()
+        _check(lib().lgx_field_analyses(self._h, _p(out, C.c_float), out.size, C.byref(ux),
+                                        C.byref(uy)))
+        return out, (np.float32(ux.value), np.float32(uy.value))
 
     def lattice_mean_velocity(self):
         """Lattice::mean_velocity (src/lattice.rs:286-294) of this lattice's cells: momentum

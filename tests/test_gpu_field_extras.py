@@ -31,3 +31,24 @@ def test_vorticity_and_mean_velocity_match_the_oracle(LG, O, w, h, bx, by):
     wx, wy = O.field_mean_velocity(f.ux, f.uy, f.solid)
     assert np.float32(mx).view(np.uint32) == np.float32(wx).view(np.uint32)
     assert np.float32(my).view(np.uint32) == np.float32(wy).view(np.uint32)
+    vort2, (mx2, my2) = g.field_analyses()      # both in one launch
+    assert np.array_equal(vort2.view(np.uint32), got.view(np.uint32))
+    assert (np.float32(mx2).view(np.uint32), np.float32(my2).view(np.uint32)) == (
+        np.float32(mx).view(np.uint32), np.float32(my).view(np.uint32))
+
+
+def test_field_analyses_refuse_bad_requests(LG):
+    import ctypes as C
+    g = LG.GpuLattice(64, 32, True, 1)
+    L = LG.lib()
+    fx, fy = C.c_float(), C.c_float()
+    out = np.zeros(8, np.float32)               # the 4 x 2 blocks of a 16 x 16 field
+    p = out.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lgx_field_analyses(g.handle, p, 8, C.byref(fx), C.byref(fy)) == 4   # no field
+    g.attach_field(16, 16)
+    assert L.lgx_field_analyses(g.handle, p, 3, C.byref(fx), C.byref(fy)) == 1   # wrong count
+    assert L.lgx_field_analyses(g.handle, None, 0, None, None) == 1               # nothing asked
+    assert L.lgx_field_analyses(g.handle, None, 0, C.byref(fx), None) == 1        # half asked
+    assert L.lgx_field_analyses(g.handle, p, 8, None, None) == 0                  # vorticity only
+    assert L.lgx_field_analyses(g.handle, None, 0, C.byref(fx), C.byref(fy)) == 0
+    assert (fx.value, fy.value) == (0.0, 0.0)     # an empty lattice: no particles, zero field
