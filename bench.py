@@ -46,7 +46,8 @@ def peaks():
     return 6800.0, "fallback"
 
 
-# Figures from ncu captures of the wake run's lgx_step_kernel (one launch = one
+# Figures from ncu captures of the wake run's step kernel in the shape the tuner
+# picks there, four words per lane (lgx_step_lanes_kernel; one launch = one
 # step): DRAM bytes read + written per launch (cold cache under ncu; the 18 MB of
 # planes stay in L2 between steps of a timed run) and the ALU-pipe warp
 # instructions per launch, which do not depend on timing; and, for the roofline
@@ -54,12 +55,12 @@ def peaks():
 # (the full 32768 x 16384 case scales with its sites).  They hold for the kernel
 # sources they were captured from: STEP_SOURCES hashed to CAPTURED_SOURCES_SHA.
 # When the sources differ the line says "stale": true.
-STEP_TRAFFIC_BYTES = 8419072 + 0
-STEP_ALU_WARP_INSTR = 3455811
-BIG_DRAM_BYTES_PER_SITE = (118769408 + 72740864) / (16384 * 8192)
+STEP_TRAFFIC_BYTES = 9312512 + 0
+STEP_ALU_WARP_INSTR = 3001044
+BIG_DRAM_BYTES_PER_SITE = (125132288 + 74130048) / (16384 * 8192)
 STEP_SOURCES = ("lgx_step.cu", "lgx_step_impl.cuh", "lgx_device.cuh",
                 os.path.join("generated", "collide.cuh"))
-CAPTURED_SOURCES_SHA = "unrecorded"
+CAPTURED_SOURCES_SHA = "5c2b69e14b3be987"
 
 
 def step_sources_sha() -> str:
@@ -458,13 +459,19 @@ REFERENCE_CPU_STEP_ROWS = [
 
 
 STEP_MODE_NAMES = {1: "single", 2: "wave", 3: "temporal", 4: "graph"}
+SHAPE_NAMES = {1: "1 chunk per warp", 2: "2 chunks per warp", 3: "2 words per lane",
+               4: "4 words per lane"}
+STEP_KERNEL_NAMES = {1: "lgx_step_kernel (1 chunk per warp)",
+                     2: "lgx_step_kernel (2 chunks per warp)",
+                     3: "lgx_step_lanes_kernel (2 words per lane)",
+                     4: "lgx_step_lanes_kernel (4 words per lane)"}
 
 
 def plan_name(plan: dict) -> str:
     """The step mode the tuner picked, as words."""
     name = STEP_MODE_NAMES.get(plan["mode"], str(plan["mode"]))
     if plan["mode"] == 1:
-        name += " (%d chunk%s per warp)" % (plan["words"], "s" if plan["words"] > 1 else "")
+        name += " (%s)" % SHAPE_NAMES.get(plan["words"], str(plan["words"]))
     elif plan["mode"] == 3:
         name += " k=%d" % plan["depth"]
     return name
@@ -838,7 +845,8 @@ def run_gb300(args, world, rank, local):
                                      "stale": src_sha != CAPTURED_SOURCES_SHA,
                                      "covers": "traffic, int_pipe.alu_warp_instr_per_launch, "
                                                "roofline_case.single.dram_GBps_from_ncu"},
-                     "kernel": "lgx_step_kernel", "step_kernel_us": round(step_ms * 1e3, 3),
+                     "kernel": STEP_KERNEL_NAMES.get(g.step_plan["words"], "lgx_step_kernel"),
+                     "step_kernel_us": round(step_ms * 1e3, 3),
                      "algorithmic_bytes_per_launch": wl.sites * ALGO_BYTES_PER_SITE,
                      "note": "the step is integer-ALU bound, not HBM bound: see int_pipe",
                      "int_pipe": {"achieved": round(alu_achieved / 1e12, 2),

@@ -109,16 +109,31 @@ int lgx_set_step_mode(lgx_lattice *lat, int mode);
  * over HBM, the intermediate steps kept in registers (lattices at least 64
  * words wide; other runs, and steps up to a sampling point, go one at a time). */
 int lgx_set_temporal_depth(lgx_lattice *lat, int k);
+/* Pins the single-step kernel's shape (no counterpart in the reference, whose
+ * lgca_step has one, src/gpu.rs:203-310).  0: the step-mode tuner's choice (or,
+ * outside AUTO, by size).  1, 2: a word per lane, one or two 32-word chunks per
+ * warp.  3, 4: two or four consecutive words per lane in 64- or 128-bit loads
+ * and stores, for lattices whose words per row are a multiple of that count
+ * (otherwise the shape by size runs).  Results are identical in every shape. */
+enum {
+  LGX_SHAPE_AUTO = 0,
+  LGX_SHAPE_CHUNK1 = 1,
+  LGX_SHAPE_CHUNK2 = 2,
+  LGX_SHAPE_LANES2 = 3,
+  LGX_SHAPE_LANES4 = 4
+};
+int lgx_set_step_shape(lgx_lattice *lat, int shape);
 /* What AUTO resolves to for this lattice, and the tuner's times per step (0 where a
  * mode does not apply); tunes the size class now if it has not been. */
 typedef struct lgx_step_plan {
   int mode;
   uint32_t depth;
-  uint32_t words;          /* 32-word chunks per warp of the single-step kernel */
+  uint32_t words;          /* the single-step kernel's shape (LGX_SHAPE_*) */
   float single_us;         /* one launch per step, with that shape */
   float single1_us, single2_us;  /* one launch per step, one and two chunks per warp */
   float wave_us, temporal4_us, temporal8_us;
   float graph_us;          /* the one-lattice batch (GRAPH) */
+  float lanes2_us, lanes4_us;  /* one launch per step, two and four words per lane */
 } lgx_step_plan;
 int lgx_get_step_plan(lgx_lattice *lat, lgx_step_plan *out);
 /* GpuLattice::sample_field (src/gpu.rs:710-721). */

@@ -88,6 +88,40 @@ __global__ void __launch_bounds__(256 / WORDS, 4 * WORDS) lgx_batch_step_kernel(
   batch_block<RULE, WORDS>(p);
 }
 
+// The same step with two consecutive words per lane (128 threads, 64-bit plane
+// accesses; a block still covers 256 words, so the block tables are the
+// same).  A block of a lattice whose words per row are odd runs the two-chunk
+// mapping instead (the branch is uniform across the block).
+template <int RULE>
+__global__ void __launch_bounds__(128, 6) lgx_batch_lanes_kernel(BatchStepArgs p) {
+  const uint32_t blk = p.first_block + blockIdx.x;
+  const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
+  const LatDesc& d = p.descs[li];
+  if (d.dm.wpr & 1u) {
+    batch_block<RULE, 2>(p);
+    return;
+  }
+  uint32_t gq = (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 2u;
+  const bool live = gq < d.dm.total;
+  if (!live) gq = d.dm.total - 2u;
+  const uint64_t local = *p.base + p.k;
+  const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
+  Draws s[2];
+  s[0] = draws(gq ^ seed32);
+  s[1] = draws((gq + 1u) ^ seed32);
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
+  const uint32_t* src = par ? d.planes[1] : d.planes[0];
+  uint32_t* dst = par ? d.planes[0] : d.planes[1];
+  const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)p.k * d.dm.h * d.dm.iw * 7u : nullptr;
+  if (RULE == 2 ? d.rest != 0 : RULE == 1)
+    step_lane_words<true, 2, 2>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq, live);
+  else
+    step_lane_words<false, 2, 2>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
+                                 live);
+}
+
 // Inlet draws for steps base .. base + nsteps - 1 of every lattice with an
 // inlet: one thread per (lattice, step, row, inlet word).
 __global__ void __launch_bounds__(128) lgx_batch_inlet_kernel(BatchInletArgs p) {
@@ -149,16 +183,21 @@ __global__ void lgx_batch_owner_kernel(const uint32_t* block0, uint32_t nlat, ui
 
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st) {
-  if (words == 0) words = nblocks >= 152u * 8u ? 2 : 1;  // two chunks once a wave is full
+  if (words == 0) words = kBatchLanes2;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
-  cfg.blockDim = dim3(words == 2 ? 128 : 256);
+  cfg.blockDim = dim3(words == 1 ? 256 : 128);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (words == kBatchLanes2) {
+    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2>, a);
+    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1>, a);
+    return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0>, a);
+  }
   if (words == 2) {
     if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<2, 2>, a);
     if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<1, 2>, a);

@@ -148,55 +148,92 @@ __device__ __forceinline__ float vorticity_at(const float* __restrict__ ux,
 }
 
 // Field::mean_velocity (src/render.rs:146-161) by one block: the f32 sums run in
-// block order, as the reference adds them, so one thread adds them all.  The
-// block stages a chunk at a time in shared memory with all its threads, each
-// non-solid block's velocity as it is and each solid block's (and the padding's)
-// as -0.0: adding -0.0 leaves every f32 unchanged in round-to-nearest
-// (x + -0 = x, +0 + -0 = +0, -0 + -0 = -0), so the adding thread's sums are the
-// reference's with no test in its loop.  The adding thread reads 32 values of
-// each sum ahead of the adds that use them (two register sets), so the dependent
-// chain of f32 adds, not the shared-memory latency, sets its pace.  The
-// reference's count n adds 1.0f per non-solid block: the exact count up to 2^24,
-// where it stops growing; the block counts with a reduction and rounds the same way.
-constexpr uint32_t kMeanChunk = 4096;  // blocks per staged chunk (32 KB)
+// block order, as the reference adds them, so one thread (lane 0 of warp 0) adds
+// them all.  The other warps stage the field in chunks of kMeanChunk blocks into
+// two shared buffers: while the adding thread works through chunk c, they load
+// chunk c + 1, every load of a thread issued before any of its stores, so a
+// chunk costs one memory latency rather than one per row of threads.  Each
+// non-solid block's velocity is staged as it is and each solid block's (and
+// the padding's) as -0.0: adding -0.0 leaves every f32 unchanged in
+// round-to-nearest (x + -0 = x, +0 + -0 = +0, -0 + -0 = -0), so the adding
+// thread's sums are the reference's with no test in its loop.  It reads 32
+// values of each sum ahead of the adds that use them (two register sets), so
+// the dependent chain of f32 adds, not the shared-memory latency, sets its
+// pace.  The reference's count n adds 1.0f per non-solid block: the exact count
+// up to 2^24, where it stops growing; the block counts with a reduction and
+// rounds the same way.
+constexpr uint32_t kMeanChunk = 2048;  // blocks per staged chunk (8 KB per sum)
 constexpr uint32_t kAnalysisThreads = 256;
+constexpr uint32_t kStagers = kAnalysisThreads - 32;  // warps 1.. stage, warp 0 adds
+constexpr uint32_t kStagePer = (kMeanChunk + kStagers - 1) / kStagers;
+
+__device__ __forceinline__ uint32_t stage_chunk(const float* __restrict__ ux,
+                                                const float* __restrict__ uy,
+                                                const float* __restrict__ sol, uint32_t nb,
+                                                uint32_t c0, float* fx, float* fy) {
+  const uint32_t t = threadIdx.x - 32u;
+  float vx[kStagePer], vy[kStagePer];
+  uint32_t fluid = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < kStagePer; ++i) {
+    const uint32_t k = t + i * kStagers;
+    const bool in = k < kMeanChunk && c0 + k < nb;
+    const bool f = in && __ldg(sol + c0 + k) < 0.5f;
+    vx[i] = f ? __ldg(ux + c0 + k) : -0.0f;
+    vy[i] = f ? __ldg(uy + c0 + k) : -0.0f;
+    fluid += f ? 1u : 0u;
+  }
+#pragma unroll
+  for (uint32_t i = 0; i < kStagePer; ++i) {
+    const uint32_t k = t + i * kStagers;
+    if (k < kMeanChunk) {
+      fx[k] = vx[i];
+      fy[k] = vy[i];
+    }
+  }
+  return fluid;
+}
 
 __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux,
                                                     const float* __restrict__ uy,
                                                     const float* __restrict__ sol, uint32_t nb,
                                                     float* __restrict__ out) {
-  __shared__ float4 s_ux[kMeanChunk / 4], s_uy[kMeanChunk / 4];
+  __shared__ float4 s_ux[2][kMeanChunk / 4], s_uy[2][kMeanChunk / 4];
   __shared__ unsigned long long s_count;
-  float* fx = reinterpret_cast<float*>(s_ux);
-  float* fy = reinterpret_cast<float*>(s_uy);
   if (threadIdx.x == 0) s_count = 0;
   float sx = 0.0f, sy = 0.0f;
   uint32_t mine = 0;
-  for (uint32_t c0 = 0; c0 < nb; c0 += kMeanChunk) {
-    const uint32_t len = min(kMeanChunk, nb - c0);
-    const uint32_t padded = (len + 31u) & ~31u;
-    for (uint32_t k = threadIdx.x; k < padded; k += blockDim.x) {
-      const bool fluid = k < len && sol[c0 + k] < 0.5f;
-      fx[k] = fluid ? ux[c0 + k] : -0.0f;
-      fy[k] = fluid ? uy[c0 + k] : -0.0f;
-      mine += fluid ? 1u : 0u;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const uint32_t nq = padded / 4u;  // float4s per sum, a multiple of 8
+  const bool stager = threadIdx.x >= 32u;
+  const uint32_t nchunks = (nb + kMeanChunk - 1u) / kMeanChunk;
+  if (stager && nchunks)
+    mine += stage_chunk(ux, uy, sol, nb, 0, reinterpret_cast<float*>(s_ux[0]),
+                        reinterpret_cast<float*>(s_uy[0]));
+  __syncthreads();
+  for (uint32_t c = 0; c < nchunks; ++c) {
+    const uint32_t cur = c & 1u;
+    if (stager) {
+      if (c + 1u < nchunks)
+        mine += stage_chunk(ux, uy, sol, nb, (c + 1u) * kMeanChunk,
+                            reinterpret_cast<float*>(s_ux[cur ^ 1u]),
+                            reinterpret_cast<float*>(s_uy[cur ^ 1u]));
+    } else if (threadIdx.x == 0) {
+      const uint32_t len = min(kMeanChunk, nb - c * kMeanChunk);
+      const uint32_t nq = ((len + 31u) & ~31u) / 4u;  // float4s per sum, a multiple of 8
+      const float4* qa = s_ux[cur];
+      const float4* qb = s_uy[cur];
       float4 a[8], b[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        a[i] = s_ux[i];
-        b[i] = s_uy[i];
+        a[i] = qa[i];
+        b[i] = qb[i];
       }
       for (uint32_t q = 0; q < nq; q += 8u) {
         const uint32_t qn = q + 8u < nq ? q + 8u : q;  // the last round rereads its own
         float4 na[8], nb4[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          na[i] = s_ux[qn + i];
-          nb4[i] = s_uy[qn + i];
+          na[i] = qa[qn + i];
+          nb4[i] = qb[qn + i];
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {

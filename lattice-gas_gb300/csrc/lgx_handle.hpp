@@ -48,10 +48,11 @@ struct lgx_lattice {
   bool auto_resolved = false;   // LGX_STEP_AUTO: the tuner's choice below is set
   int auto_mode = LGX_STEP_SINGLE;
   uint32_t auto_depth = 0;
-  uint32_t auto_words = 0;        // chunks per warp of the single-step kernel
-  float auto_us[7] = {0, 0, 0, 0, 0, 0, 0};  // single (best, 1, 2 chunks), wave, temporal 4,
-                                              // 8, graph
-  uint32_t step_words = 0;        // a pinned kernel shape (0: by size, or the tuner's)
+  uint32_t auto_words = 0;        // the single-step kernel's shape (lgx::kShape*)
+  float auto_us[9] = {};  // single (best, 1 and 2 chunks), wave, temporal 4, 8, graph,
+                          // single (2 and 4 words per lane)
+  uint32_t step_words = 0;        // a pinned kernel shape, lgx::kShape* (0: the tuner's or
+                                  // by size)
   // LGX_STEP_GRAPH: a batch of this lattice alone, whose work runs on the
   // lattice's stream; made at first use, dropped when the inlet or the field
   // (which a batch lays out when it is made) changes

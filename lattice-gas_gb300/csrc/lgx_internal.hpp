@@ -37,8 +37,17 @@ struct StepArgs {
   Dims dm;
   uint64_t seed;
   uint64_t steps;  // steps taken before this one
-  uint32_t words;  // 32-word chunks per warp (1 or 2; 0: chosen by the lattice's size)
+  uint32_t words;  // the kernel's shape, a kShape* value (0: chosen by the lattice's size)
 };
+
+// Shapes of the single-step kernel.  Chunk1, Chunk2: one word per lane, a warp
+// takes one or two 32-word chunks (256- and 128-thread blocks).  Lanes2,
+// Lanes4: two or four consecutive words per lane in 64- or 128-bit accesses,
+// for lattices whose words per row are a multiple of that count.
+constexpr uint32_t kShapeChunk1 = 1, kShapeChunk2 = 2, kShapeLanes2 = 3, kShapeLanes4 = 4;
+// The shape a launch with `shape` requested runs: the request when it applies
+// to the lattice, else the size-based default.
+uint32_t step_shape(const Dims& dm, uint32_t shape);
 
 // `nsteps` steps of one lattice in one cooperative launch.  The state after
 // local step s lives in planes[s & 1]; done[b] is the last step CTA b has

@@ -252,7 +252,8 @@ int resolve_auto(lgx_lattice* lat) {
     // the tuner could not run here (e.g. no room for its scratch lattice): the
     // reference's own launch pattern, one kernel per step
     cudaGetLastError();
-    p = lgx::StepPlan{LGX_STEP_SINGLE, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    p = lgx::StepPlan{};
+    p.mode = LGX_STEP_SINGLE;
   }
   lat->auto_mode = p.mode;
   lat->auto_depth = p.depth;
@@ -264,6 +265,8 @@ int resolve_auto(lgx_lattice* lat) {
   lat->auto_us[4] = p.temporal4_us;
   lat->auto_us[5] = p.temporal8_us;
   lat->auto_us[6] = p.graph_us;
+  lat->auto_us[7] = p.lanes2_us;
+  lat->auto_us[8] = p.lanes4_us;
   lat->auto_resolved = true;
   return LGX_OK;
 }
@@ -622,6 +625,17 @@ int lgx_get_step_plan(lgx_lattice* lat, lgx_step_plan* out) {
   out->temporal4_us = lat->auto_us[4];
   out->temporal8_us = lat->auto_us[5];
   out->graph_us = lat->auto_us[6];
+  out->lanes2_us = lat->auto_us[7];
+  out->lanes4_us = lat->auto_us[8];
+  return LGX_OK;
+}
+
+int lgx_set_step_shape(lgx_lattice* lat, int shape) {
+  if (!lat || shape < LGX_SHAPE_AUTO || shape > LGX_SHAPE_LANES4) {
+    lgx::set_error("lgx_set_step_shape: bad handle or shape (0 to 4)");
+    return LGX_ERR_ARG;
+  }
+  lat->step_words = (uint32_t)shape;
   return LGX_OK;
 }
 

@@ -31,12 +31,13 @@ namespace lgx {
 
 namespace {
 
-// The single-step kernel's shapes, both compiled for six resident blocks per
-// SM.  A lattice that fills the GPU takes 128-thread blocks with two
-// consecutive 32-word chunks per warp (two independent word updates per thread
-// for the scheduler to interleave: 7.69 -> 7.22 us per wake-run step, 95.6 ->
-// 91.4 us at 16384 x 8192); a smaller one, whose step is latency-bound, takes
-// 256-thread blocks with one chunk per warp (twice the threads in flight).
+// The single-step kernel's word-per-lane shapes, both compiled for six resident
+// blocks per SM: 128-thread blocks with two consecutive 32-word chunks per warp
+// (two independent word updates per thread for the scheduler to interleave:
+// 7.69 -> 7.22 us per wake-run step, 95.6 -> 91.4 us at 16384 x 8192), and
+// 256-thread blocks with one chunk per warp (twice the threads in flight, for
+// lattices too small to fill the GPU).  The lane shapes (several consecutive
+// words per lane, lgx_step_lanes_kernel) come after them.
 constexpr uint32_t kTwoChunkMinWords = 152u * 6u * 256u;  // one wave of two-chunk blocks
 constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
 // Resident blocks per SM the register allocation must allow (64 registers).
@@ -77,6 +78,34 @@ __global__ void __launch_bounds__(256 / WORDS, LGX_STEP_MINB) lgx_step_kernel(co
 #pragma unroll
   for (int q = 0; q < kStepWords; ++q)
     step_word<REST, false>(p.a, p.b, p.solid, p.anysolid, p.inlet, p.dm, s[q], g[q], live[q]);
+}
+
+// One step per launch with V consecutive words per lane (V = 2 or 4; rows a
+// whole number of V-word groups): a warp takes 32 V consecutive words, four
+// warps a block.  All V draws of the lane come first, as above, then the
+// planes arrive in 64- or 128-bit loads.  Four words per lane are compiled for
+// four resident blocks (128 registers), two for six (80).  Measured against
+// other choices on GB300 (us per step, wake run / 32768 x 16384): making the
+// draws after the wait, 7.64 / 290.8 against 6.20 / 290.1 (the draws no longer
+// fill the previous step's drain); half of them before it, 6.93 / 315;
+// three resident blocks of 155 registers, 7.35 / 339; five of 96, draws
+// after the wait, 9.11 / 290.1.  The hash outputs' shifts as multiplies on the
+// FMA pipe: 6.03 / 297.0.
+template <bool REST, int V>
+__global__ void __launch_bounds__(128, V == 4 ? 4 : 6) lgx_step_lanes_kernel(const StepArgs p) {
+  constexpr int E = V;  // draws made before the wait
+  const uint32_t warp = blockIdx.x * 4u + (threadIdx.x >> 5);
+  uint32_t gq = warp * (32u * V) + (threadIdx.x & 31u) * V;
+  const bool live = gq < p.dm.total;
+  if (!live) gq = p.dm.total - V;
+  const uint32_t seed32 = step_seed32(p.seed, p.steps);
+  Draws s[E > 0 ? E : 1];
+#pragma unroll
+  for (int q = 0; q < E; ++q) s[q] = draws((gq + q) ^ seed32);
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  step_lane_words<REST, V, E>(p.a, p.b, p.solid, p.anysolid, p.inlet, p.dm, s, seed32, gq,
+                              live);
 }
 
 // ---- the persistent multi-step kernel ---------------------------------------
@@ -209,11 +238,28 @@ __global__ void __launch_bounds__(128) lgx_inlet_kernel(const InletArgs p) {
 
 }  // namespace
 
+// The shape by size: from one full wave of two-chunk blocks up, four words per
+// lane where the rows allow it (wake run 7.07 -> 6.20 us per step, 32768 x
+// 16384 347 -> 290 us), else two, else two chunks per warp; below that two
+// words per lane where they fit (2048 x 1280: 5.04 -> 4.30 us), else one chunk.
+uint32_t step_shape(const Dims& dm, uint32_t shape) {
+  if (shape == kShapeLanes4 && dm.wpr % 4u == 0u) return shape;
+  if (shape == kShapeLanes2 && dm.wpr % 2u == 0u) return shape;
+  if (shape == kShapeChunk1 || shape == kShapeChunk2) return shape;
+  if (dm.total >= kTwoChunkMinWords) {
+    if (dm.wpr % 4u == 0u) return kShapeLanes4;
+    return dm.wpr % 2u == 0u ? kShapeLanes2 : kShapeChunk2;
+  }
+  return dm.wpr % 2u == 0u ? kShapeLanes2 : kShapeChunk1;
+}
+
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
-  const bool two = s.words ? s.words == 2 : s.dm.total >= kTwoChunkMinWords;
+  const uint32_t shape = step_shape(s.dm, s.words);
   cfg.gridDim = dim3((s.dm.total + 255u) / 256u);
-  cfg.blockDim = dim3(two ? 128 : 256);
+  cfg.blockDim = dim3(shape == kShapeChunk1 ? 256 : 128);
+  if (shape == kShapeLanes2) cfg.gridDim = dim3((s.dm.total + 255u) / 256u);
+  if (shape == kShapeLanes4) cfg.gridDim = dim3((s.dm.total + 511u) / 512u);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -221,12 +267,20 @@ cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (two) {
-    if (rest) return cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 2>, s);
-    return cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 2>, s);
+  switch (shape) {
+    case kShapeLanes4:
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4>, s);
+    case kShapeLanes2:
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2>, s);
+    case kShapeChunk2:
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 2>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 2>, s);
+    default:
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 1>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 1>, s);
   }
-  if (rest) return cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 1>, s);
-  return cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 1>, s);
 }
 
 cudaError_t wave_grid(bool rest, uint32_t total, uint32_t* grid) {

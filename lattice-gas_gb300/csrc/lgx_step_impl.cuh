@@ -156,6 +156,158 @@ __device__ __forceinline__ void step_word(const uint32_t* a, uint32_t* b,
                                             j, live);
 }
 
+// V consecutive words of one row held by one lane (V = 2 or 4), loaded and
+// stored as one 64- or 128-bit access per plane.
+template <int V> struct LaneWords;
+template <> struct LaneWords<2> {
+  typedef uint2 T;
+  static __device__ __forceinline__ void get(const T& t, uint32_t* v) { v[0] = t.x; v[1] = t.y; }
+  static __device__ __forceinline__ T make(const uint32_t* v) { return make_uint2(v[0], v[1]); }
+};
+template <> struct LaneWords<4> {
+  typedef uint4 T;
+  static __device__ __forceinline__ void get(const T& t, uint32_t* v) {
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+  static __device__ __forceinline__ T make(const uint32_t* v) {
+    return make_uint4(v[0], v[1], v[2], v[3]);
+  }
+};
+
+// One step of words gq .. gq+V-1 of planes a -> b, V consecutive words of one
+// row per lane, for lattices whose rows are a whole number of such groups
+// (wpr % V == 0; then every plane row starts on a 16-byte boundary).  The
+// same update as step_word, word for word; what V words share is computed
+// once: the row, its neighbours and their pointers, the wrap and edge
+// predicates, one shuffle per plane and side (the neighbour word inside the
+// lane's group is already in a register), the obstacle summary and the
+// inflow and tail tests.  All 32 lanes call this together with consecutive
+// groups; lanes past the end repeat the last group and do not store.
+template <bool REST, int V, int E>
+__device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
+                                                uint32_t* __restrict__ b,
+                                                const uint32_t* __restrict__ solid,
+                                                const uint32_t* __restrict__ anysolid,
+                                                const uint32_t* __restrict__ inlet,
+                                                const Dims& dm, const Draws* s, uint32_t seed32,
+                                                uint32_t gq, bool live) {
+  typedef LaneWords<V> LW;
+  typedef typename LW::T VT;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t t = __umulhi(gq, dm.div_m);
+  const uint32_t y = (t + ((gq - t) >> dm.div_s1)) >> dm.div_s2;  // gq / wpr
+  const uint32_t j0 = gq - y * dm.wpr;
+  const uint32_t ym = (y == 0u) ? dm.h - 1u : y - 1u;
+  const uint32_t yp = (y + 1u == dm.h) ? 0u : y + 1u;
+  const size_t S = dm.total;
+  const uint32_t* rc = a + (size_t)y * dm.wpr;   // row y, plane 0
+  const uint32_t* rm = a + (size_t)ym * dm.wpr;  // row y-1
+  const uint32_t* rp = a + (size_t)yp * dm.wpr;  // row y+1
+  // plane d's row: 1, 2 from y-1; 0, 3, 6 from y; 4, 5 from y+1
+  const uint32_t* r[7] = {rc, rm + S, rm + 2 * S, rc + 3 * S, rp + 4 * S, rp + 5 * S, rc + 6 * S};
+  uint32_t w[7][V];
+#pragma unroll
+  for (int d = 0; d < 7; ++d) LW::get(__ldg(reinterpret_cast<const VT*>(r[d] + j0)), w[d]);
+
+  const unsigned FULL = 0xffffffffu;
+  const bool lok = lane > 0u && j0 > 0u;        // lane - 1 holds words j0-V .. j0-1 of this row
+  const bool rok = lane < 31u && j0 + V < dm.wpr;  // lane + 1 holds j0+V .. j0+2V-1
+  const bool last = j0 + V == dm.wpr;           // word V-1 is the row's last word
+  // the word left of j0 for planes 0, 1, 5 and right of j0+V-1 for 2, 3, 4
+  uint32_t lw[3], rw[3];
+  {
+    const int lp[3] = {0, 1, 5}, rpn[3] = {2, 3, 4};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const uint32_t l = __shfl_up_sync(FULL, w[lp[i]][V - 1], 1);
+      const uint32_t q = __shfl_down_sync(FULL, w[rpn[i]][0], 1);
+      lw[i] = lok ? l : (j0 > 0u ? __ldg(r[lp[i]] + j0 - 1u)
+                                 : __ldg(r[lp[i]] + dm.lastword) << (31u - dm.lastbit));
+      rw[i] = rok ? q : (last ? 0u : __ldg(r[rpn[i]] + j0 + V));
+    }
+  }
+  // bit 0 of word 0 of the rows planes 2, 3, 4 read, the wrap into the last word
+  uint32_t wrap[3] = {0u, 0u, 0u};
+  if (last) {
+    wrap[0] = __ldg(r[2]) & 1u;
+    wrap[1] = __ldg(r[3]) & 1u;
+    wrap[2] = __ldg(r[4]) & 1u;
+  }
+
+  // obstacle summary bits of the V words (V divides 32, groups are aligned)
+  const uint32_t abits = (__ldg(anysolid + (gq >> 5)) >> (gq & 31u)) & ((1u << V) - 1u);
+  const bool warp_solid = __any_sync(FULL, abits != 0u);
+  uint32_t sw[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) sw[q] = 0u;
+  if (abits != 0u) LW::get(__ldg(reinterpret_cast<const VT*>(solid + gq)), sw);
+
+  const bool odd = y & 1u;
+  uint32_t res[7][V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    auto left = [&](int i, int d) { return q > 0 ? w[d][q - 1] : lw[i]; };
+    auto right = [&](int i, int d) -> uint32_t {
+      uint32_t v = __funnelshift_r(w[d][q], q < V - 1 ? w[d][q + 1] : rw[i], 1);
+      if (q == V - 1 && last) v = (v & ~(1u << dm.lastbit)) | (wrap[i] << dm.lastbit);
+      return v;
+    };
+    uint32_t n[7];
+    n[0] = __funnelshift_l(left(0, 0), w[0][q], 1);
+    n[3] = right(1, 3);
+    if (odd) {
+      n[1] = w[1][q];
+      n[2] = right(0, 2);
+      n[4] = right(2, 4);
+      n[5] = w[5][q];
+    } else {
+      n[1] = __funnelshift_l(left(1, 1), w[1][q], 1);
+      n[2] = w[2][q];
+      n[4] = w[4][q];
+      n[5] = __funnelshift_l(left(2, 5), w[5][q], 1);
+    }
+    n[6] = w[6][q];
+    uint32_t o[7];
+    if (q < E) {
+      collide<REST>(n, s[q], o);
+    } else {
+      const Draws sq = draws((gq + q) ^ seed32);
+      collide<REST>(n, sq, o);
+    }
+    if (warp_solid) {
+      uint32_t rr[7];
+      walls(n, o, sw[q], rr);
+#pragma unroll
+      for (int d = 0; d < 7; ++d) res[d][q] = rr[d];
+    } else {
+#pragma unroll
+      for (int d = 0; d < 7; ++d) res[d][q] = o[d];
+    }
+  }
+
+  if (j0 < dm.iw) {  // inflow re-seed of the leftmost columns (src/gpu.rs:296-306)
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const uint32_t j = j0 + q;
+      if (j < dm.iw) {
+        const uint32_t span = min(dm.inlet_cols - j * 32u, 32u);
+        const uint32_t imask = (span >= 32u) ? 0xffffffffu : ((1u << span) - 1u);
+        const uint32_t apply = imask & ~sw[q];
+        const uint32_t* bern = inlet + ((size_t)y * dm.iw + j) * 7u;
+#pragma unroll
+        for (int d = 0; d < 7; ++d) res[d][q] = (res[d][q] & ~apply) | (__ldg(bern + d) & apply);
+      }
+    }
+  }
+  if (last) {  // clear the bits past the row's end
+#pragma unroll
+    for (int d = 0; d < 7; ++d) res[d][V - 1] &= dm.tail;
+  }
+  if (live) {
+#pragma unroll
+    for (int d = 0; d < 7; ++d) *reinterpret_cast<VT*>(b + d * S + gq) = LW::make(res[d]);
+  }
+}
 
 // Coarse-graining of field block `blk` of one lattice by one whole warp
 // (lgca_sample, src/gpu.rs:324-377).  Lanes take rows of the block; each row

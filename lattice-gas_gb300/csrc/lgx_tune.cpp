@@ -38,7 +38,7 @@ constexpr size_t kTuneMaxWords = 4u << 20;  // per-plane words of all synthetic 
 
 std::mutex g_mu;
 std::map<std::tuple<int, uint32_t, uint32_t, bool>, ClassPlan> g_plans;
-std::map<std::tuple<int, uint32_t, bool, bool>, StepPlan> g_step_plans;
+std::map<std::tuple<int, uint32_t, bool, bool, uint32_t>, StepPlan> g_step_plans;
 
 struct Scratch {
   std::vector<void*> ptrs;
@@ -227,7 +227,9 @@ uint32_t graph_max_words(int device) {
 int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out) {
   const Dims dm = make_dims(w, h, 0);
   const bool wide = temporal_supported(dm, 4);
-  const auto key = std::make_tuple(device, class_bucket(dm.total), wide, rest);
+  // the words per row decide which shapes apply: a multiple of 4, of 2, or neither
+  const uint32_t lanes = dm.wpr % 4u == 0u ? 4u : dm.wpr % 2u == 0u ? 2u : 1u;
+  const auto key = std::make_tuple(device, class_bucket(dm.total), wide, rest, lanes);
   {
     std::lock_guard<std::mutex> g(g_mu);
     auto it = g_step_plans.find(key);
@@ -239,16 +241,24 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
   lgx_lattice* t = nullptr;
   int rc = lgx_create(w, h, rest ? 1 : 0, 0x7E57ull, &t);
   if (rc) return rc;
-  StepPlan p{LGX_STEP_SINGLE, 0, 1, 0, 0, 0, 0, 0, 0, 0};
+  StepPlan p{};
+  p.mode = LGX_STEP_SINGLE;
+  p.words = kShapeChunk1;
   const float est = time_mode(t, LGX_STEP_SINGLE, 0, 0);
-  for (uint32_t words : {1u, 2u}) {  // the single-step kernel's two shapes
-    t->step_words = words;
+  // the single-step kernel's shapes: a word per lane in one or two chunks per
+  // warp, and two or four consecutive words per lane where the rows allow
+  float* shape_us[4] = {&p.single1_us, &p.single2_us, &p.lanes2_us, &p.lanes4_us};
+  for (uint32_t shape = kShapeChunk1; shape <= kShapeLanes4; ++shape) {
+    if (step_shape(dm, shape) != shape) continue;
+    t->step_words = shape;
     const float us = time_mode(t, LGX_STEP_SINGLE, 0, est);
-    (words == 1 ? p.single1_us : p.single2_us) = us > 0 ? us : 0;
+    *shape_us[shape - 1] = us > 0 ? us : 0;
+    if (us > 0 && (p.single_us <= 0 || us < p.single_us)) {
+      p.single_us = us;
+      p.words = shape;
+    }
   }
   t->step_words = 0;
-  p.words = (p.single2_us > 0 && (p.single1_us <= 0 || p.single2_us < p.single1_us)) ? 2 : 1;
-  p.single_us = p.words == 2 ? p.single2_us : p.single1_us;
   const float w_us = time_mode(t, LGX_STEP_WAVE, 0, p.single_us);
   p.wave_us = w_us > 0 ? w_us : 0;
   if (wide) {

@@ -26,19 +26,21 @@ uint32_t class_bucket(uint32_t words);
 // current device), timed on first use and cached for the process.
 cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ClassPlan* out);
 
-// How LGX_STEP_AUTO steps one lattice: the fastest of one launch per step (with
-// one or two 32-word chunks per warp), the persistent wave kernel, temporal
+// How LGX_STEP_AUTO steps one lattice: the fastest of one launch per step (in
+// each kernel shape that applies, kShape*), the persistent wave kernel, temporal
 // blocking of 4 or 8 steps and, for lattices below one full wave of step
 // blocks, the one-lattice batch (LGX_STEP_GRAPH), timed on a
 // scratch lattice of the same shape on first use of its size class (words
 // rounded up to a power of two, whether it is wide enough for temporal
-// blocking, the rule) and cached for the process.  Times are microseconds per
-// step; 0 where a mode does not apply.
+// blocking, the rule, whether the words per row are a multiple of 4 or 2) and
+// cached for the process.  Times are microseconds per step; 0 where a mode does
+// not apply.
 struct StepPlan {
   int mode;        // LGX_STEP_SINGLE, LGX_STEP_WAVE, LGX_STEP_TEMPORAL or LGX_STEP_GRAPH
   uint32_t depth;  // temporal depth when TEMPORAL
-  uint32_t words;  // chunks per warp of the single-step kernel (1 or 2)
+  uint32_t words;  // the single-step kernel's shape (kShape*)
   float single_us, single1_us, single2_us, wave_us, temporal4_us, temporal8_us, graph_us;
+  float lanes2_us, lanes4_us;
 };
 int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out);
 

@@ -88,7 +88,8 @@ class StepPlan(C.Structure):
     _fields_ = [("mode", C.c_int), ("depth", C.c_uint32), ("words", C.c_uint32),
                 ("single_us", C.c_float), ("single1_us", C.c_float), ("single2_us", C.c_float),
                 ("wave_us", C.c_float), ("temporal4_us", C.c_float),
-                ("temporal8_us", C.c_float), ("graph_us", C.c_float)]
+                ("temporal8_us", C.c_float), ("graph_us", C.c_float),
+                ("lanes2_us", C.c_float), ("lanes4_us", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -133,6 +134,7 @@ def lib():
         _sig(L, "lgx_sample_field", vp, C.c_float)
         _sig(L, "lgx_set_step_mode", vp, C.c_int)
         _sig(L, "lgx_set_temporal_depth", vp, C.c_int)
+        _sig(L, "lgx_set_step_shape", vp, C.c_int)
         _sig(L, "lgx_get_step_plan", vp, C.POINTER(StepPlan))
         _sig(L, "lgx_read_field", vp, f32p, f32p, f32p, f32p, sz)
         _sig(L, "lgx_read_block_sums", vp, i32p, i32p, i32p, i32p, sz)
@@ -352,9 +354,14 @@ class GpuLattice:
         _check(lib().lgx_advance_sampling(self._h, int(n), int(sample_every), float(alpha)))
 
     STEP_AUTO, STEP_SINGLE, STEP_WAVE, STEP_TEMPORAL, STEP_GRAPH = 0, 1, 2, 3, 4
+    SHAPE_AUTO, SHAPE_CHUNK1, SHAPE_CHUNK2, SHAPE_LANES2, SHAPE_LANES4 = 0, 1, 2, 3, 4
 
     def set_step_mode(self, mode: int):
         _check(lib().lgx_set_step_mode(self._h, int(mode)))
+
+    def set_step_shape(self, shape: int):
+        """Pin the single-step kernel's shape (SHAPE_*; 0: tuner / by size)."""
+        _check(lib().lgx_set_step_shape(self._h, int(shape)))
 
     def set_temporal_depth(self, k: int):
         _check(lib().lgx_set_temporal_depth(self._h, int(k)))

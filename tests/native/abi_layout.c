@@ -19,7 +19,7 @@ int main(void) {
   F(lgx_step_plan, mode); F(lgx_step_plan, depth); F(lgx_step_plan, words);
   F(lgx_step_plan, single_us); F(lgx_step_plan, single1_us); F(lgx_step_plan, single2_us);
   F(lgx_step_plan, wave_us); F(lgx_step_plan, temporal4_us); F(lgx_step_plan, temporal8_us);
-  F(lgx_step_plan, graph_us);
+  F(lgx_step_plan, graph_us); F(lgx_step_plan, lanes2_us); F(lgx_step_plan, lanes4_us);
   END();
   BEGIN("lgx_batch_class", lgx_batch_class);
   F(lgx_batch_class, words); F(lgx_batch_class, lattices); F(lgx_batch_class, rest);

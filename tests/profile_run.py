@@ -13,7 +13,9 @@ byte-per-cell update, 16 bands).  --policy picks the sweep's batch
 policy (under a profiler pass 1: the tuner's timings are not meaningful there, and
 without one it picks one launch per step for every class of this sweep).  --mode
 picks the step
-launch mode (1 one launch per step, 2 persistent waves, 3 temporal blocking).
+launch mode (1 one launch per step, 2 persistent waves, 3 temporal blocking), --shape
+the single-step kernel's shape (1, 2: one or two 32-word chunks per warp; 3, 4: two or
+four consecutive words per lane).
 """
 import argparse
 import os
@@ -36,6 +38,8 @@ def main():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--mode", type=int, default=1)
     ap.add_argument("--depth", type=int, default=4)
+    ap.add_argument("--shape", type=int, default=0,
+                    help="the single-step kernel's shape (0 by size, 1-4 LGX_SHAPE_*)")
     a = ap.parse_args()
     if a.case == "tiny":
         # --size x --size lattices (8 of them) as one batch under --policy
@@ -81,6 +85,7 @@ def main():
     wl = W.wake_run() if a.case == "wake" else W.roofline_case(w=16384, h=8192, n_circles=50)
     g = LG.GpuLattice(wl.w, wl.h, True, wl.seed)
     g.set_step_mode(a.mode)
+    g.set_step_shape(a.shape)
     if a.mode == 3:
         g.set_temporal_depth(a.depth)
     g.set_inlet(wl.inlet_cols, wl.density, wl.inflow, True)

@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("w,h,bx,by", [(256, 128, 16, 16), (300, 96, 20, 8), (128, 64, 32, 32),
                                        (64, 40, 64, 10),
-                                       (2048, 1280, 20, 20),   # 6528 blocks: two staged chunks
+                                       (2048, 1280, 20, 20),   # 6528 blocks: four staged chunks, the last partial
                                        (4096, 2304, 8, 8)])    # 147,456 blocks
 def test_vorticity_and_mean_velocity_match_the_oracle(LG, O, w, h, bx, by):
     cells = np.zeros(w * h, np.uint8)

@@ -277,6 +277,47 @@ def test_small_lattices_bit_exact(LG, O, w, h, inlet, rest, mode):
         assert_same(g, o)
 
 
+SHAPES = [1, 2, 3, 4]   # chunk of one / two per warp, two / four consecutive words per lane
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("w,h,inlet,rest", [
+    (128, 34, 40, True),    # four words per row: one four-word group per row
+    (250, 20, 8, True),     # eight words per row, 26 valid bits in the last
+    (60, 16, 8, True),      # two words per row: both wraps inside one lane's pair
+    (190, 24, 70, False),   # six words per row: pairs apply, fours fall back
+    (1000, 40, 8, True),    # 32 words per row: a warp spans several rows
+    (4000, 12, 40, False),  # 125 words per row: neither applies
+])
+def test_step_shapes_bit_exact(LG, O, w, h, inlet, rest, shape):
+    """Every kernel shape, pinned, against the oracle: obstacles, inflows,
+    ragged rows and both rules, across inlet chunks and sampling points."""
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, w / 2.0, h * 0.43, min(w, h) / 5.0)
+    LG.add_box(cells, w, h, w // 5, w // 5 + 2, 0, h // 3)
+    LG.init_equilibrium(cells, 0.3, 0.2, 0.0, rest, 4321 + w)
+    g, o = pair(LG, O, w, h, rest, 0xC0FFEE + w, cells,
+                inlet=(inlet, 0.3, (0.2, 0.0), rest) if inlet else None, block=4, mode=1)
+    g.set_step_shape(shape)
+    for chunk in (1, 7, 64, 130):
+        g.advance_sampling(chunk, 10, 0.3)
+        o.advance_sampling(chunk, 10, 0.3)
+        assert_same(g, o)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_step_shapes_on_the_full_wake_run(LG, O, shape):
+    """4096 x 2304 (128 words per row), 24 steps in each shape against the oracle."""
+    from lattice_gas import workloads as W
+    wl = W.wake_run()
+    g, o = pair(LG, O, wl.w, wl.h, True, wl.seed, wl.cells,
+                inlet=(wl.inlet_cols, wl.density, wl.inflow, True), block=wl.block, mode=1)
+    g.set_step_shape(shape)
+    g.advance_sampling(24, 12, wl.alpha)
+    o.advance_sampling(24, 12, wl.alpha)
+    assert_same(g, o)
+
+
 def test_restart_resets_the_stream(LG, O):
     w, h = 96, 32
     cells = np.zeros(w * h, np.uint8)

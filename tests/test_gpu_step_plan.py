@@ -7,13 +7,18 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("w,h", [(64, 64), (300, 96), (4096, 256)])
+@pytest.mark.parametrize("w,h", [(64, 64), (300, 96), (4096, 256), (190, 96)])
 def test_auto_picks_the_fastest_timed_mode(LG, w, h):
     g = LG.GpuLattice(w, h, True, 3)
     p = g.step_plan
+    wpr = (w + 31) // 32
     assert p["single1_us"] > 0 and p["single2_us"] > 0
-    assert p["single_us"] == min(p["single1_us"], p["single2_us"])
-    assert p["words"] == (1 if p["single_us"] == p["single1_us"] else 2)
+    # the lane shapes are timed exactly where the words per row allow them
+    assert (p["lanes2_us"] > 0) == (wpr % 2 == 0)
+    assert (p["lanes4_us"] > 0) == (wpr % 4 == 0)
+    shapes = {1: p["single1_us"], 2: p["single2_us"], 3: p["lanes2_us"], 4: p["lanes4_us"]}
+    assert p["single_us"] == min(t for t in shapes.values() if t > 0)
+    assert shapes[p["words"]] == p["single_us"]
     if (w + 31) // 32 >= 64:
         assert p["temporal4_us"] > 0 and p["temporal8_us"] > 0
     else:
