@@ -92,6 +92,46 @@ __global__ void __launch_bounds__(256 / WORDS, 4 * WORDS) lgx_batch_step_kernel(
 // accesses; a block still covers 256 words, so the block tables are the
 // same).  A block of a lattice whose words per row are odd runs the two-chunk
 // mapping instead (the branch is uniform across the block).
+// V consecutive words per lane from word gq of lattice d (all 32 lanes of the
+// warp together), the draws made before the wait on the previous step.
+template <int RULE, int V>
+__device__ __forceinline__ void batch_lane_words(const BatchStepArgs& p, const LatDesc& d,
+                                                 uint32_t gq) {
+  const bool live = gq < d.dm.total;
+  if (!live) gq = d.dm.total - V;
+  const uint64_t local = *p.base + p.k;
+  const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
+  Draws s[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) s[q] = draws((gq + q) ^ seed32);
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
+  const uint32_t* src = par ? d.planes[1] : d.planes[0];
+  uint32_t* dst = par ? d.planes[0] : d.planes[1];
+  const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)p.k * d.dm.h * d.dm.iw * 7u : nullptr;
+  if (RULE == 2 ? d.rest != 0 : RULE == 1)
+    step_lane_words<true, V, V>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq, live);
+  else
+    step_lane_words<false, V, V>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
+                                 live);
+}
+
+// Four consecutive words per lane in 64-thread blocks (256 words a block).  A
+// block of a lattice whose words per row are not a multiple of four takes four
+// 32-word chunks per warp instead.
+template <int RULE>
+__global__ void __launch_bounds__(64, 8) lgx_batch_lanes4_kernel(BatchStepArgs p) {
+  const uint32_t blk = p.first_block + blockIdx.x;
+  const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
+  const LatDesc& d = p.descs[li];
+  if (d.dm.wpr & 3u) {
+    batch_block<RULE, 4>(p);
+    return;
+  }
+  batch_lane_words<RULE, 4>(p, d, (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 4u);
+}
+
 template <int RULE>
 __global__ void __launch_bounds__(128, 6) lgx_batch_lanes_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
@@ -186,13 +226,18 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule
   if (words == 0) words = kBatchLanes2;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
-  cfg.blockDim = dim3(words == 1 ? 256 : 128);
+  cfg.blockDim = dim3(words == 1 ? 256 : words == kBatchLanes4 ? 64 : 128);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (words == kBatchLanes4) {
+    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<2>, a);
+    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<1>, a);
+    return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<0>, a);
+  }
   if (words == kBatchLanes2) {
     if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2>, a);
     if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1>, a);

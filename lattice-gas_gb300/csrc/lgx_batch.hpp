@@ -91,7 +91,18 @@ constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;
 // chunk shape at every size measured (transport sweep 1224 -> 1275
 // Gsite-updates/s; eight 2048 x 1280 lattices 14.7 -> 12.8 us per step; eight
 // 256 x 256 3.37 -> 3.05 us).
-constexpr int kBatchLanes2 = 3;
+// kBatchLanes4: four words per lane in 64-thread blocks, for launches whose
+// every lattice has a multiple of 4 words per row (a block of another lattice
+// would take four chunks per warp, slow: the mixed-width transport sweep ran at
+// 971 against 1276 Gsite-updates/s); it pays from one full wave of such blocks
+// up (eight 2048 x 1280 lattices 12.76 -> 11.44 us per step, one 4096 x 2304
+// 6.78 -> 5.97) and loses below it (one 2048 x 1280, 3.05 -> 5.26).
+constexpr int kBatchLanes2 = 3, kBatchLanes4 = 4;
+// The shape a batched step launch of `nblocks` 256-word blocks takes, given
+// whether every lattice it covers has a multiple of 4 words per row.
+inline int batch_step_words(uint32_t nblocks, bool all_wpr4) {
+  return all_wpr4 && nblocks >= 152u * 8u ? kBatchLanes4 : kBatchLanes2;
+}
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st);
 cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st);

@@ -41,6 +41,7 @@ struct GraphEntry {
 // that one chain's launch gaps are filled by the others' blocks.
 struct StepGroup {
   uint32_t first = 0, count = 0, nblocks = 0, rest_blocks = 0;
+  bool wpr4 = true;  // every lattice of the chain has a multiple of 4 words per row
   uint32_t* d_block0 = nullptr;
   uint32_t* d_owner = nullptr;
   cudaStream_t st = nullptr;  // null for the batch's own stream
@@ -130,6 +131,7 @@ cudaError_t build_chains(lgx_batch* b, uint32_t ngroups) {
     while (i < b->nstep && (g + 1 == ngroups || block0[i] < target || sg.count == 0)) {
       gb0.push_back(gb0.back() + block0[i + 1] - block0[i]);
       if (b->lats[i]->rest) sg.rest_blocks = gb0.back();
+      sg.wpr4 = sg.wpr4 && b->lats[i]->dm.wpr % 4u == 0u;
       ++sg.count;
       ++i;
     }
@@ -254,7 +256,8 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
       // rest-particle lattices' blocks first, then the six-direction ones
       lgx::BatchStepArgs sa{b->d_descs + sg.first, sg.d_block0, sg.d_owner, sg.count,
                             b->d_base, k, 0};
-      e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks), 0, st);
+      e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks),
+                                 lgx::batch_step_words(sg.nblocks, sg.wpr4), st);
       if (e == cudaSuccess && b->hook && b->hook_per_step)
         e = b->hook(b->hook_ctx, st, b->d_base, k + 1);
     }

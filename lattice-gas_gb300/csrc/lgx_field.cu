@@ -148,30 +148,31 @@ __device__ __forceinline__ float vorticity_at(const float* __restrict__ ux,
 }
 
 // Field::mean_velocity (src/render.rs:146-161) by one block: the f32 sums run in
-// block order, as the reference adds them, so one thread (lane 0 of warp 0) adds
-// them all.  The other warps stage the field in chunks of kMeanChunk blocks into
-// two shared buffers: while the adding thread works through chunk c, they load
-// chunk c + 1, every load of a thread issued before any of its stores, so a
-// chunk costs one memory latency rather than one per row of threads.  Each
-// non-solid block's velocity is staged as it is and each solid block's (and
-// the padding's) as -0.0: adding -0.0 leaves every f32 unchanged in
-// round-to-nearest (x + -0 = x, +0 + -0 = +0, -0 + -0 = -0), so the adding
-// thread's sums are the reference's with no test in its loop.  It reads 32
-// values of each sum ahead of the adds that use them (two register sets), so
-// the dependent chain of f32 adds, not the shared-memory latency, sets its
-// pace.  The reference's count n adds 1.0f per non-solid block: the exact count
-// up to 2^24, where it stops growing; the block counts with a reduction and
-// rounds the same way.
+// block order, as the reference adds them, so each is one dependent chain of
+// adds on one thread: lane 0 of warp 0 adds the x components, lane 0 of warp 1
+// the y components, on different schedulers.  The other six warps stage the
+// field in chunks of kMeanChunk blocks into two shared buffers: while the
+// adding threads work through chunk c, they load chunk c + 1, every load of a
+// thread issued before any of its stores, so a chunk costs one memory latency
+// rather than one per row of threads.  Each non-solid block's velocity is
+// staged as it is and each solid block's (and the padding's) as -0.0: adding
+// -0.0 leaves every f32 unchanged in round-to-nearest (x + -0 = x,
+// +0 + -0 = +0, -0 + -0 = -0), so the sums are the reference's with no test in
+// the adding loop.  An adding thread reads 64 values ahead of the adds that use
+// them (two register sets), so the chain of f32 adds, not the shared-memory
+// latency, sets its pace.  The reference's count n adds 1.0f per non-solid
+// block: the exact count up to 2^24, where it stops growing; the block counts
+// with a reduction and rounds the same way.
 constexpr uint32_t kMeanChunk = 2048;  // blocks per staged chunk (8 KB per sum)
 constexpr uint32_t kAnalysisThreads = 256;
-constexpr uint32_t kStagers = kAnalysisThreads - 32;  // warps 1.. stage, warp 0 adds
+constexpr uint32_t kStagers = kAnalysisThreads - 64;  // warps 2.. stage, warps 0, 1 add
 constexpr uint32_t kStagePer = (kMeanChunk + kStagers - 1) / kStagers;
 
 __device__ __forceinline__ uint32_t stage_chunk(const float* __restrict__ ux,
                                                 const float* __restrict__ uy,
                                                 const float* __restrict__ sol, uint32_t nb,
                                                 uint32_t c0, float* fx, float* fy) {
-  const uint32_t t = threadIdx.x - 32u;
+  const uint32_t t = threadIdx.x - 64u;
   float vx[kStagePer], vy[kStagePer];
   uint32_t fluid = 0;
 #pragma unroll
@@ -194,16 +195,40 @@ __device__ __forceinline__ uint32_t stage_chunk(const float* __restrict__ ux,
   return fluid;
 }
 
+// One chain: s + q[0] + q[1] + ... over `nq` float4s (a multiple of 16), in order.
+__device__ __forceinline__ float add_in_order(float s, const float4* q, uint32_t nq) {
+  float4 a[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = q[i];
+  for (uint32_t k = 0; k < nq; k += 16u) {
+    const uint32_t kn = k + 16u < nq ? k + 16u : k;  // the last round rereads its own
+    float4 n[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) n[i] = q[kn + i];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      s = __fadd_rn(s, a[i].x);
+      s = __fadd_rn(s, a[i].y);
+      s = __fadd_rn(s, a[i].z);
+      s = __fadd_rn(s, a[i].w);
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) a[i] = n[i];
+  }
+  return s;
+}
+
 __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux,
                                                     const float* __restrict__ uy,
                                                     const float* __restrict__ sol, uint32_t nb,
                                                     float* __restrict__ out) {
   __shared__ float4 s_ux[2][kMeanChunk / 4], s_uy[2][kMeanChunk / 4];
   __shared__ unsigned long long s_count;
+  __shared__ float s_sy;
   if (threadIdx.x == 0) s_count = 0;
-  float sx = 0.0f, sy = 0.0f;
+  float sum = 0.0f;  // x on thread 0, y on thread 32
   uint32_t mine = 0;
-  const bool stager = threadIdx.x >= 32u;
+  const bool stager = threadIdx.x >= 64u;
   const uint32_t nchunks = (nb + kMeanChunk - 1u) / kMeanChunk;
   if (stager && nchunks)
     mine += stage_chunk(ux, uy, sol, nb, 0, reinterpret_cast<float*>(s_ux[0]),
@@ -216,48 +241,21 @@ __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux
         mine += stage_chunk(ux, uy, sol, nb, (c + 1u) * kMeanChunk,
                             reinterpret_cast<float*>(s_ux[cur ^ 1u]),
                             reinterpret_cast<float*>(s_uy[cur ^ 1u]));
-    } else if (threadIdx.x == 0) {
+    } else if ((threadIdx.x & 31u) == 0u) {
       const uint32_t len = min(kMeanChunk, nb - c * kMeanChunk);
-      const uint32_t nq = ((len + 31u) & ~31u) / 4u;  // float4s per sum, a multiple of 8
-      const float4* qa = s_ux[cur];
-      const float4* qb = s_uy[cur];
-      float4 a[8], b[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        a[i] = qa[i];
-        b[i] = qb[i];
-      }
-      for (uint32_t q = 0; q < nq; q += 8u) {
-        const uint32_t qn = q + 8u < nq ? q + 8u : q;  // the last round rereads its own
-        float4 na[8], nb4[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          na[i] = qa[qn + i];
-          nb4[i] = qb[qn + i];
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          sx = __fadd_rn(sx, a[i].x); sy = __fadd_rn(sy, b[i].x);
-          sx = __fadd_rn(sx, a[i].y); sy = __fadd_rn(sy, b[i].y);
-          sx = __fadd_rn(sx, a[i].z); sy = __fadd_rn(sy, b[i].z);
-          sx = __fadd_rn(sx, a[i].w); sy = __fadd_rn(sy, b[i].w);
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          a[i] = na[i];
-          b[i] = nb4[i];
-        }
-      }
+      const uint32_t nq = ((len + 63u) & ~63u) / 4u;  // float4s, a multiple of 16
+      sum = add_in_order(sum, threadIdx.x == 0 ? s_ux[cur] : s_uy[cur], nq);
     }
     __syncthreads();
   }
+  if (threadIdx.x == 32) s_sy = sum;
   atomicAdd(&s_count, (unsigned long long)mine);
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned long long c = s_count;
     const float n = c <= (1ull << 24) ? (float)c : 16777216.0f;
-    out[0] = n == 0.0f ? 0.0f : __fdiv_rn(sx, n);
-    out[1] = n == 0.0f ? 0.0f : __fdiv_rn(sy, n);
+    out[0] = n == 0.0f ? 0.0f : __fdiv_rn(sum, n);
+    out[1] = n == 0.0f ? 0.0f : __fdiv_rn(s_sy, n);
   }
 }
 

@@ -64,7 +64,8 @@ struct lgx_lattice {
   // row and column profiles: scratch, row_ux[h], column_uy[w], column sums
   // [3][w] and the device copy of the profile descriptor, one allocation
   void* prof = nullptr;
-  float* vort = nullptr;  // vorticity of the field, bw*bh, then the mean velocity (2)
+  float* vort = nullptr;  // device address of vort_host: the field's vorticity (bw*bh),
+                          // then its mean velocity (2)
   float* vort_host = nullptr;  // page-locked copy of the same, for the read-back
 };
 

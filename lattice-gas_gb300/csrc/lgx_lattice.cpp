@@ -100,8 +100,7 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->sums);
   cudaFree(lat->prof);
   cudaFree(lat->fill_scratch);
-  cudaFree(lat->vort);
-  if (lat->vort_host) cudaFreeHost(lat->vort_host);
+  if (lat->vort_host) cudaFreeHost(lat->vort_host);  // lat->vort maps into it
   cudaFree(lat->done);
   cudaFree(lat->error);
   for (auto& e : lat->ev)
@@ -495,8 +494,7 @@ int lgx_attach_field(lgx_lattice* lat, size_t bx, size_t by) {
   drop_solo(lat);  // its block tables were laid out for the old field
   cudaFree(lat->field);
   cudaFree(lat->sums);
-  cudaFree(lat->vort);  // sized for the old block grid
-  if (lat->vort_host) cudaFreeHost(lat->vort_host);
+  if (lat->vort_host) cudaFreeHost(lat->vort_host);  // sized for the old block grid
   lat->field = nullptr;
   lat->sums = nullptr;
   lat->vort = nullptr;
@@ -679,23 +677,32 @@ int lgx_read_field(lgx_lattice* lat, float* ux, float* uy, float* rho, float* so
   return LGX_OK;
 }
 
-// The vorticity / mean-velocity buffers of the attached field: on the device, and
-// page-locked on the host so that the read-back is one DMA copy.
+// The field analyses' results: one page-locked host buffer, mapped into the
+// device's address space, that the analysis kernel writes directly (vorticity,
+// bw * bh floats, then the mean velocity's two), so a call is one launch and one
+// synchronisation with no copy between them.
 static int field_scratch(lgx_lattice* lat, float** out) {
   if (!lat->has_field) {
     lgx::set_error("no field attached to this lattice");
     return LGX_ERR_STATE;
   }
   const size_t bytes = ((size_t)lat->bw * lat->bh + 2) * 4;
-  if (!lat->vort) LGX_CUDA(cudaMalloc(&lat->vort, bytes));
-  if (!lat->vort_host) LGX_CUDA(cudaHostAlloc((void**)&lat->vort_host, bytes,
-                                              cudaHostAllocDefault));
+  if (!lat->vort_host) {
+    LGX_CUDA(cudaHostAlloc((void**)&lat->vort_host, bytes, cudaHostAllocMapped));
+    const cudaError_t e = cudaHostGetDevicePointer((void**)&lat->vort, lat->vort_host, 0);
+    if (e != cudaSuccess) {
+      cudaFreeHost(lat->vort_host);
+      lat->vort_host = nullptr;
+      lat->vort = nullptr;
+      LGX_CUDA(e);
+    }
+  }
   *out = lat->vort;
   return LGX_OK;
 }
 
-// Field::vorticity and/or Field::mean_velocity of the attached field: one launch,
-// one copy back of what was asked for (the two sit side by side on the device).
+// Field::vorticity and/or Field::mean_velocity of the attached field: one launch
+// that writes what was asked for into the mapped result buffer, one wait.
 static int field_analyses(lgx_lattice* lat, float* w, float* mx, float* my) {
   float* d = nullptr;
   int rc = field_scratch(lat, &d);
@@ -705,9 +712,6 @@ static int field_analyses(lgx_lattice* lat, float* w, float* mx, float* my) {
   LGX_CUDA(lgx::launch_field_analyses(lat->field, lat->bw, lat->bh, lat->bx, lat->by,
                                       w ? d : nullptr, mean ? d + nb : nullptr, lat->stream));
   lat->launches += 1;
-  const size_t first = w ? 0 : nb, count = (w ? nb : 0) + (mean ? 2 : 0);
-  LGX_CUDA(cudaMemcpyAsync(lat->vort_host + first, d + first, count * 4, cudaMemcpyDeviceToHost,
-                           lat->stream));
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
   if (w) memcpy(w, lat->vort_host, nb * 4);
   if (mean) {

@@ -5,7 +5,8 @@
 
 Cases: `wake` (the 4096 x 2304 wake run), `big` (the roofline case's geometry at
 16384 x 8192: planes of 235 MB, larger than L2, a few GB on the device),
-`sweep` (the 64-lattice transport sweep as one batch), `transport` (one
+`sweep` (the 64-lattice transport sweep as one batch), `analyses` (the field
+vorticity and mean velocity of a 2048 x 1280 lattice, --steps calls), `transport` (one
 transport::measure at --size, density 0.22), `fill` (init_equilibrium on the
 device over the roofline case's geometry at 16384 x 8192), `tiny` (eight --size x
 --size lattices as one batch), `bytes` (the wake run on the reference's
@@ -24,6 +25,8 @@ import sys
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
                                 "lattice-gas_gb300"))
 
+import numpy as np  # noqa: E402
+
 import lattice_gas as LG  # noqa: E402
 from lattice_gas import workloads as W  # noqa: E402
 
@@ -31,7 +34,8 @@ from lattice_gas import workloads as W  # noqa: E402
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="wake",
-                    choices=["wake", "big", "sweep", "transport", "fill", "tiny", "bytes"])
+                    choices=["wake", "big", "sweep", "transport", "fill", "tiny", "bytes",
+                             "analyses"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--policy", type=int, default=0,
                     help="batch policy for the sweep: 0 tuned, 1 one launch per step, 2 resident")
@@ -47,6 +51,21 @@ def main():
         b = LG.Batch(lats, a.policy)
         b.advance(a.steps)
         print("tiny: 8 x %d^2, %d steps, policy %d, plan %s" % (a.size, a.steps, a.policy, b.plan))
+        return
+    if a.case == "analyses":
+        # Field::vorticity and Field::mean_velocity of a 2048 x 1280 lattice's
+        # 20 x 20 field (6,528 blocks), --steps calls of each
+        w, h = 2048, 1280
+        cells = np.zeros(w * h, np.uint8)
+        LG.init_equilibrium(cells, 0.22, 0.4, 0.0, True, 1)
+        g = LG.GpuLattice(w, h, True, 1)
+        g.attach_field(20, 20)
+        g.load(cells)
+        g.advance_sampling(100, 5, 0.2)
+        for _ in range(a.steps):
+            g.mean_velocity()
+            g.vorticity()
+        print("analyses: %d x %d, %d calls each, mean %s" % (w, h, a.steps, g.mean_velocity()))
         return
     if a.case == "bytes":
         wl = W.wake_run()

@@ -77,6 +77,34 @@ def test_batch_equals_each_lattice_alone(LG, n, every, policy):
     b.close()
 
 
+WIDE_SPECS = [  # every lattice a multiple of 4 words per row; 2,560 blocks of 256 words
+    (2048, 1280, True, 40, True, 32, 21),
+    (2048, 1280, False, 8, False, 16, 22),   # six-direction rule: a mixed-rule launch
+    (4096, 640, True, 8, True, 32, 23),
+    (2048, 1280, True, 0, True, 0, 24),
+    (2048, 1280, True, 70, False, 20, 25),
+    (4096, 640, False, 0, True, 16, 26),
+    (2048, 1280, True, 8, True, 32, 27),
+    (2048, 1280, True, 0, False, 16, 28),
+]
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_wide_batch_of_four_word_rows_equals_alone(LG, policy):
+    """Each launch chain covers at least a full wave of blocks and every row is a
+    multiple of four words, so the batched step takes four words per lane."""
+    specs = make(LG, WIDE_SPECS)
+    alone = [build(LG, s) for s in specs]
+    for g in alone:
+        g.advance_sampling(130, 40, 0.4)
+    together = [build(LG, s) for s in specs]
+    b = LG.Batch(together, policy)
+    b.advance_sampling(130, 40, 0.4)
+    for x, y in zip(alone, together):
+        same(snapshot(x), snapshot(y))
+    b.close()
+
+
 def test_resident_policy_plans_small_classes(LG):
     """Every class of up to 32768 words is listed; under BATCH_RESIDENT those with
     a usable cluster shape run resident, under BATCH_PER_STEP none does."""
