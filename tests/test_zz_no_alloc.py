@@ -52,11 +52,13 @@ def dev(torch, a):
     return torch.from_numpy(a.view(np.int32).copy()).cuda()
 
 
-@pytest.mark.parametrize("inlet", [40, 0])
-def test_no_alloc_step_matches_the_lattice_api_twice(LG, inlet):
-    """With a two-word inflow (the scratch in use) and without one."""
+@pytest.mark.parametrize("w,h,inlet", [(300, 64, 40), (300, 64, 0), (4096, 1856, 8)])
+def test_no_alloc_step_matches_the_lattice_api_twice(LG, w, h, inlet):
+    """With a two-word inflow (the scratch in use) and without one, on a small
+    lattice; and a lattice of a full wave of step blocks, whose step takes the
+    kernel shape for large lattices."""
     torch = pytest.importorskip("torch")
-    w, h, rest = 300, 64, True
+    rest = True
     seed = 0xDEADBEEF12345678
     cells = np.zeros(w * h, np.uint8)
     LG.add_circle(cells, w, h, 120.0, 27.0, 9.0)
