@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256 / WORDS, LGX_STEP_MINB) lgx_step_kernel(co
 // three resident blocks of 155 registers, 7.35 / 339; five of 96, draws
 // after the wait, 9.11 / 290.1.  The hash outputs' shifts as multiplies on the
 // FMA pipe: 6.03 / 297.0.
-template <bool REST, int V>
+template <bool REST, int V, bool INFLOW>
 __global__ void __launch_bounds__(128, V == 4 ? 4 : 6) lgx_step_lanes_kernel(const StepArgs p) {
   constexpr int E = V;  // draws made before the wait
   const uint32_t warp = blockIdx.x * 4u + (threadIdx.x >> 5);
@@ -104,8 +104,8 @@ __global__ void __launch_bounds__(128, V == 4 ? 4 : 6) lgx_step_lanes_kernel(con
   for (int q = 0; q < E; ++q) s[q] = draws((gq + q) ^ seed32);
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  step_lane_words<REST, V, E>(p.a, p.b, p.solid, p.anysolid, p.inlet, p.dm, s, seed32, gq,
-                              live);
+  step_lane_words<REST, V, E, INFLOW>(p.a, p.b, p.solid, p.anysolid, p.inlet, p.dm, s, seed32,
+                                      gq, live);
 }
 
 // ---- the persistent multi-step kernel ---------------------------------------
@@ -267,13 +267,23 @@ cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  // the lane shapes come with and without the inflow (its early loads cost
+  // registers: 0.8% on 32768 x 16384 without one, against 2.9% gained on the
+  // wake run and 5.7% at 1024 x 512 with one)
+  const bool in = s.dm.iw != 0u;
   switch (shape) {
     case kShapeLanes4:
-      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4>, s)
-                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4>, s);
+      if (in)
+        return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4, true>, s)
+                    : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4, true>, s);
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4, false>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4, false>, s);
     case kShapeLanes2:
-      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2>, s)
-                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2>, s);
+      if (in)
+        return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2, true>, s)
+                    : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2, true>, s);
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2, false>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2, false>, s);
     case kShapeChunk2:
       return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 2>, s)
                   : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 2>, s);

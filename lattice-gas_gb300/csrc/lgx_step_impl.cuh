@@ -182,8 +182,10 @@ template <> struct LaneWords<4> {
 // predicates, one shuffle per plane and side (the neighbour word inside the
 // lane's group is already in a register), the obstacle summary and the
 // inflow and tail tests.  All 32 lanes call this together with consecutive
-// groups; lanes past the end repeat the last group and do not store.
-template <bool REST, int V, int E>
+// groups; lanes past the end repeat the last group and do not store.  INFLOW
+// false compiles the update without the inflow (for lattices with none: the
+// registers its early loads hold are then free).
+template <bool REST, int V, int E, bool INFLOW = true>
 __device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
                                                 uint32_t* __restrict__ b,
                                                 const uint32_t* __restrict__ solid,
@@ -208,6 +210,16 @@ __device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
   uint32_t w[7][V];
 #pragma unroll
   for (int d = 0; d < 7; ++d) LW::get(__ldg(reinterpret_cast<const VT*>(r[d] + j0)), w[d]);
+  // The inflow's Bernoulli words for the group's first word, loaded with the
+  // planes so that their latency passes during the collision (with V words per
+  // lane every warp of a lattice up to 32 V words wide holds a row start).
+  const bool inflow0 = INFLOW && j0 < dm.iw;
+  uint32_t bern0[7] = {0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  if (inflow0) {
+    const uint32_t* bp = inlet + ((size_t)y * dm.iw + j0) * 7u;
+#pragma unroll
+    for (int d = 0; d < 7; ++d) bern0[d] = __ldg(bp + d);
+  }
 
   const unsigned FULL = 0xffffffffu;
   const bool lok = lane > 0u && j0 > 0u;        // lane - 1 holds words j0-V .. j0-1 of this row
@@ -285,7 +297,7 @@ __device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
     }
   }
 
-  if (j0 < dm.iw) {  // inflow re-seed of the leftmost columns (src/gpu.rs:296-306)
+  if (inflow0) {  // inflow re-seed of the leftmost columns (src/gpu.rs:296-306)
 #pragma unroll
     for (int q = 0; q < V; ++q) {
       const uint32_t j = j0 + q;
@@ -295,7 +307,10 @@ __device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
         const uint32_t apply = imask & ~sw[q];
         const uint32_t* bern = inlet + ((size_t)y * dm.iw + j) * 7u;
 #pragma unroll
-        for (int d = 0; d < 7; ++d) res[d][q] = (res[d][q] & ~apply) | (__ldg(bern + d) & apply);
+        for (int d = 0; d < 7; ++d) {
+          const uint32_t b = q == 0 ? bern0[d] : __ldg(bern + d);
+          res[d][q] = (res[d][q] & ~apply) | (b & apply);
+        }
       }
     }
   }
