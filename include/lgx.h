@@ -267,6 +267,7 @@ typedef struct lgx_batch_class {
   uint32_t threads;     /* and threads per CTA */
   float step_us;        /* tuner's time per step of the class, one launch per step */
   float resident_us;    /* and on the resident kernel (0: no usable shape) */
+  uint32_t steps_per_barrier;  /* the resident kernel's steps between cluster barriers */
 } lgx_batch_class;
 /* The classes of small lattices (larger ones are not listed): *n is their number,
  * the first min(cap, *n) are written. */

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(256 / WORDS, 4 * WORDS) lgx_batch_step_kernel(
 // mapping instead (the branch is uniform across the block).
 // V consecutive words per lane from word gq of lattice d (all 32 lanes of the
 // warp together), the draws made before the wait on the previous step.
-template <int RULE, int V>
+template <int RULE, int V, bool INFLOW>
 __device__ __forceinline__ void batch_lane_words(const BatchStepArgs& p, const LatDesc& d,
                                                  uint32_t gq) {
   const bool live = gq < d.dm.total;
@@ -111,16 +111,17 @@ __device__ __forceinline__ void batch_lane_words(const BatchStepArgs& p, const L
   uint32_t* dst = par ? d.planes[0] : d.planes[1];
   const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)p.k * d.dm.h * d.dm.iw * 7u : nullptr;
   if (RULE == 2 ? d.rest != 0 : RULE == 1)
-    step_lane_words<true, V, V>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq, live);
+    step_lane_words<true, V, V, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
+                                        live);
   else
-    step_lane_words<false, V, V>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
-                                 live);
+    step_lane_words<false, V, V, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32,
+                                         gq, live);
 }
 
 // Four consecutive words per lane in 64-thread blocks (256 words a block).  A
 // block of a lattice whose words per row are not a multiple of four takes four
 // 32-word chunks per warp instead.
-template <int RULE>
+template <int RULE, bool INFLOW>
 __global__ void __launch_bounds__(64, 8) lgx_batch_lanes4_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
@@ -129,10 +130,10 @@ __global__ void __launch_bounds__(64, 8) lgx_batch_lanes4_kernel(BatchStepArgs p
     batch_block<RULE, 4>(p);
     return;
   }
-  batch_lane_words<RULE, 4>(p, d, (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 4u);
+  batch_lane_words<RULE, 4, INFLOW>(p, d, (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 4u);
 }
 
-template <int RULE>
+template <int RULE, bool INFLOW>
 __global__ void __launch_bounds__(128, 6) lgx_batch_lanes_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
@@ -156,10 +157,11 @@ __global__ void __launch_bounds__(128, 6) lgx_batch_lanes_kernel(BatchStepArgs p
   uint32_t* dst = par ? d.planes[0] : d.planes[1];
   const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)p.k * d.dm.h * d.dm.iw * 7u : nullptr;
   if (RULE == 2 ? d.rest != 0 : RULE == 1)
-    step_lane_words<true, 2, 2>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq, live);
+    step_lane_words<true, 2, 2, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
+                                        live);
   else
-    step_lane_words<false, 2, 2>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
-                                 live);
+    step_lane_words<false, 2, 2, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32,
+                                         gq, live);
 }
 
 // Inlet draws for steps base .. base + nsteps - 1 of every lattice with an
@@ -223,6 +225,8 @@ __global__ void lgx_batch_owner_kernel(const uint32_t* block0, uint32_t nlat, ui
 
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st) {
+  const bool inflow = (words & kBatchNoInflow) == 0;
+  words &= ~kBatchNoInflow;
   if (words == 0) words = kBatchLanes2;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
@@ -234,14 +238,24 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (words == kBatchLanes4) {
-    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<2>, a);
-    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<1>, a);
-    return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<0>, a);
+    if (inflow) {
+      if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<2, true>, a);
+      if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<1, true>, a);
+      return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<0, true>, a);
+    }
+    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<2, false>, a);
+    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<1, false>, a);
+    return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<0, false>, a);
   }
   if (words == kBatchLanes2) {
-    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2>, a);
-    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1>, a);
-    return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0>, a);
+    if (inflow) {
+      if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, true>, a);
+      if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, true>, a);
+      return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0, true>, a);
+    }
+    if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, false>, a);
+    if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, false>, a);
+    return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0, false>, a);
   }
   if (words == 2) {
     if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_step_kernel<2, 2>, a);

@@ -63,19 +63,24 @@ struct ResSched {
 // sched), one thread-block cluster each, in one launch.  The batch step
 // before the first of them is *base (null: 0); after local step t the state of
 // a lattice is in planes[(cur0 + t) & 1].  Inlet draws as for the batched step.
+// ksteps > 1 (with clusters of more than one CTA): up to ksteps steps between
+// cluster barriers, each CTA keeping ksteps halo rows on either side of its
+// band and recomputing them; 0 or 1: one cluster barrier per step.
 struct ResidentArgs {
   const LatDesc* descs;
   const ResSched* sched;
   uint32_t first_lat;
   const uint64_t* base;
   uint32_t len;
+  uint32_t ksteps;
 };
 bool resident_config_valid(uint32_t csize, uint32_t threads);
 // Shared memory one CTA of a csize-CTA cluster holds for a lattice (both
-// buffers of its band), and whether the lattice can run resident that way.
+// buffers of its band, with ksteps halo rows either side when ksteps > 1), and
+// whether the lattice can run resident that way (every band at least ksteps rows).
 constexpr size_t kResidentMaxSmem = 200u * 1024u;
-size_t resident_smem_bytes(const Dims& dm, uint32_t csize);
-bool resident_fits(const Dims& dm, uint32_t csize);
+size_t resident_smem_bytes(const Dims& dm, uint32_t csize, uint32_t ksteps = 1);
+bool resident_fits(const Dims& dm, uint32_t csize, uint32_t ksteps = 1);
 // smem: dynamic shared memory per CTA, at least resident_smem_bytes of every
 // lattice of the launch.
 cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
@@ -97,11 +102,17 @@ constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;
 // 971 against 1276 Gsite-updates/s); it pays from one full wave of such blocks
 // up (eight 2048 x 1280 lattices 12.76 -> 11.44 us per step, one 4096 x 2304
 // 6.78 -> 5.97) and loses below it (one 2048 x 1280, 3.05 -> 5.26).
-constexpr int kBatchLanes2 = 3, kBatchLanes4 = 4;
+// kBatchNoInflow, or-ed in: no lattice of the launch has an inflow, so the
+// lane kernels compiled without one run (the inflow's early loads cost
+// registers: the transport sweep, which has none, ran at 1215 with them
+// against 1275 Gsite-updates/s without).
+constexpr int kBatchLanes2 = 3, kBatchLanes4 = 4, kBatchNoInflow = 0x10;
 // The shape a batched step launch of `nblocks` 256-word blocks takes, given
-// whether every lattice it covers has a multiple of 4 words per row.
-inline int batch_step_words(uint32_t nblocks, bool all_wpr4) {
-  return all_wpr4 && nblocks >= 152u * 8u ? kBatchLanes4 : kBatchLanes2;
+// whether every lattice it covers has a multiple of 4 words per row and
+// whether any has an inflow.
+inline int batch_step_words(uint32_t nblocks, bool all_wpr4, bool any_inflow) {
+  return (all_wpr4 && nblocks >= 152u * 8u ? kBatchLanes4 : kBatchLanes2) |
+         (any_inflow ? 0 : kBatchNoInflow);
 }
 cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule, int words,
                               cudaStream_t st);

@@ -41,7 +41,8 @@ struct GraphEntry {
 // that one chain's launch gaps are filled by the others' blocks.
 struct StepGroup {
   uint32_t first = 0, count = 0, nblocks = 0, rest_blocks = 0;
-  bool wpr4 = true;  // every lattice of the chain has a multiple of 4 words per row
+  bool wpr4 = true;     // every lattice of the chain has a multiple of 4 words per row
+  bool inflow = false;  // some lattice of the chain has an inflow
   uint32_t* d_block0 = nullptr;
   uint32_t* d_owner = nullptr;
   cudaStream_t st = nullptr;  // null for the batch's own stream
@@ -132,6 +133,7 @@ cudaError_t build_chains(lgx_batch* b, uint32_t ngroups) {
       gb0.push_back(gb0.back() + block0[i + 1] - block0[i]);
       if (b->lats[i]->rest) sg.rest_blocks = gb0.back();
       sg.wpr4 = sg.wpr4 && b->lats[i]->dm.wpr % 4u == 0u;
+      sg.inflow = sg.inflow || b->lats[i]->dm.iw != 0u;
       ++sg.count;
       ++i;
     }
@@ -246,7 +248,7 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
   cudaStream_t rs = res_branch ? b->side : b->stream;
   for (const ResClass& c : b->classes) {
     if (e != cudaSuccess) break;
-    lgx::ResidentArgs ra{b->d_descs, sched, c.first, b->d_base, len};
+    lgx::ResidentArgs ra{b->d_descs, sched, c.first, b->d_base, len, c.plan.ksteps};
     e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, c.smem, rs);
   }
   for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; ++g) {
@@ -257,7 +259,7 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
       lgx::BatchStepArgs sa{b->d_descs + sg.first, sg.d_block0, sg.d_owner, sg.count,
                             b->d_base, k, 0};
       e = lgx::launch_batch_step(sa, sg.nblocks, step_rule(sg.rest_blocks, sg.nblocks),
-                                 lgx::batch_step_words(sg.nblocks, sg.wpr4), st);
+                                 lgx::batch_step_words(sg.nblocks, sg.wpr4, sg.inflow), st);
       if (e == cudaSuccess && b->hook && b->hook_per_step)
         e = b->hook(b->hook_ctx, st, b->d_base, k + 1);
     }
@@ -400,6 +402,7 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
     bool rest;
     uint32_t count;
     lgx::ClassPlan plan;
+    uint32_t row_words;  // the widest member's words per row: the tuner's shape
   };
   std::vector<Key> keys;
   for (size_t i = 0; i < n && policy != LGX_BATCH_PER_STEP; ++i) {
@@ -407,8 +410,9 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
     const uint32_t wb = lgx::class_bucket(lats[i]->dm.total);
     size_t k = 0;
     while (k < keys.size() && !(keys[k].words == wb && keys[k].rest == lats[i]->rest)) ++k;
-    if (k == keys.size()) keys.push_back({wb, lats[i]->rest, 0, {}});
+    if (k == keys.size()) keys.push_back({wb, lats[i]->rest, 0, {}, 0});
     keys[k].count += 1;
+    keys[k].row_words = std::max(keys[k].row_words, lats[i]->dm.wpr);
     cls[i] = (int)k;
   }
   std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& c) {
@@ -423,17 +427,25 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
   }
   std::vector<bool> res_class(keys.size(), false);
   for (size_t k = 0; k < keys.size() && e == cudaSuccess; ++k) {
-    if (lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, &keys[k].plan) !=
-        cudaSuccess) {
+    if (lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, keys[k].row_words,
+                        &keys[k].plan) != cudaSuccess) {
       // the tuner could not run here (e.g. no room for its synthetic lattices):
       // the class takes one launch per step
       cudaGetLastError();
       keys[k].plan = lgx::ClassPlan{};
     }
-    const lgx::ClassPlan& p = keys[k].plan;
+    lgx::ClassPlan& p = keys[k].plan;
     res_class[k] = policy == LGX_BATCH_RESIDENT ? p.csize != 0 : p.resident;
-    for (size_t i = 0; i < n && res_class[k]; ++i)  // every member's band must fit
-      if (cls[i] == (int)k && !lgx::resident_fits(lats[i]->dm, p.csize)) res_class[k] = false;
+    // every member's band must fit, and hold the halo rows of the class's steps
+    // per cluster barrier (fewer steps per barrier where a member's bands are short)
+    auto all_fit = [&](uint32_t kk) {
+      for (size_t i = 0; i < n; ++i)
+        if (cls[i] == (int)k && !lgx::resident_fits(lats[i]->dm, p.csize, kk)) return false;
+      return true;
+    };
+    if (p.ksteps == 0) p.ksteps = 1;
+    while (res_class[k] && p.ksteps > 1 && !all_fit(p.ksteps)) p.ksteps /= 2;
+    if (res_class[k] && !all_fit(p.ksteps)) res_class[k] = false;
     lgx_batch_class c{};
     c.words = keys[k].words;
     c.lattices = keys[k].count;
@@ -441,6 +453,7 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
     c.resident = res_class[k] ? 1 : 0;
     c.cluster = p.csize;
     c.threads = p.threads;
+    c.steps_per_barrier = p.ksteps;
     c.step_us = p.step_us;
     c.resident_us = p.resident_us;
     b->plan.push_back(c);
@@ -458,7 +471,8 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
     for (size_t i = 0; i < n; ++i)
       if (cls[i] == (int)k) {
         b->lats.push_back(lats[i]);
-        rc.smem = std::max(rc.smem, lgx::resident_smem_bytes(lats[i]->dm, rc.plan.csize));
+        rc.smem = std::max(rc.smem, lgx::resident_smem_bytes(lats[i]->dm, rc.plan.csize,
+                                                             rc.plan.ksteps));
       }
     rc.count = (uint32_t)b->lats.size() - rc.first;
     b->classes.push_back(rc);

@@ -181,10 +181,166 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
   store_band(p.len & 1u, (d.cur0 + (uint32_t)(base + p.len)) & 1u);
 }
 
+// Up to K = p.ksteps steps between cluster barriers (clusters of C > 1 CTAs).
+// CTA r keeps, for each of the two buffers, local rows 0 .. nb + 2K - 1 of its
+// band [y0, y1) widened by K rows either side (local row i is lattice row
+// y0 - K + i, periodic in y).  A super-step of k <= K steps (cut at sampling
+// points and at the end of the launch) begins with a cluster barrier (every
+// band of the current buffer is complete), copies the k rows above and below
+// the band from the neighbouring CTAs' bands (distributed shared memory), and
+// arrives at a second barrier phase: the neighbours may overwrite their
+// current buffer from their second step on, so the CTA waits on that phase
+// after its first step.  Step s of the super-step computes local rows
+// K - k + s .. K + nb + k - s - 1 (one row fewer on each side per step) from
+// the other buffer, with block barriers between steps, so after k steps the
+// band is exact.  Every word's update is the same step_core as everywhere,
+// keyed on the lattice word, so results are bit-identical to single steps.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) lgx_resident_multi_kernel(const ResidentArgs p) {
+  extern __shared__ uint32_t shm[];
+  const cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t C = cluster.num_blocks(), rank = cluster.block_rank();
+  const uint32_t li = p.first_lat + blockIdx.x / C;
+  const LatDesc& d = p.descs[li];
+  const ResSched sch = p.sched[li];
+  const Dims& dm = d.dm;
+  const size_t S = dm.total;
+  const uint32_t K = p.ksteps;
+  const uint32_t y0 = band_start(rank, dm.h, C), y1 = band_start(rank + 1u, dm.h, C);
+  const uint32_t nb = y1 - y0;                    // rows of this band (>= K)
+  const uint32_t cap = (dm.h + C - 1u) / C;       // rows of the largest band
+  const size_t lps = (size_t)(cap + 2u * K) * dm.wpr;  // local plane stride
+  const size_t lbs = 7 * lps;                     // local buffer stride
+  const uint64_t base = p.base ? *p.base : 0ull;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = THREADS / 32;
+  const uint32_t nbf = d.bw * d.bh;
+  const uint32_t bandw = nb * dm.wpr;             // words of the band
+
+  // the band of the state the interval starts from, into local rows K.. of buffer 0
+  {
+    const uint32_t* g = ((d.cur0 + (uint32_t)base) & 1u) ? d.planes[1] : d.planes[0];
+    for (uint32_t i = threadIdx.x; i < bandw; i += THREADS)
+#pragma unroll
+      for (int q = 0; q < 7; ++q)
+        shm[q * lps + (size_t)K * dm.wpr + i] = __ldcg(g + q * S + (size_t)y0 * dm.wpr + i);
+  }
+  auto store_band = [&](uint32_t buf, uint32_t par) {
+    uint32_t* g = par ? d.planes[1] : d.planes[0];
+    for (uint32_t i = threadIdx.x; i < bandw; i += THREADS)
+#pragma unroll
+      for (int q = 0; q < 7; ++q)
+        g[q * S + (size_t)y0 * dm.wpr + i] = shm[buf * lbs + q * lps + (size_t)K * dm.wpr + i];
+  };
+  // The K rows above the band are the last K of rank - 1's band (local rows
+  // nb_up .. nb_up + K - 1 there), the K below the first K of rank + 1's (local
+  // rows K .. 2K - 1); every band has at least K rows.
+  const uint32_t up = (rank + C - 1u) % C, down = (rank + 1u) % C;
+  const uint32_t nb_up = band_start(up + 1u, dm.h, C) - band_start(up, dm.h, C);
+  const uint32_t* up_shm = cluster.map_shared_rank(shm, up);
+  const uint32_t* down_shm = cluster.map_shared_rank(shm, down);
+  auto div_wpr = [&](uint32_t x) {  // x / wpr by the lattice's multiply-shift
+    const uint32_t t = __umulhi(x, dm.div_m);
+    return (t + ((x - t) >> dm.div_s1)) >> dm.div_s2;
+  };
+
+  uint32_t cur = 0;  // the buffer holding the state after step t
+  for (uint32_t t = 0; t < p.len;) {
+    // this super-step: up to K steps, ending at the next sampling point
+    uint32_t k = min(K, p.len - t);
+    if (nbf && sch.every)
+      for (uint32_t s = 1; s < k; ++s)
+        if ((sch.since + t + s) % sch.every == 0u || t + s == sch.left) {
+          k = s;
+          break;
+        }
+    // (1) every band of buffer `cur` is complete (and loaded, before the first)
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    // the k rows on either side of the band, from the neighbours' bands
+    {
+      const uint32_t hw = k * dm.wpr;  // words per plane and side
+      for (uint32_t i = threadIdx.x; i < 7u * hw; i += THREADS) {
+        const uint32_t q = i / hw, w = i - q * hw;
+        const size_t off = cur * lbs + q * lps;
+        shm[off + (size_t)(K - k) * dm.wpr + w] = up_shm[off + (size_t)(K + nb_up - k) * dm.wpr + w];
+        shm[off + (size_t)(K + nb) * dm.wpr + w] = down_shm[off + (size_t)K * dm.wpr + w];
+      }
+    }
+    // (2) done reading the neighbours' buffer `cur`: they may overwrite it
+    // from their second step on, after waiting for this phase
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    __syncthreads();  // the halo rows are in place for every warp
+    for (uint32_t s = 1; s <= k; ++s) {
+      const uint64_t local = base + t + s - 1u;
+      const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
+      const uint32_t* inlet = dm.iw ? d.inlet + (size_t)(t + s - 1u) * dm.h * dm.iw * 7u : nullptr;
+      const uint32_t r0 = K - k + s;                          // first local row
+      const uint32_t nw = (nb + 2u * (k - s)) * dm.wpr;       // words this step
+      const uint32_t nch = (nw + 31u) >> 5;
+      const uint32_t sb = cur, db = cur ^ 1u;
+      for (uint32_t c = warp; c < nch; c += nwarps) {
+        uint32_t lw = c * 32u + lane;
+        const bool live = lw < nw;
+        if (!live) lw = nw - 1u;
+        const uint32_t rr = div_wpr(lw), j = lw - rr * dm.wpr;
+        const uint32_t r = r0 + rr;                           // local row
+        uint32_t y = y0 + dm.h - K + r;                       // lattice row
+        if (y >= dm.h) y -= dm.h;
+        if (y >= dm.h) y -= dm.h;
+        const uint32_t g = y * dm.wpr + j;
+        const uint32_t* src = shm + sb * lbs;
+        const uint32_t* rows[7] = {src + 0 * lps + (size_t)r * dm.wpr,
+                                   src + 1 * lps + (size_t)(r - 1u) * dm.wpr,
+                                   src + 2 * lps + (size_t)(r - 1u) * dm.wpr,
+                                   src + 3 * lps + (size_t)r * dm.wpr,
+                                   src + 4 * lps + (size_t)(r + 1u) * dm.wpr,
+                                   src + 5 * lps + (size_t)(r + 1u) * dm.wpr,
+                                   src + 6 * lps + (size_t)r * dm.wpr};
+        uint32_t* out = shm + db * lbs + (size_t)r * dm.wpr + j;
+        const Draws dr = draws(g ^ seed32);
+        if (d.rest)
+          step_core<true, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, dr, g, y,
+                                      j, live);
+        else
+          step_core<false, LD_GENERIC>(rows, out, lps, d.solid, d.anysolid, inlet, dm, dr, g, y,
+                                       j, live);
+      }
+      cur ^= 1u;
+      __syncthreads();
+      if (s == 1u) asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
+    t += k;
+    // sampling point after step t of this launch: from global memory
+    const bool due = nbf && sch.every && ((sch.since + t) % sch.every == 0u || t == sch.left);
+    if (due) {
+      const uint32_t par = (d.cur0 + (uint32_t)(base + t)) & 1u;
+      store_band(cur, par);
+      cluster.sync();
+      SampleArgs sa;
+      sa.a = par ? d.planes[1] : d.planes[0];
+      sa.solid = d.solid;
+      sa.dm = dm;
+      sa.bx = d.bx;
+      sa.by = d.by;
+      sa.bw = d.bw;
+      sa.bh = d.bh;
+      sa.alpha = d.alpha;
+      sa.ux = d.field;
+      sa.uy = d.field + nbf;
+      sa.rho = d.field + 2 * nbf;
+      sa.sol = d.field + 3 * nbf;
+      sa.sums = d.sums;
+      for (uint32_t b = rank * nwarps + warp; b < nbf; b += C * nwarps) sample_block(sa, b);
+    }
+  }
+  // the state after the interval, to the planes the next launch reads
+  store_band(cur, (d.cur0 + (uint32_t)(base + p.len)) & 1u);
+}
+
 // The kernel attributes a launch needs (16-CTA clusters are an opt-in; dynamic
 // shared memory above 48 KB too), set once per device and kernel: setting them
 // costs host time on every launch otherwise.
-template <int THREADS>
+template <int THREADS, bool MULTI>
 cudaError_t ensure_attributes(size_t smem) {
   constexpr int kMaxDev = 64;
   static std::mutex mu;
@@ -193,16 +349,17 @@ cudaError_t ensure_attributes(size_t smem) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDev) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+  const void* fn = MULTI ? (const void*)lgx_resident_multi_kernel<THREADS>
+                         : (const void*)lgx_resident_kernel<THREADS>;
   std::lock_guard<std::mutex> g(mu);
   if (!wide_set[dev]) {
-    e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
-                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     wide_set[dev] = true;
   }
   if (smem > smem_set[dev]) {
-    e = cudaFuncSetAttribute(lgx_resident_kernel<THREADS>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResidentMaxSmem);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kResidentMaxSmem);
     if (e != cudaSuccess) return e;
     smem_set[dev] = kResidentMaxSmem;
   }
@@ -212,7 +369,9 @@ cudaError_t ensure_attributes(size_t smem) {
 template <int THREADS>
 cudaError_t launch_resident_t(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
                               size_t smem, cudaStream_t st) {
-  cudaError_t e = ensure_attributes<THREADS>(smem);
+  const bool multi = a.ksteps > 1u && csize > 1u;
+  cudaError_t e = multi ? ensure_attributes<THREADS, true>(smem)
+                        : ensure_attributes<THREADS, false>(smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nlat * csize);
@@ -226,6 +385,7 @@ cudaError_t launch_resident_t(const ResidentArgs& a, uint32_t nlat, uint32_t csi
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (multi) return cudaLaunchKernelEx(&cfg, lgx_resident_multi_kernel<THREADS>, a);
   return cudaLaunchKernelEx(&cfg, lgx_resident_kernel<THREADS>, a);
 }
 
@@ -236,13 +396,15 @@ bool resident_config_valid(uint32_t csize, uint32_t threads) {
          (threads == 128 || threads == 256 || threads == 512 || threads == 1024);
 }
 
-size_t resident_smem_bytes(const Dims& dm, uint32_t csize) {
+size_t resident_smem_bytes(const Dims& dm, uint32_t csize, uint32_t ksteps) {
   const size_t cap = (dm.h + csize - 1) / csize;
-  return 2 * 7 * cap * dm.wpr * sizeof(uint32_t);
+  const size_t halo = (ksteps > 1 && csize > 1) ? 2 * (size_t)ksteps : 0;
+  return 2 * 7 * (cap + halo) * dm.wpr * sizeof(uint32_t);
 }
 
-bool resident_fits(const Dims& dm, uint32_t csize) {
-  return dm.h >= 2 * csize && resident_smem_bytes(dm, csize) <= kResidentMaxSmem;
+bool resident_fits(const Dims& dm, uint32_t csize, uint32_t ksteps) {
+  if (dm.h < 2 * csize || resident_smem_bytes(dm, csize, ksteps) > kResidentMaxSmem) return false;
+  return ksteps <= 1 || csize == 1 || dm.h / csize >= ksteps;  // the smallest band
 }
 
 cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,

@@ -326,7 +326,8 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
   const size_t bytes = n * sizeof(lgx::LatDesc) + words * sizeof(uint32_t);
   item0[0] = 0;
   std::vector<uint32_t> nblocks(nch, 0), rest_blocks(nch, 0);
-  std::vector<char> wpr4(nch, 1);  // every lattice of the chain: a multiple of 4 words per row
+  std::vector<char> wpr4(nch, 1);    // every lattice of the chain: a multiple of 4 words per row
+  std::vector<char> inflow(nch, 0);  // some lattice of the chain has an inflow
   for (size_t c = 0; c < nch; ++c) {
     const size_t nc = cfirst[c + 1] - cfirst[c];
     uint32_t* block0 = item0 + off[c];
@@ -358,6 +359,7 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
       block0[q + 1] = block0[q] + words_blocks[i];
       if (r->spec.rest_particles) rest_blocks[c] = block0[q + 1];
       if (r->dm.wpr % 4u) wpr4[c] = 0;
+      if (r->dm.iw) inflow[c] = 1;
       item0[i + 1] = item0[i] + (uint32_t)len * r->dm.h * r->dm.iw;
       for (size_t j = 0; j < m; ++j) blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q];
       due_points(r, len, [&](uint64_t k) {
@@ -410,8 +412,8 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     size_t j = 0;
     for (uint32_t k = 0; k < len && e == cudaSuccess; ++k) {
       lgx::BatchStepArgs sa{dd, d_block0, owner[c], (uint32_t)nc, s->d_zero, k, 0};
-      e = lgx::launch_batch_step(sa, nblocks[c], rule, lgx::batch_step_words(nblocks[c], wpr4[c]),
-                                 st);
+      e = lgx::launch_batch_step(sa, nblocks[c], rule,
+                                 lgx::batch_step_words(nblocks[c], wpr4[c], inflow[c]), st);
       s->launches += 1;
       if (e == cudaSuccess && j < m && pts[j] == k + 1) {
         const uint32_t* tb = blk + j * (nc + 1);

@@ -15,6 +15,7 @@
 // on the word count and the obstacle summary, which is clear.
 #include <cuda_runtime.h>
 
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -37,7 +38,7 @@ constexpr uint32_t kResidentTuneSteps = 128;  // the longest interval a batch la
 constexpr size_t kTuneMaxWords = 4u << 20;  // per-plane words of all synthetic lattices
 
 std::mutex g_mu;
-std::map<std::tuple<int, uint32_t, uint32_t, bool>, ClassPlan> g_plans;
+std::map<std::tuple<int, uint32_t, uint32_t, bool, uint32_t>, ClassPlan> g_plans;
 std::map<std::tuple<int, uint32_t, bool, bool, uint32_t>, StepPlan> g_step_plans;
 
 struct Scratch {
@@ -61,14 +62,18 @@ struct Scratch {
   }
 };
 
-cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
+cudaError_t measure(uint32_t words, uint32_t count, bool rest, uint32_t row_words,
+                    ClassPlan* out) {
   Scratch s;
   cudaError_t e = cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&s.e0);
   if (e == cudaSuccess) e = cudaEventCreate(&s.e1);
   if (e != cudaSuccess) return e;
-  // a lattice of `words` words: 64-word rows (or fewer), an even row count
-  const uint32_t wpr = std::min<uint32_t>(64, std::max<uint32_t>(1, words / 8));
+  // a lattice of `words` words with the class's words per row (at least six
+  // rows), an even row count: the rows set the bands and halos of the resident
+  // kernel, so a 256 x 256 lattice is timed as 8-word rows, not as 64-word ones
+  const uint32_t wpr = std::min<uint32_t>(std::max<uint32_t>(1, row_words),
+                                          std::max<uint32_t>(1, words / 6));
   uint32_t h = std::max<uint32_t>(6, (words + wpr - 1) / wpr);
   h += h & 1u;
   const Dims dm = make_dims(wpr * 32u, h, 0);
@@ -124,7 +129,7 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   for (uint32_t k = 0; k < kTuneSteps && e == cudaSuccess; ++k) {
     BatchStepArgs sa{(const LatDesc*)descs, (const uint32_t*)block0, (const uint32_t*)owner, n,
                      (const uint64_t*)base, k, 0};
-    e = launch_batch_step(sa, b0[n], rule, 0, s.st);
+    e = launch_batch_step(sa, b0[n], rule, kBatchLanes2 | kBatchNoInflow, s.st);
   }
   cudaError_t e2 = cudaStreamEndCapture(s.st, &graph);
   if (e == cudaSuccess) e = e2;
@@ -137,41 +142,52 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   }
   if (e != cudaSuccess) return e;
   out->resident = false;
-  out->csize = out->threads = 0;
+  out->csize = out->threads = out->ksteps = 0;
   out->resident_us = 0;
   out->tuned_count = n;
-  const uint32_t nchunks = (dm.total + 31) / 32;
+  // LGX_RESIDENT_STEPS (1, 2, 4 or 8) pins the steps per cluster barrier of
+  // multi-CTA shapes (and, above 1, leaves out single-CTA ones), for tests and
+  // measurements; otherwise each is timed
+  uint32_t pinned_k = 0;
+  if (const char* v = getenv("LGX_RESIDENT_STEPS")) {
+    const int k = atoi(v);
+    if (k == 1 || k == 2 || k == 4 || k == 8) pinned_k = (uint32_t)k;
+  }
   for (uint32_t cs : {1u, 2u, 4u, 8u, 16u})
-    for (uint32_t th : {128u, 256u, 512u, 1024u}) {
-      const uint32_t warps = cs * th / 32;
-      if (warps > nchunks || warps * 16 < nchunks || !resident_fits(dm, cs)) continue;
-      float us = 0;
-      // one launch of a full interval, as the batch runs it
-      ResidentArgs ra{(const LatDesc*)descs, (const ResSched*)sched, 0, (const uint64_t*)base,
-                      kResidentTuneSteps};
-      const size_t smem = resident_smem_bytes(dm, cs);
-      cudaError_t r =
-          time_it([&]() { return launch_resident(ra, n, cs, th, smem, s.st); }, &us);
-      us *= (float)kTuneSteps / (float)kResidentTuneSteps;
-      if (r != cudaSuccess) {
-        cudaGetLastError();  // a cluster shape this device cannot place: skip it
-        continue;
+    for (uint32_t th : {128u, 256u, 512u, 1024u})
+      for (uint32_t kk : {1u, 2u, 4u, 8u}) {
+        if (kk > 1 && cs == 1) continue;  // one CTA: block barriers only
+        if (pinned_k && (cs > 1 ? kk != pinned_k : pinned_k > 1)) continue;
+        // chunks of one step, the halo rows recomputed included
+        const uint32_t nchunks = (dm.total + cs * 2 * (kk - 1) * dm.wpr + 31) / 32;
+        const uint32_t warps = cs * th / 32;
+        if (warps > nchunks || warps * 16 < nchunks || !resident_fits(dm, cs, kk)) continue;
+        float us = 0;
+        // one launch of a full interval, as the batch runs it
+        ResidentArgs ra{(const LatDesc*)descs, (const ResSched*)sched, 0, (const uint64_t*)base,
+                        kResidentTuneSteps, kk};
+        const size_t smem = resident_smem_bytes(dm, cs, kk);
+        cudaError_t r =
+            time_it([&]() { return launch_resident(ra, n, cs, th, smem, s.st); }, &us);
+        us *= (float)kTuneSteps / (float)kResidentTuneSteps;
+        if (r != cudaSuccess) {
+          cudaGetLastError();  // a cluster shape this device cannot place: skip it
+          continue;
+        }
+        if (out->resident_us == 0 || us < out->resident_us) {
+          out->resident_us = us;
+          out->csize = cs;
+          out->threads = th;
+          out->ksteps = kk;
+        }
       }
-      if (out->resident_us == 0 || us < out->resident_us) {
-        out->resident_us = us;
-        out->csize = cs;
-        out->threads = th;
-      }
-    }
   out->resident = out->resident_us > 0 && out->resident_us < out->step_us;
   return cudaSuccess;
 }
 
 // Microseconds per step of `mode` on the scratch lattice: the median of three
-// runs of about 1.5 ms of steps each (a multiple of 8, at least 8), so that one
-// run caught in a fast or a slow spell of the host (which paces one launch per
-// step on a lattice too small to fill the GPU) does not decide.  <0: the mode
-// failed to run here.
+// runs of about 1.5 ms of steps each (a multiple of 8, at least 8).  <0: the
+// mode failed to run here.
 float time_mode_once(lgx_lattice* t, int mode, uint32_t depth, float est_us);
 
 float time_mode(lgx_lattice* t, int mode, uint32_t depth, float est_us) {
@@ -245,31 +261,50 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
   p.mode = LGX_STEP_SINGLE;
   p.words = kShapeChunk1;
   const float est = time_mode(t, LGX_STEP_SINGLE, 0, 0);
-  // the single-step kernel's shapes: a word per lane in one or two chunks per
-  // warp, and two or four consecutive words per lane where the rows allow
+  // The candidates: the single-step kernel's shapes (a word per lane in one or
+  // two chunks per warp, two or four consecutive words per lane where the rows
+  // allow), the wave kernel, temporal blocking, the one-lattice batch.  They
+  // are timed in interleaved rounds (every candidate once per round) and each
+  // keeps the median of its rounds, so that a fast or slow spell of the host,
+  // which paces one launch per step on lattices that do not fill the GPU,
+  // falls on all of them alike rather than on whichever ran then.
+  struct Cand {
+    int mode;
+    uint32_t depth, shape;
+    float* us;
+  };
+  std::vector<Cand> cands;
   float* shape_us[4] = {&p.single1_us, &p.single2_us, &p.lanes2_us, &p.lanes4_us};
+  for (uint32_t shape = kShapeChunk1; shape <= kShapeLanes4; ++shape)
+    if (step_shape(dm, shape) == shape)
+      cands.push_back({LGX_STEP_SINGLE, 0, shape, shape_us[shape - 1]});
+  cands.push_back({LGX_STEP_WAVE, 0, 0, &p.wave_us});
+  if (wide) {
+    cands.push_back({LGX_STEP_TEMPORAL, 4, 0, &p.temporal4_us});
+    cands.push_back({LGX_STEP_TEMPORAL, 8, 0, &p.temporal8_us});
+  }
+  if (dm.total <= graph_max_words(device)) cands.push_back({LGX_STEP_GRAPH, 0, 0, &p.graph_us});
+  constexpr int kRounds = 5;
+  std::vector<std::vector<float>> runs(cands.size());
+  for (int r = 0; r < kRounds; ++r)
+    for (size_t c = 0; c < cands.size(); ++c) {
+      if (!runs[c].empty() && runs[c].back() < 0) continue;  // failed here: out
+      t->step_words = cands[c].shape;
+      runs[c].push_back(time_mode_once(t, cands[c].mode, cands[c].depth, est));
+    }
+  t->step_words = 0;
+  for (size_t c = 0; c < cands.size(); ++c) {
+    std::vector<float>& v = runs[c];
+    if (v.empty() || v.back() < 0) continue;  // stays 0: not available
+    std::sort(v.begin(), v.end());
+    *cands[c].us = v[v.size() / 2];
+  }
   for (uint32_t shape = kShapeChunk1; shape <= kShapeLanes4; ++shape) {
-    if (step_shape(dm, shape) != shape) continue;
-    t->step_words = shape;
-    const float us = time_mode(t, LGX_STEP_SINGLE, 0, est);
-    *shape_us[shape - 1] = us > 0 ? us : 0;
+    const float us = *shape_us[shape - 1];
     if (us > 0 && (p.single_us <= 0 || us < p.single_us)) {
       p.single_us = us;
       p.words = shape;
     }
-  }
-  t->step_words = 0;
-  const float w_us = time_mode(t, LGX_STEP_WAVE, 0, p.single_us);
-  p.wave_us = w_us > 0 ? w_us : 0;
-  if (wide) {
-    const float t4 = time_mode(t, LGX_STEP_TEMPORAL, 4, p.single_us);
-    const float t8 = time_mode(t, LGX_STEP_TEMPORAL, 8, p.single_us);
-    p.temporal4_us = t4 > 0 ? t4 : 0;
-    p.temporal8_us = t8 > 0 ? t8 : 0;
-  }
-  if (dm.total <= graph_max_words(device)) {
-    const float g = time_mode(t, LGX_STEP_GRAPH, 0, p.single_us);
-    p.graph_us = g > 0 ? g : 0;
   }
   lgx_destroy(t);
   if (p.single_us <= 0) {
@@ -312,11 +347,14 @@ uint32_t class_bucket(uint32_t words) {
   return b;
 }
 
-cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
+cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, uint32_t row_words,
+                       ClassPlan* out) {
   const uint32_t wb = class_bucket(words);
   uint32_t cb = 1;
   while (cb < count) cb <<= 1;
-  const auto key = std::make_tuple(device, wb, cb, rest);
+  uint32_t rb = 1;  // words per row, rounded up to a power of two
+  while (rb < row_words) rb <<= 1;
+  const auto key = std::make_tuple(device, wb, cb, rest, rb);
   {
     std::lock_guard<std::mutex> g(g_mu);
     auto it = g_plans.find(key);
@@ -326,7 +364,7 @@ cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, Cl
     }
   }
   ClassPlan p{};
-  cudaError_t e = measure(wb, cb, rest, &p);
+  cudaError_t e = measure(wb, cb, rest, rb, &p);
   if (e != cudaSuccess) return e;
   p.words = wb;
   p.count = cb;

@@ -77,7 +77,8 @@ class BatchClass(C.Structure):
     """lgx_batch_class: one size class of a batch and the tuner's timings."""
     _fields_ = [("words", C.c_uint32), ("lattices", C.c_uint32), ("rest", C.c_int),
                 ("resident", C.c_int), ("cluster", C.c_uint32), ("threads", C.c_uint32),
-                ("step_us", C.c_float), ("resident_us", C.c_float)]
+                ("step_us", C.c_float), ("resident_us", C.c_float),
+                ("steps_per_barrier", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -1,6 +1,8 @@
 """Batches: many uneven lattices advanced together must give, lattice by
 lattice, exactly what advancing each alone gives (and what the oracle gives).
 Every test here needs a GPU."""
+import os
+
 import numpy as np
 import pytest
 
@@ -189,3 +191,75 @@ def test_batch_rejects_bad_arguments(LG):
         LG.Batch([g, g])
     with pytest.raises(LG.LgxError):
         LG.Batch([])
+
+
+_STEPS_CHILD = r'''
+import os, sys
+import numpy as np
+sys.path.insert(0, os.path.join(sys.argv[1], "lattice-gas_gb300"))
+import lattice_gas as LG
+specs = [  # (w, h, rest, inlet, obstacle, block, seed)
+    (256, 256, True, 0, True, 16, 41),
+    (128, 128, True, 8, False, 8, 42),     # bands of 8 rows on 16 CTAs
+    (100, 96, True, 40, True, 8, 43),      # ragged rows, two-word inflow
+    (300, 64, False, 8, True, 16, 44),     # six-direction rule
+    (1000, 64, True, 0, False, 0, 45),     # no field
+    (64, 36, True, 8, False, 4, 46),       # short bands: fewer steps per barrier
+]
+def build(s):
+    w, h, rest, inlet, obstacle, block, seed = s
+    cells = np.zeros(w * h, np.uint8)
+    if obstacle:
+        LG.add_circle(cells, w, h, w / 3.0, h * 0.43, min(w, h) / 6.0)
+    LG.init_equilibrium(cells, 0.3, 0.15, 0.0, rest, seed)
+    g = LG.GpuLattice(w, h, rest, seed)
+    if inlet:
+        g.set_inlet(inlet, 0.3, (0.15, 0.0), rest)
+    if block:
+        g.attach_field(block, block)
+    g.load(cells)
+    return g
+def snap(g):
+    out = [g.store(), g.steps, g.total_particles()]
+    if g._field is not None:
+        out += list(g.read_block_sums())
+        f = g.read_field()
+        out += [f.ux.copy(), f.uy.copy(), f.rho.copy(), f.solid.copy()]
+    return out
+k = int(os.environ["LGX_RESIDENT_STEPS"])
+for n, every in ((37, 0), (300, 7), (257, 50)):
+    alone = [build(s) for s in specs]
+    for g in alone:
+        g.set_step_mode(1)
+        g.advance_sampling(n, every, 0.4)
+    together = [build(s) for s in specs]
+    b = LG.Batch(together, LG.BATCH_RESIDENT)
+    multi = [c for c in b.plan if c["resident"] and c["cluster"] > 1 and c["steps_per_barrier"] > 1]
+    assert multi, b.plan
+    assert all(c["steps_per_barrier"] <= k for c in b.plan), b.plan
+    b.advance_sampling(n, every, 0.4)
+    for s, x, y in zip(specs, alone, together):
+        for u, v in zip(snap(x), snap(y)):
+            if isinstance(u, np.ndarray):
+                assert np.array_equal(u.view(np.uint8), v.view(np.uint8)), (s, n, every)
+            else:
+                assert u == v, (s, n, every, u, v)
+    b.close()
+print("steps per barrier", k, "ok:", [(c["words"], c["cluster"], c["steps_per_barrier"]) for c in multi])
+'''
+
+
+@pytest.mark.parametrize("k", [2, 4, 8])
+def test_resident_steps_per_cluster_barrier_equal_alone(k):
+    """The resident kernel with k steps between cluster barriers (halo rows
+    recomputed): every lattice as each alone, across sampling points and short
+    bands (where the batch takes fewer steps per barrier).  The tuner caches its
+    plans per process, so the pinned k runs in a child process."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, LGX_RESIDENT_STEPS=str(k))
+    r = subprocess.run([sys.executable, "-c", _STEPS_CHILD, root], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "ok" in r.stdout
