@@ -402,7 +402,6 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
     bool rest;
     uint32_t count;
     lgx::ClassPlan plan;
-    uint32_t row_words;  // the widest member's words per row: the tuner's shape
   };
   std::vector<Key> keys;
   for (size_t i = 0; i < n && policy != LGX_BATCH_PER_STEP; ++i) {
@@ -410,9 +409,8 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
     const uint32_t wb = lgx::class_bucket(lats[i]->dm.total);
     size_t k = 0;
     while (k < keys.size() && !(keys[k].words == wb && keys[k].rest == lats[i]->rest)) ++k;
-    if (k == keys.size()) keys.push_back({wb, lats[i]->rest, 0, {}, 0});
+    if (k == keys.size()) keys.push_back({wb, lats[i]->rest, 0, {}});
     keys[k].count += 1;
-    keys[k].row_words = std::max(keys[k].row_words, lats[i]->dm.wpr);
     cls[i] = (int)k;
   }
   std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& c) {
@@ -427,8 +425,8 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
   }
   std::vector<bool> res_class(keys.size(), false);
   for (size_t k = 0; k < keys.size() && e == cudaSuccess; ++k) {
-    if (lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, keys[k].row_words,
-                        &keys[k].plan) != cudaSuccess) {
+    if (lgx::plan_class(b->device, keys[k].words, keys[k].count, keys[k].rest, &keys[k].plan) !=
+        cudaSuccess) {
       // the tuner could not run here (e.g. no room for its synthetic lattices):
       // the class takes one launch per step
       cudaGetLastError();

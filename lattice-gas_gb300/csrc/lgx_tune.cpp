@@ -38,7 +38,7 @@ constexpr uint32_t kResidentTuneSteps = 128;  // the longest interval a batch la
 constexpr size_t kTuneMaxWords = 4u << 20;  // per-plane words of all synthetic lattices
 
 std::mutex g_mu;
-std::map<std::tuple<int, uint32_t, uint32_t, bool, uint32_t>, ClassPlan> g_plans;
+std::map<std::tuple<int, uint32_t, uint32_t, bool>, ClassPlan> g_plans;
 std::map<std::tuple<int, uint32_t, bool, bool, uint32_t>, StepPlan> g_step_plans;
 
 struct Scratch {
@@ -62,18 +62,17 @@ struct Scratch {
   }
 };
 
-cudaError_t measure(uint32_t words, uint32_t count, bool rest, uint32_t row_words,
-                    ClassPlan* out) {
+cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   Scratch s;
   cudaError_t e = cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&s.e0);
   if (e == cudaSuccess) e = cudaEventCreate(&s.e1);
   if (e != cudaSuccess) return e;
-  // a lattice of `words` words with the class's words per row (at least six
-  // rows), an even row count: the rows set the bands and halos of the resident
-  // kernel, so a 256 x 256 lattice is timed as 8-word rows, not as 64-word ones
-  const uint32_t wpr = std::min<uint32_t>(std::max<uint32_t>(1, row_words),
-                                          std::max<uint32_t>(1, words / 6));
+  // a lattice of `words` words: 64-word rows (or fewer), an even row count.
+  // (Timing each class on its members' own row width instead moved
+  // transport::measure's 256 x 256 class onto the resident kernel, which its
+  // short sampling intervals make slower: 43 -> 49 ms per measure.)
+  const uint32_t wpr = std::min<uint32_t>(64, std::max<uint32_t>(1, words / 8));
   uint32_t h = std::max<uint32_t>(6, (words + wpr - 1) / wpr);
   h += h & 1u;
   const Dims dm = make_dims(wpr * 32u, h, 0);
@@ -347,14 +346,11 @@ uint32_t class_bucket(uint32_t words) {
   return b;
 }
 
-cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, uint32_t row_words,
-                       ClassPlan* out) {
+cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   const uint32_t wb = class_bucket(words);
   uint32_t cb = 1;
   while (cb < count) cb <<= 1;
-  uint32_t rb = 1;  // words per row, rounded up to a power of two
-  while (rb < row_words) rb <<= 1;
-  const auto key = std::make_tuple(device, wb, cb, rest, rb);
+  const auto key = std::make_tuple(device, wb, cb, rest);
   {
     std::lock_guard<std::mutex> g(g_mu);
     auto it = g_plans.find(key);
@@ -364,7 +360,7 @@ cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ui
     }
   }
   ClassPlan p{};
-  cudaError_t e = measure(wb, cb, rest, rb, &p);
+  cudaError_t e = measure(wb, cb, rest, &p);
   if (e != cudaSuccess) return e;
   p.words = wb;
   p.count = cb;

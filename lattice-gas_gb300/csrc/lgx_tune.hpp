@@ -23,11 +23,9 @@ struct ClassPlan {
 // Words per lattice rounded up to the class's power of two (at least 64).
 uint32_t class_bucket(uint32_t words);
 
-// The plan for `count` lattices of up to `words` words with about `row_words`
-// words per row on `device` (the current device), timed on first use and
-// cached for the process (per power of two of words, count and row words).
-cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, uint32_t row_words,
-                       ClassPlan* out);
+// The plan for `count` lattices of up to `words` words on `device` (the
+// current device), timed on first use and cached for the process.
+cudaError_t plan_class(int device, uint32_t words, uint32_t count, bool rest, ClassPlan* out);
 
 // How LGX_STEP_AUTO steps one lattice: the fastest of one launch per step (in
 // each kernel shape that applies, kShape*), the persistent wave kernel, temporal
