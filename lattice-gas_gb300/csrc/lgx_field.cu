@@ -158,7 +158,7 @@ __device__ __forceinline__ float vorticity_at(const float* __restrict__ ux,
 // staged as it is and each solid block's (and the padding's) as -0.0: adding
 // -0.0 leaves every f32 unchanged in round-to-nearest (x + -0 = x,
 // +0 + -0 = +0, -0 + -0 = -0), so the sums are the reference's with no test in
-// the adding loop.  An adding thread reads 64 values ahead of the adds that use
+// the adding loop.  An adding thread reads 32 values ahead of the adds that use
 // them (two register sets), so the chain of f32 adds, not the shared-memory
 // latency, sets its pace.  The reference's count n adds 1.0f per non-solid
 // block: the exact count up to 2^24, where it stops growing; the block counts
@@ -173,15 +173,25 @@ __device__ __forceinline__ uint32_t stage_chunk(const float* __restrict__ ux,
                                                 const float* __restrict__ sol, uint32_t nb,
                                                 uint32_t c0, float* fx, float* fy) {
   const uint32_t t = threadIdx.x - 64u;
-  float vx[kStagePer], vy[kStagePer];
+  float vx[kStagePer], vy[kStagePer], vs[kStagePer];
   uint32_t fluid = 0;
+  // all three loads of every block first, none waiting on another's value: one
+  // memory latency per chunk (the velocity loads once waited on the solid
+  // fraction's, two latencies per row of threads)
 #pragma unroll
   for (uint32_t i = 0; i < kStagePer; ++i) {
     const uint32_t k = t + i * kStagers;
     const bool in = k < kMeanChunk && c0 + k < nb;
-    const bool f = in && __ldg(sol + c0 + k) < 0.5f;
-    vx[i] = f ? __ldg(ux + c0 + k) : -0.0f;
-    vy[i] = f ? __ldg(uy + c0 + k) : -0.0f;
+    const uint32_t at = in ? c0 + k : 0u;
+    vs[i] = in ? __ldg(sol + at) : 1.0f;
+    vx[i] = __ldg(ux + at);
+    vy[i] = __ldg(uy + at);
+  }
+#pragma unroll
+  for (uint32_t i = 0; i < kStagePer; ++i) {
+    const bool f = vs[i] < 0.5f;
+    vx[i] = f ? vx[i] : -0.0f;
+    vy[i] = f ? vy[i] : -0.0f;
     fluid += f ? 1u : 0u;
   }
 #pragma unroll
@@ -195,25 +205,28 @@ __device__ __forceinline__ uint32_t stage_chunk(const float* __restrict__ ux,
   return fluid;
 }
 
-// One chain: s + q[0] + q[1] + ... over `nq` float4s (a multiple of 16), in order.
+// One chain: s + q[0] + q[1] + ... over `nq` float4s (a multiple of kAhead), in
+// order, the next kAhead float4s loaded while the current ones are added (32
+// adds, about 140 cycles, cover a shared-memory load's latency).
+constexpr uint32_t kAhead = 8;
 __device__ __forceinline__ float add_in_order(float s, const float4* q, uint32_t nq) {
-  float4 a[16];
+  float4 a[kAhead];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) a[i] = q[i];
-  for (uint32_t k = 0; k < nq; k += 16u) {
-    const uint32_t kn = k + 16u < nq ? k + 16u : k;  // the last round rereads its own
-    float4 n[16];
+  for (int i = 0; i < (int)kAhead; ++i) a[i] = q[i];
+  for (uint32_t k = 0; k < nq; k += kAhead) {
+    const uint32_t kn = k + kAhead < nq ? k + kAhead : k;  // the last round rereads its own
+    float4 n[kAhead];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) n[i] = q[kn + i];
+    for (int i = 0; i < (int)kAhead; ++i) n[i] = q[kn + i];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
+    for (int i = 0; i < (int)kAhead; ++i) {
       s = __fadd_rn(s, a[i].x);
       s = __fadd_rn(s, a[i].y);
       s = __fadd_rn(s, a[i].z);
       s = __fadd_rn(s, a[i].w);
     }
 #pragma unroll
-    for (int i = 0; i < 16; ++i) a[i] = n[i];
+    for (int i = 0; i < (int)kAhead; ++i) a[i] = n[i];
   }
   return s;
 }
@@ -243,8 +256,13 @@ __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux
                             reinterpret_cast<float*>(s_uy[cur ^ 1u]));
     } else if ((threadIdx.x & 31u) == 0u) {
       const uint32_t len = min(kMeanChunk, nb - c * kMeanChunk);
-      const uint32_t nq = ((len + 63u) & ~63u) / 4u;  // float4s, a multiple of 16
-      sum = add_in_order(sum, threadIdx.x == 0 ? s_ux[cur] : s_uy[cur], nq);
+      const uint32_t nq = ((len + 31u) & ~31u) / 4u;  // float4s, a multiple of kAhead
+      // each thread names its own shared array, so that its loads stay
+      // shared-memory loads (a pointer picked at run time would be generic)
+      if (threadIdx.x == 0)
+        sum = add_in_order(sum, s_ux[cur], nq);
+      else
+        sum = add_in_order(sum, s_uy[cur], nq);
     }
     __syncthreads();
   }
