@@ -91,11 +91,14 @@ WIDE_SPECS = [  # every lattice a multiple of 4 words per row; 2,560 blocks of 2
 ]
 
 
+@pytest.mark.parametrize("inflows", [True, False])
 @pytest.mark.parametrize("policy", [0, 1])
-def test_wide_batch_of_four_word_rows_equals_alone(LG, policy):
+def test_wide_batch_of_four_word_rows_equals_alone(LG, policy, inflows):
     """Each launch chain covers at least a full wave of blocks and every row is a
-    multiple of four words, so the batched step takes four words per lane."""
-    specs = make(LG, WIDE_SPECS)
+    multiple of four words, so the batched step takes four words per lane: with
+    inflows in the chains, and without any (the kernel compiled without them)."""
+    wide = WIDE_SPECS if inflows else [(w, h, r, 0, o, b, s) for w, h, r, _, o, b, s in WIDE_SPECS]
+    specs = make(LG, wide)
     alone = [build(LG, s) for s in specs]
     for g in alone:
         g.advance_sampling(130, 40, 0.4)
