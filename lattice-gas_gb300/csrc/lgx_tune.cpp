@@ -146,7 +146,9 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   out->tuned_count = n;
   // LGX_RESIDENT_STEPS (1, 2, 4 or 8) pins the steps per cluster barrier of
   // multi-CTA shapes (and, above 1, leaves out single-CTA ones), for tests and
-  // measurements; otherwise each is timed
+  // measurements; otherwise 1 and 4 are timed (4 was the best of 2, 4 and 8 on
+  // 256 x 256 lattices, and every shape timed costs the first call of a class:
+  // timing all four made the 22-density transport scan's one call 235 -> 272 ms)
   uint32_t pinned_k = 0;
   if (const char* v = getenv("LGX_RESIDENT_STEPS")) {
     const int k = atoi(v);
@@ -157,6 +159,7 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
       for (uint32_t kk : {1u, 2u, 4u, 8u}) {
         if (kk > 1 && cs == 1) continue;  // one CTA: block barriers only
         if (pinned_k && (cs > 1 ? kk != pinned_k : pinned_k > 1)) continue;
+        if (!pinned_k && kk != 1 && kk != 4) continue;
         // chunks of one step, the halo rows recomputed included
         const uint32_t nchunks = (dm.total + cs * 2 * (kk - 1) * dm.wpr + 31) / 32;
         const uint32_t warps = cs * th / 32;
