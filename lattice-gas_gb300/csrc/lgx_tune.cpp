@@ -148,7 +148,7 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   // multi-CTA shapes (and, above 1, leaves out single-CTA ones), for tests and
   // measurements; otherwise 1 and 4 are timed (4 was the best of 2, 4 and 8 on
   // 256 x 256 lattices, and every shape timed costs the first call of a class:
-  // timing all four made the 22-density transport scan's one call 235 -> 272 ms)
+  // timing all four made the 22-density transport scan's one call 0.22 -> 0.27 s)
   uint32_t pinned_k = 0;
   if (const char* v = getenv("LGX_RESIDENT_STEPS")) {
     const int k = atoi(v);
