@@ -255,7 +255,14 @@ uint32_t step_shape(const Dims& dm, uint32_t shape) {
 
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
-  const uint32_t shape = step_shape(s.dm, s.words);
+  uint32_t shape = step_shape(s.dm, s.words);
+  // The lane shapes move planes and obstacles in 64- or 128-bit accesses, so
+  // they need those buffers 8- or 16-byte aligned.  The engine's own are; a
+  // caller's (lgx_step_planes_noalloc) may be word-aligned only, and then the
+  // word-per-lane shape of the same size runs.
+  const uintptr_t al = (uintptr_t)s.a | (uintptr_t)s.b | (uintptr_t)s.solid;
+  if ((shape == kShapeLanes4 && (al & 15u)) || (shape == kShapeLanes2 && (al & 7u)))
+    shape = s.dm.total >= kTwoChunkMinWords ? kShapeChunk2 : kShapeChunk1;
   cfg.gridDim = dim3((s.dm.total + 255u) / 256u);
   cfg.blockDim = dim3(shape == kShapeChunk1 ? 256 : 128);
   if (shape == kShapeLanes2) cfg.gridDim = dim3((s.dm.total + 255u) / 256u);

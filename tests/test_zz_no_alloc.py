@@ -48,15 +48,23 @@ def unpack(planes, solid, w, h):
     return out[:, :w].reshape(-1)
 
 
-def dev(torch, a):
-    return torch.from_numpy(a.view(np.int32).copy()).cuda()
+def dev(torch, a, offset=0):
+    """a on the device, starting `offset` 32-bit words into its allocation (so that
+    offset 1 gives a buffer aligned to a word but not to 8 or 16 bytes)."""
+    t = torch.zeros(a.size + offset, dtype=torch.int32)
+    t[offset:] = torch.from_numpy(a.view(np.int32).copy())
+    return t.cuda()
 
 
-@pytest.mark.parametrize("w,h,inlet", [(300, 64, 40), (300, 64, 0), (4096, 1856, 8)])
-def test_no_alloc_step_matches_the_lattice_api_twice(LG, w, h, inlet):
+@pytest.mark.parametrize("w,h,inlet,offset", [(300, 64, 40, 0), (300, 64, 0, 0),
+                                              (4096, 1856, 8, 0), (4096, 1856, 8, 1),
+                                              (300, 64, 40, 1)])
+def test_no_alloc_step_matches_the_lattice_api_twice(LG, w, h, inlet, offset):
     """With a two-word inflow (the scratch in use) and without one, on a small
     lattice; and a lattice of a full wave of step blocks, whose step takes the
-    kernel shape for large lattices."""
+    kernel shape for large lattices.  offset 1: the caller's buffers start one
+    word into their allocations, aligned to 4 bytes only (the step then keeps to
+    32-bit accesses)."""
     torch = pytest.importorskip("torch")
     rest = True
     seed = 0xDEADBEEF12345678
@@ -79,20 +87,21 @@ def test_no_alloc_step_matches_the_lattice_api_twice(LG, w, h, inlet):
     # the allocation-free path, two calls in a row on caller-owned buffers
     planes, solid, anysolid = pack(cells, w, h)
     assert np.array_equal(unpack(planes, solid, w, h), cells)
-    a, b = dev(torch, planes), dev(torch, np.zeros_like(planes))
-    s, an = dev(torch, solid), dev(torch, anysolid)
+    a, b = dev(torch, planes, offset), dev(torch, np.zeros_like(planes), offset)
+    s, an = dev(torch, solid, offset), dev(torch, anysolid, offset)
     torch.cuda.synchronize()
     L = LG.lib()
     th = np.ascontiguousarray(thresh, np.uint32)
     src, dst = a, b
+    o = 4 * offset
     for step in range(2):
-        rc = L.lgx_step_planes_noalloc(src.data_ptr(), dst.data_ptr(), s.data_ptr(),
-                                       an.data_ptr(), w, h, int(rest), inlet,
+        rc = L.lgx_step_planes_noalloc(src.data_ptr() + o, dst.data_ptr() + o, s.data_ptr() + o,
+                                       an.data_ptr() + o, w, h, int(rest), inlet,
                                        th.ctypes.data_as(C.POINTER(C.c_uint32)), seed, step,
                                        None)
         assert rc == 0, L.lgx_last_error().decode()
         torch.cuda.synchronize()
-        got = unpack(dst.cpu().numpy().view(np.uint32), solid, w, h)
+        got = unpack(dst.cpu().numpy().view(np.uint32)[offset:], solid, w, h)
         assert np.array_equal(got, want[step]), "step %d differs in %d cells" % (
             step, int((got != want[step]).sum()))
         src, dst = dst, src
