@@ -268,6 +268,8 @@ typedef struct lgx_batch_class {
   float step_us;        /* tuner's time per step of the class, one launch per step */
   float resident_us;    /* and on the resident kernel (0: no usable shape) */
   uint32_t steps_per_barrier;  /* the resident kernel's steps between cluster barriers */
+  int word_per_thread;  /* 1: the resident kernel that keeps each thread on one word of
+                         * its band for the whole launch (every member fits it) */
 } lgx_batch_class;
 /* The classes of small lattices (larger ones are not listed): *n is their number,
  * the first min(cap, *n) are written. */

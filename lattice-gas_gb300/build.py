@@ -24,15 +24,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I" + CSRC, "-I" + INCLUDE]
 SOURCES = ["lgx_step.cu", "lgx_temporal.cu", "lgx_field.cu", "lgx_batch.cu", "lgx_bytes.cu",
-           "lgx_noalloc.cu",
-    "lgx_init.cu",
-    "lgx_profile.cu",
-    "lgx_transport.cpp",
-    "lgx_resident.cu",
-    "lgx_tune.cpp",
-           "lgx_probe.cu",
-           "lgx_lattice.cpp",
-           "lgx_batch_host.cpp", "lgx_server.cpp", "lgx_setup.cpp"]
+           "lgx_noalloc.cu", "lgx_init.cu", "lgx_profile.cu", "lgx_transport.cpp",
+           "lgx_resident.cu", "lgx_resident_fixed.cu", "lgx_tune.cpp", "lgx_probe.cu",
+           "lgx_lattice.cpp", "lgx_batch_host.cpp", "lgx_server.cpp", "lgx_setup.cpp"]
 
 
 def _deps():

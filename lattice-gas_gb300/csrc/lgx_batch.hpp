@@ -81,10 +81,29 @@ bool resident_config_valid(uint32_t csize, uint32_t threads);
 constexpr size_t kResidentMaxSmem = 200u * 1024u;
 size_t resident_smem_bytes(const Dims& dm, uint32_t csize, uint32_t ksteps = 1);
 bool resident_fits(const Dims& dm, uint32_t csize, uint32_t ksteps = 1);
+// The threads a CTA of the fixed-word resident kernels needs for a lattice
+// (one word each: the whole lattice in one CTA, or a band with its recomputed
+// halo rows under ksteps >= 2 steps per cluster barrier), or 0 where those
+// kernels cannot hold it (a plane of a band over 1024 words; clusters of more
+// than one CTA at one step per barrier).  A launch can take them when every
+// lattice's count is nonzero and the largest fits its threads (at most 512).
+constexpr uint32_t kResidentFixedMaxThreads = 512;
+uint32_t resident_fixed_threads(const Dims& dm, uint32_t csize, uint32_t ksteps = 1);
+bool resident_fixed_usable(uint32_t fixed_threads, uint32_t threads);
+// Whether launch_resident takes the fixed-word kernels for a launch of this shape.
+bool resident_runs_fixed(uint32_t fixed_threads, uint32_t csize, uint32_t threads,
+                         uint32_t ksteps);
+// LGX_RESIDENT_FIXED: 0 never the fixed-word kernels, 2 the tuner times only
+// shapes that take them (where a class has any), 1 (unset) the tuner's choice.
+int resident_fixed_mode();
+cudaError_t launch_resident_fixed(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
+                                  uint32_t threads, cudaStream_t st);
 // smem: dynamic shared memory per CTA, at least resident_smem_bytes of every
-// lattice of the launch.
+// lattice of the launch; fixed_threads: the largest resident_fixed_threads of
+// them (0 if any is 0): the fixed-word kernels run where it fits the threads.
 cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
-                            uint32_t threads, size_t smem, cudaStream_t st);
+                            uint32_t threads, size_t smem, uint32_t fixed_threads,
+                            cudaStream_t st);
 
 // The rule of the blocks a batched step launch covers.
 constexpr int kRuleNoRest = 0, kRuleRest = 1, kRuleMixed = 2;

@@ -54,6 +54,7 @@ struct ResClass {
   uint32_t first, count;
   lgx::ClassPlan plan;
   size_t smem;  // shared memory per CTA: the largest member's band
+  uint32_t fixed_threads;  // the largest member's resident_fixed_threads (0: one has none)
 };
 
 int cuda_fail(cudaError_t e, const char* what) {
@@ -249,7 +250,8 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
   for (const ResClass& c : b->classes) {
     if (e != cudaSuccess) break;
     lgx::ResidentArgs ra{b->d_descs, sched, c.first, b->d_base, len, c.plan.ksteps};
-    e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, c.smem, rs);
+    e = lgx::launch_resident(ra, c.count, c.plan.csize, c.plan.threads, c.smem,
+                             c.fixed_threads, rs);
   }
   for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; ++g) {
     const StepGroup& sg = b->groups[g];
@@ -465,13 +467,21 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
   b->nstep = (uint32_t)b->lats.size();
   for (size_t k = 0; k < keys.size(); ++k) {
     if (!res_class[k]) continue;
-    ResClass rc{(uint32_t)b->lats.size(), 0, keys[k].plan, 0};
+    ResClass rc{(uint32_t)b->lats.size(), 0, keys[k].plan, 0, 0};
+    bool fixed = true;
     for (size_t i = 0; i < n; ++i)
       if (cls[i] == (int)k) {
         b->lats.push_back(lats[i]);
         rc.smem = std::max(rc.smem, lgx::resident_smem_bytes(lats[i]->dm, rc.plan.csize,
                                                              rc.plan.ksteps));
+        const uint32_t ft =
+            lgx::resident_fixed_threads(lats[i]->dm, rc.plan.csize, rc.plan.ksteps);
+        fixed = fixed && ft != 0;
+        rc.fixed_threads = std::max(rc.fixed_threads, ft);
       }
+    if (!fixed) rc.fixed_threads = 0;
+    b->plan[k].word_per_thread = lgx::resident_runs_fixed(rc.fixed_threads, rc.plan.csize,
+                                                          rc.plan.threads, rc.plan.ksteps);
     rc.count = (uint32_t)b->lats.size() - rc.first;
     b->classes.push_back(rc);
   }

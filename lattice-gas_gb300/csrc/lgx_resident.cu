@@ -19,6 +19,8 @@
 // launch; clusters the GPU cannot hold at once run when others finish.
 #include <cooperative_groups.h>
 
+#include <stdlib.h>
+
 #include <mutex>
 
 #include "lgx_batch.hpp"
@@ -407,9 +409,29 @@ bool resident_fits(const Dims& dm, uint32_t csize, uint32_t ksteps) {
   return ksteps <= 1 || csize == 1 || dm.h / csize >= ksteps;  // the smallest band
 }
 
+// LGX_RESIDENT_FIXED=0 keeps every launch on the kernels of this file, so that
+// tests and measurements can compare them with the fixed-word kernels.
+int resident_fixed_mode() {
+  static const int mode = [] {
+    const char* v = getenv("LGX_RESIDENT_FIXED");
+    return v && v[0] == '0' ? 0 : v && v[0] == '2' ? 2 : 1;
+  }();
+  return mode;
+}
+static bool fixed_kernels_enabled() { return resident_fixed_mode() != 0; }
+
+bool resident_runs_fixed(uint32_t fixed_threads, uint32_t csize, uint32_t threads,
+                         uint32_t ksteps) {
+  return fixed_kernels_enabled() && resident_fixed_usable(fixed_threads, threads) &&
+         (csize == 1u || ksteps > 1u);
+}
+
 cudaError_t launch_resident(const ResidentArgs& a, uint32_t nlat, uint32_t csize,
-                            uint32_t threads, size_t smem, cudaStream_t st) {
+                            uint32_t threads, size_t smem, uint32_t fixed_threads,
+                            cudaStream_t st) {
   if (nlat == 0 || a.len == 0) return cudaSuccess;
+  if (resident_runs_fixed(fixed_threads, csize, threads, a.ksteps))
+    return launch_resident_fixed(a, nlat, csize, threads, st);
   if (!resident_config_valid(csize, threads) || smem > kResidentMaxSmem)
     return cudaErrorInvalidValue;
   switch (threads) {

@@ -68,11 +68,15 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   if (e == cudaSuccess) e = cudaEventCreate(&s.e0);
   if (e == cudaSuccess) e = cudaEventCreate(&s.e1);
   if (e != cudaSuccess) return e;
-  // a lattice of `words` words: 64-word rows (or fewer), an even row count.
-  // (Timing each class on its members' own row width instead moved
-  // transport::measure's 256 x 256 class onto the resident kernel, which its
-  // short sampling intervals make slower: 43 -> 49 ms per measure.)
-  const uint32_t wpr = std::min<uint32_t>(64, std::max<uint32_t>(1, words / 8));
+  // a square lattice of `words` words (a power of two): rows of
+  // 2^floor((log2 words - 5) / 2) words, as many rows as cells per row or twice
+  // as many, an even row count.  The cluster shapes whose bands fit one word per
+  // thread, and the halo rows that several steps per barrier recompute, depend
+  // on the row width; square lattices are the common case (the transport
+  // measurements, the reference's 256 x 256 benchmark).
+  uint32_t lg = 0;
+  while ((2u << lg) <= words) ++lg;
+  const uint32_t wpr = lg >= 5 ? 1u << ((lg - 5) / 2) : 1u;
   uint32_t h = std::max<uint32_t>(6, (words + wpr - 1) / wpr);
   h += h & 1u;
   const Dims dm = make_dims(wpr * 32u, h, 0);
@@ -154,6 +158,10 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
     const int k = atoi(v);
     if (k == 1 || k == 2 || k == 4 || k == 8) pinned_k = (uint32_t)k;
   }
+  // LGX_RESIDENT_FIXED=2 (tests): only the shapes that run on the fixed-word
+  // kernels, where the class has any
+  const bool only_fixed = resident_fixed_mode() == 2;
+  for (int pass = only_fixed ? 0 : 1; pass < 2 && out->resident_us == 0; ++pass)
   for (uint32_t cs : {1u, 2u, 4u, 8u, 16u})
     for (uint32_t th : {128u, 256u, 512u, 1024u})
       for (uint32_t kk : {1u, 2u, 4u, 8u}) {
@@ -163,14 +171,24 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
         // chunks of one step, the halo rows recomputed included
         const uint32_t nchunks = (dm.total + cs * 2 * (kk - 1) * dm.wpr + 31) / 32;
         const uint32_t warps = cs * th / 32;
-        if (warps > nchunks || warps * 16 < nchunks || !resident_fits(dm, cs, kk)) continue;
+        // the fixed-word kernels take one word per thread: only the smallest
+        // block that holds a CTA's words is worth timing
+        const uint32_t ft = resident_fixed_threads(dm, cs, kk);
+        if (resident_runs_fixed(ft, cs, th, kk)) {
+          if (th > 128 && ft <= th / 2) continue;
+        } else if (pass == 0 || warps > nchunks || warps * 16 < nchunks) {
+          continue;
+        }
+        if (!resident_fits(dm, cs, kk)) continue;
         float us = 0;
         // one launch of a full interval, as the batch runs it
         ResidentArgs ra{(const LatDesc*)descs, (const ResSched*)sched, 0, (const uint64_t*)base,
                         kResidentTuneSteps, kk};
         const size_t smem = resident_smem_bytes(dm, cs, kk);
         cudaError_t r =
-            time_it([&]() { return launch_resident(ra, n, cs, th, smem, s.st); }, &us);
+            time_it([&]() {
+              return launch_resident(ra, n, cs, th, smem, ft, s.st);
+            }, &us);
         us *= (float)kTuneSteps / (float)kResidentTuneSteps;
         if (r != cudaSuccess) {
           cudaGetLastError();  // a cluster shape this device cannot place: skip it

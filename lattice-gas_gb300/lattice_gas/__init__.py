@@ -78,7 +78,7 @@ class BatchClass(C.Structure):
     _fields_ = [("words", C.c_uint32), ("lattices", C.c_uint32), ("rest", C.c_int),
                 ("resident", C.c_int), ("cluster", C.c_uint32), ("threads", C.c_uint32),
                 ("step_us", C.c_float), ("resident_us", C.c_float),
-                ("steps_per_barrier", C.c_uint32)]
+                ("steps_per_barrier", C.c_uint32), ("word_per_thread", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

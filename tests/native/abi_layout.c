@@ -25,7 +25,7 @@ int main(void) {
   F(lgx_batch_class, words); F(lgx_batch_class, lattices); F(lgx_batch_class, rest);
   F(lgx_batch_class, resident); F(lgx_batch_class, cluster); F(lgx_batch_class, threads);
   F(lgx_batch_class, step_us); F(lgx_batch_class, resident_us);
-  F(lgx_batch_class, steps_per_barrier);
+  F(lgx_batch_class, steps_per_barrier); F(lgx_batch_class, word_per_thread);
   END();
   BEGIN("lgx_transport", lgx_transport);
   F(lgx_transport, nu); F(lgx_transport, g); F(lgx_transport, window_nu);

@@ -230,6 +230,7 @@ def snap(g):
         out += [f.ux.copy(), f.uy.copy(), f.rho.copy(), f.solid.copy()]
     return out
 k = int(os.environ["LGX_RESIDENT_STEPS"])
+fixed = os.environ["LGX_RESIDENT_FIXED"]
 for n, every in ((37, 0), (300, 7), (257, 50)):
     alone = [build(s) for s in specs]
     for g in alone:
@@ -238,8 +239,17 @@ for n, every in ((37, 0), (300, 7), (257, 50)):
     together = [build(s) for s in specs]
     b = LG.Batch(together, LG.BATCH_RESIDENT)
     multi = [c for c in b.plan if c["resident"] and c["cluster"] > 1 and c["steps_per_barrier"] > 1]
-    assert multi, b.plan
+    assert multi or k == 1, b.plan
     assert all(c["steps_per_barrier"] <= k for c in b.plan), b.plan
+    per_thread = [c for c in b.plan if c["resident"] and c["word_per_thread"]]
+    if fixed == "0":
+        assert not per_thread, b.plan
+    else:
+        assert per_thread, b.plan
+        if k > 1:
+            assert any(c["cluster"] > 1 for c in per_thread), b.plan
+    summary = [(c["words"], c["cluster"], c["threads"], c["steps_per_barrier"],
+                c["word_per_thread"]) for c in b.plan if c["resident"]]
     b.advance_sampling(n, every, 0.4)
     for s, x, y in zip(specs, alone, together):
         for u, v in zip(snap(x), snap(y)):
@@ -248,20 +258,24 @@ for n, every in ((37, 0), (300, 7), (257, 50)):
             else:
                 assert u == v, (s, n, every, u, v)
     b.close()
-print("steps per barrier", k, "ok:", [(c["words"], c["cluster"], c["steps_per_barrier"]) for c in multi])
+print("steps per barrier", k, "fixed", fixed, "ok:", summary)
 '''
 
 
-@pytest.mark.parametrize("k", [2, 4, 8])
-def test_resident_steps_per_cluster_barrier_equal_alone(k):
-    """The resident kernel with k steps between cluster barriers (halo rows
+@pytest.mark.parametrize("fixed", ["0", "2"])
+@pytest.mark.parametrize("k", [1, 2, 4, 8])
+def test_resident_steps_per_cluster_barrier_equal_alone(k, fixed):
+    """The resident kernels with k steps between cluster barriers (halo rows
     recomputed): every lattice as each alone, across sampling points and short
-    bands (where the batch takes fewer steps per barrier).  The tuner caches its
-    plans per process, so the pinned k runs in a child process."""
+    bands (where the batch takes fewer steps per barrier); on the kernels that
+    keep each thread on one word of its band (fixed "2": the tuner times only
+    shapes that take them) and on the others (fixed "0").  k = 1 covers the
+    single-CTA shapes.  The tuner caches its plans per process, so each pinned
+    setting runs in a child process."""
     import subprocess
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    env = dict(os.environ, LGX_RESIDENT_STEPS=str(k))
+    env = dict(os.environ, LGX_RESIDENT_STEPS=str(k), LGX_RESIDENT_FIXED=fixed)
     r = subprocess.run([sys.executable, "-c", _STEPS_CHILD, root], env=env, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
