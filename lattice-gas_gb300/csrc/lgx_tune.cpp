@@ -150,9 +150,11 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
   out->tuned_count = n;
   // LGX_RESIDENT_STEPS (1, 2, 4 or 8) pins the steps per cluster barrier of
   // multi-CTA shapes (and, above 1, leaves out single-CTA ones), for tests and
-  // measurements; otherwise 1 and 4 are timed (4 was the best of 2, 4 and 8 on
-  // 256 x 256 lattices, and every shape timed costs the first call of a class:
-  // timing all four made the 22-density transport scan's one call 0.22 -> 0.27 s)
+  // measurements; otherwise 1 and 4 are timed, and 8 on the fixed-word kernels
+  // (on the others 4 was the best of 2, 4 and 8 on 256 x 256 lattices, and every
+  // shape timed costs the first call of a class: timing all four made the
+  // 22-density transport scan's one call 0.22 -> 0.27 s; the fixed-word kernels
+  // gain from 4 to 8, one 256 x 256 lattice 1.11 -> 1.02 us per step)
   uint32_t pinned_k = 0;
   if (const char* v = getenv("LGX_RESIDENT_STEPS")) {
     const int k = atoi(v);
@@ -167,14 +169,15 @@ cudaError_t measure(uint32_t words, uint32_t count, bool rest, ClassPlan* out) {
       for (uint32_t kk : {1u, 2u, 4u, 8u}) {
         if (kk > 1 && cs == 1) continue;  // one CTA: block barriers only
         if (pinned_k && (cs > 1 ? kk != pinned_k : pinned_k > 1)) continue;
-        if (!pinned_k && kk != 1 && kk != 4) continue;
+        const uint32_t ft = resident_fixed_threads(dm, cs, kk);
+        const bool fx = resident_runs_fixed(ft, cs, th, kk);
+        if (!pinned_k && kk != 1 && kk != 4 && !(kk == 8 && fx)) continue;
         // chunks of one step, the halo rows recomputed included
         const uint32_t nchunks = (dm.total + cs * 2 * (kk - 1) * dm.wpr + 31) / 32;
         const uint32_t warps = cs * th / 32;
         // the fixed-word kernels take one word per thread: only the smallest
         // block that holds a CTA's words is worth timing
-        const uint32_t ft = resident_fixed_threads(dm, cs, kk);
-        if (resident_runs_fixed(ft, cs, th, kk)) {
+        if (fx) {
           if (th > 128 && ft <= th / 2) continue;
         } else if (pass == 0 || warps > nchunks || warps * 16 < nchunks) {
           continue;
@@ -353,9 +356,11 @@ int plan_step_mode(int device, uint32_t w, uint32_t h, bool rest, StepPlan* out)
   }
   // Graph replays do not depend on the host keeping ahead of the GPU, as one
   // launch per step does on these lattices (its rate moves with the host's
-  // load: 3.3 to 5.0 us per step at 2048 x 1280 across runs), so they win ties
-  // within 5%.
-  if (p.graph_us > 0 && p.graph_us < 1.05f * best) {
+  // load: 3.3 to 5.0 us per step at 2048 x 1280 across runs, and within one
+  // process the tuner once timed one launch per step at 3.73 against 4.13 us for
+  // graphs, then ran it at 4.9 us per step where graphs run at 4.0), so they win
+  // ties within 15%.
+  if (p.graph_us > 0 && p.graph_us < 1.15f * best) {
     best = p.graph_us;
     p.mode = LGX_STEP_GRAPH;
     p.depth = 0;
