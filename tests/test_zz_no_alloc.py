@@ -121,3 +121,59 @@ def test_no_alloc_refuses_an_inflow_beyond_its_scratch(LG):
     rc = L.lgx_step_planes_noalloc(x.data_ptr(), y.data_ptr(), s.data_ptr(), an.data_ptr(), w,
                                    h, 1, 96, th.ctypes.data_as(C.POINTER(C.c_uint32)), 1, 0, None)
     assert rc == 1 and b"scratch" in L.lgx_last_error()
+
+
+def test_no_alloc_steps_replay_from_a_cuda_graph(LG):
+    """A warm-up call (the scratch address is looked up there), then two calls,
+    a -> b at step 0 and b -> a at step 1, captured into one CUDA graph on a torch
+    stream: each replay from the starting planes gives both steps bit for bit as
+    the allocating path does (the inflow's scratch is written and read inside the
+    graph, in stream order)."""
+    torch = pytest.importorskip("torch")
+    w, h, inlet, rest, seed = 300, 64, 40, True, 0x1234ABCD9876
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, 120.0, 27.0, 9.0)
+    LG.init_equilibrium(cells, 0.3, 0.2, 0.0, rest, 43)
+    thresh = np.ascontiguousarray(LG.thresholds(0.3, 0.2, 0.0, rest), np.uint32)
+    g = LG.GpuLattice(w, h, rest, seed)
+    g.set_step_mode(g.STEP_SINGLE)
+    g.set_inlet(inlet, 0.3, (0.2, 0.0), rest)
+    g.load(cells)
+    want = []
+    for _ in range(2):
+        g.advance(1)
+        want.append(g.store())
+
+    planes, solid, anysolid = pack(cells, w, h)
+    a, b = dev(torch, planes), dev(torch, np.zeros_like(planes))
+    s, an = dev(torch, solid), dev(torch, anysolid)
+    start = a.clone()
+    L = LG.lib()
+    tp = thresh.ctypes.data_as(C.POINTER(C.c_uint32))
+
+    def call(src, dst, step, stream):
+        rc = L.lgx_step_planes_noalloc(src.data_ptr(), dst.data_ptr(), s.data_ptr(),
+                                       an.data_ptr(), w, h, int(rest), inlet, tp, seed, step,
+                                       C.c_void_p(stream.cuda_stream))
+        assert rc == 0, L.lgx_last_error().decode()
+
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        call(a, b, 0, st)
+    st.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=st):
+        call(a, b, 0, st)
+        call(b, a, 1, st)
+    for _ in range(2):
+        a.copy_(start)
+        b.zero_()
+        torch.cuda.synchronize()
+        graph.replay()
+        torch.cuda.synchronize()
+        got0 = unpack(b.cpu().numpy().view(np.uint32), solid, w, h)
+        got1 = unpack(a.cpu().numpy().view(np.uint32), solid, w, h)
+        assert np.array_equal(got0, want[0]), "step 0 differs in %d cells" % int(
+            (got0 != want[0]).sum())
+        assert np.array_equal(got1, want[1]), "step 1 differs in %d cells" % int(
+            (got1 != want[1]).sum())
