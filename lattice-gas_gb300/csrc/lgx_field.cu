@@ -3,6 +3,10 @@
 //
 // Coarse-graining (lgca_sample, src/gpu.rs:324-377): one warp per block of the
 // field (sample_block in lgx_step_impl.cuh).
+#include <limits.h>
+#include <stddef.h>
+#include <stdlib.h>
+
 #include "lgx_device.cuh"
 #include "lgx_internal.hpp"
 #include "lgx_reduce.cuh"
@@ -231,14 +235,28 @@ __device__ __forceinline__ float add_in_order(float s, const float4* q, uint32_t
   return s;
 }
 
+// The sum over a block of kAnalysisThreads threads' counts, on thread 0: each
+// warp adds its own (one reduction instruction), thread 0 adds the warps'.  (A
+// 64-bit shared-memory atomicAdd from every thread serialises: it cost about 25k
+// cycles per block.)
+__device__ __forceinline__ unsigned long long block_count(uint32_t v, uint32_t* s_warp) {
+  const uint32_t w = __reduce_add_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31u) == 0u) s_warp[threadIdx.x >> 5] = w;
+  __syncthreads();
+  unsigned long long c = 0;
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (uint32_t i = 0; i < kAnalysisThreads / 32; ++i) c += s_warp[i];
+  return c;
+}
+
 __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux,
                                                     const float* __restrict__ uy,
                                                     const float* __restrict__ sol, uint32_t nb,
                                                     float* __restrict__ out) {
   __shared__ float4 s_ux[2][kMeanChunk / 4], s_uy[2][kMeanChunk / 4];
-  __shared__ unsigned long long s_count;
+  __shared__ uint32_t s_warp[kAnalysisThreads / 32];
   __shared__ float s_sy;
-  if (threadIdx.x == 0) s_count = 0;
   float sum = 0.0f;  // x on thread 0, y on thread 32
   uint32_t mine = 0;
   const bool stager = threadIdx.x >= 64u;
@@ -267,10 +285,8 @@ __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux
     __syncthreads();
   }
   if (threadIdx.x == 32) s_sy = sum;
-  atomicAdd(&s_count, (unsigned long long)mine);
-  __syncthreads();
+  const unsigned long long c = block_count(mine, s_warp);  // its barrier orders s_sy too
   if (threadIdx.x == 0) {
-    const unsigned long long c = s_count;
     const float n = c <= (1ull << 24) ? (float)c : 16777216.0f;
     out[0] = n == 0.0f ? 0.0f : __fdiv_rn(sum, n);
     out[1] = n == 0.0f ? 0.0f : __fdiv_rn(s_sy, n);
@@ -296,14 +312,264 @@ __global__ void __launch_bounds__(kAnalysisThreads) lgx_field_analyses_kernel(
   if (vort && k < bw * bh) vort[k] = vorticity_at(ux, uy, k, bw, bh, dx, dy);
 }
 
+// ---- the mean velocity's sums in segments, speculatively ----
+//
+// The sums must come out as the reference's in-order f32 additions, which is one
+// chain of dependent adds (4.1 cycles each on GB300: 13 us for 6,528 blocks).  The
+// field's nb values are cut into k <= 16 segments of L values.  Segment 0 is summed
+// from +0 as the reference sums it.  For every later segment j and each of the two
+// sums, kSpecParts blocks sum the segment in order from kSpecGuesses consecutive f32
+// start values (one per thread) centred on the exact sum of the values before it; the in-order f32 partial sum differs from that exact sum by its
+// accumulated rounding, usually a few to a few hundred units in the last place.
+// The last of these blocks to finish walks the segments: with the exact partial
+// sum s at the start of segment j, the thread whose start value is s (found by the
+// distance in representable floats from the centre) has summed segment j exactly
+// as the reference would have, so its end value is the exact partial sum at the
+// next segment; where s is not among the guesses (or is not finite) the segment is
+// summed from s in order instead.  Every path adds the same values in the same
+// order with the same roundings, so the result is bit-equal to the chain.  Solid
+// blocks enter as -0.0, as in the chained kernel above.
+constexpr uint32_t kSpecGuesses = 1024;      // start values per segment and sum
+constexpr uint32_t kSpecParts = kSpecGuesses / kAnalysisThreads;  // blocks per segment and sum
+constexpr uint32_t kSpecMaxSegments = 16;
+constexpr uint32_t kSpecMinSegment = 512;    // values per segment, at least
+constexpr uint32_t kSpecMaxSegment = 4096;
+constexpr uint32_t kSpecMaxBlocks = kSpecMaxSegments * kSpecMaxSegment;  // 65,536
+
+// Device scratch of one field's segmented sums, zeroed once before its first use
+// (the block counter returns to zero at the end of every launch).
+struct MeanScratch {
+  unsigned int counter;
+  unsigned int pad;
+  unsigned long long fluid;
+  float first[2];
+  float pad2[2];
+  int center[2][kSpecMaxSegments];  // the centre's order index (INT_MIN: none usable)
+  float table[2][kSpecMaxSegments][kSpecGuesses];  // 16-byte aligned: offset 160
+};
+static_assert(offsetof(MeanScratch, table) % 16 == 0, "the tables are read as float4s");
+
+// A float's index in the order of representable floats (-0.0 and +0.0 both 0).
+__device__ __forceinline__ int f_order(float f) {
+  const int b = __float_as_int(f);
+  return b >= 0 ? b : -(b & 0x7fffffff);
+}
+__device__ __forceinline__ float f_from_order(int o) {
+  if (o > 0x7f7fffff || o < -0x7f7fffff) return __int_as_float(0x7fc00000);  // past the finite
+  return o >= 0 ? __int_as_float(o) : __int_as_float((-o) | (int)0x80000000);
+}
+
+// A field block's value in the sum: its velocity component, -0.0 where solid
+// (both loads issued before either is looked at, so a loop keeps them in flight).
+__device__ __forceinline__ float mean_term(const float* __restrict__ u,
+                                           const float* __restrict__ sol, uint32_t i) {
+  const float s = __ldg(sol + i), v = __ldg(u + i);
+  return s < 0.5f ? v : -0.0f;
+}
+
+// values [i0, i0 + len) of the masked component into dst[0 .. round up to 32),
+// padded with -0.0; returns the float4 count (a multiple of kAhead)
+__device__ __forceinline__ uint32_t stage_terms(const float* __restrict__ u,
+                                                const float* __restrict__ sol, uint32_t i0,
+                                                uint32_t len, float* dst) {
+  const uint32_t padded = (len + 31u) & ~31u;
+  for (uint32_t i = threadIdx.x; i < padded; i += kAnalysisThreads)
+    dst[i] = i < len ? mean_term(u, sol, i0 + i) : -0.0f;
+  return padded / 4u;
+}
+
+// The combining block copies, for every segment, the kSpecWindow table entries
+// around the centre into shared memory in one round of loads (almost every walk
+// lands there); an entry outside that window is read from L2.
+constexpr uint32_t kSpecWindow = 256;
+constexpr uint32_t kSpecWindowWords = 2u * (kSpecMaxSegments - 1u) * kSpecWindow;
+constexpr uint32_t kSpecShared = kSpecWindowWords + kSpecMaxSegment;
+
+__device__ __forceinline__ void mean_spec_block(const float* __restrict__ ux,
+                                                const float* __restrict__ uy,
+                                                const float* __restrict__ sol, uint32_t nb,
+                                                uint32_t L, uint32_t k, uint32_t b,
+                                                MeanScratch* ms, float* out, int mode) {
+  // a segment's values (block 0: both sums' segment 0, x at 0 and y at 4096); in
+  // the combining block the table windows, then at kSpecWindowWords a segment to sum
+  __shared__ __align__(16) float s_mem[kSpecShared];
+  __shared__ int s_center[2][kSpecMaxSegments];
+  __shared__ long long s_red[kAnalysisThreads / 32];
+  __shared__ uint32_t s_warp[kAnalysisThreads / 32];
+  __shared__ float s_res[2];
+  __shared__ int s_hit[2];
+  __shared__ bool s_last;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t G = kSpecGuesses;
+  if (b == 0) {
+    const uint32_t len = min(L, nb);
+    const uint32_t nq = stage_terms(ux, sol, 0, len, s_mem);
+    stage_terms(uy, sol, 0, len, s_mem + kSpecMaxSegment);
+    uint32_t fluid = 0;
+#pragma unroll 8
+    for (uint32_t i = tid; i < nb; i += kAnalysisThreads) fluid += __ldg(sol + i) < 0.5f ? 1u : 0u;
+    const unsigned long long count = block_count(fluid, s_warp);  // and the staging is done
+    if (tid == 0 || tid == 32) {
+      const float s = tid ? add_in_order(0.0f, reinterpret_cast<const float4*>(s_mem + kSpecMaxSegment), nq)
+                          : add_in_order(0.0f, reinterpret_cast<const float4*>(s_mem), nq);
+      ms->first[tid ? 1 : 0] = s;
+    }
+    if (tid == 0) ms->fluid = count;
+  } else {
+    const uint32_t q = (b - 1u) / kSpecParts, part = (b - 1u) - q * kSpecParts;
+    const uint32_t z = q / (k - 1u);                // 0: x, 1: y
+    const uint32_t j = q - z * (k - 1u) + 1u;        // segment 1 .. k-1
+    const uint32_t gi = part * kAnalysisThreads + tid;  // this thread's guess
+    const float* u = z ? uy : ux;
+    const uint32_t i0 = j * L, len = min(L, nb - i0);
+    // the sum of the values before the segment in 64-bit fixed point (units of
+    // 2^-40: within n * 2^-41 of the exact sum, no overflow for |values| < 64 and
+    // n <= 2^16; FP64 is slow here), in a fixed order; a value out of that range
+    // leaves no centre
+    long long acc = 0;
+    bool bad = false;
+    for (uint32_t i = tid; i < i0; i += 24u * kAnalysisThreads) {  // 48 loads in flight
+      float v[24], sv[24];
+#pragma unroll
+      for (uint32_t q = 0; q < 24; ++q) {
+        const uint32_t ii = i + q * kAnalysisThreads;
+        const bool in = ii < i0;
+        sv[q] = in ? __ldg(sol + ii) : 1.0f;
+        v[q] = in ? __ldg(u + ii) : 0.0f;
+      }
+#pragma unroll
+      for (uint32_t q = 0; q < 24; ++q) {
+        const float t = sv[q] < 0.5f ? v[q] : 0.0f;
+        bad |= !(fabsf(t) < 64.0f);
+        acc += __float2ll_rn(__fmul_rn(t, 1099511627776.0f));
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_red[warp] = acc;
+    const uint32_t nq = stage_terms(u, sol, i0, len, s_mem);
+    const bool anybad = __syncthreads_or(bad);  // and the segment is staged
+    long long pre = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kAnalysisThreads / 32; ++w) pre += s_red[w];
+    const float c = anybad ? __int_as_float(0x7fc00000)
+                           : __fmul_rn(__ll2float_rn(pre), 9.094947017729282e-13f);  // 2^-40
+    const int co = f_order(c);
+    const float start = f_from_order(co + (int)gi - (int)(G / 2u));
+    ms->table[z][j][gi] = add_in_order(start, reinterpret_cast<const float4*>(s_mem), nq);
+    if (tid == 0 && part == 0) ms->center[z][j] = isfinite(c) ? co : INT_MIN;
+  }
+  // the last of the 1 + 2 (k - 1) kSpecParts blocks to finish combines
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = atomicAdd(&ms->counter, 1u) == 2u * (k - 1u) * kSpecParts;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // what the walk reads, in one round of loads: the table windows around the
+  // centres, the centres, segment 0's sums
+  constexpr uint32_t W4 = kSpecWindow / 4u, w0 = (kSpecGuesses - kSpecWindow) / 2u;
+  for (uint32_t i = tid; i < 2u * (k - 1u) * W4; i += kAnalysisThreads) {
+    const uint32_t r = i / W4, z = r / (k - 1u), j = r - z * (k - 1u) + 1u;
+    reinterpret_cast<float4*>(s_mem)[i] =
+        __ldcg(reinterpret_cast<const float4*>(&ms->table[z][j][w0]) + (i - r * W4));
+  }
+  if (tid < 2u * kSpecMaxSegments)
+    s_center[tid / kSpecMaxSegments][tid % kSpecMaxSegments] =
+        __ldcg(&ms->center[tid / kSpecMaxSegments][tid % kSpecMaxSegments]);
+  if (tid < 2) s_res[tid] = __ldcg(&ms->first[tid]);
+  __syncthreads();
+  // the walk: threads 0 and 1 follow the x and the y sum through the tables,
+  // segment after segment, until a segment whose start is not among its guesses;
+  // the whole block then stages that segment and thread 0 sums it in order
+  float* seg = s_mem + kSpecWindowWords;
+  if (tid < 2) s_hit[tid] = 1;  // s_hit[z]: the next segment of sum z to walk
+  __syncthreads();
+  for (;;) {
+    if (tid < 2) {
+      uint32_t j = (uint32_t)s_hit[tid];
+      float s = s_res[tid];
+      for (; j < k; ++j) {
+        const int c = s_center[tid][j];
+        const long long o = (long long)f_order(s) - (long long)c + (long long)(G / 2u);
+        const bool take = mode == 1 || (mode == 2 && (j & 1u) == 0u);
+        if (!(take && c != INT_MIN && isfinite(s) && o >= 0 && o < (long long)G)) break;
+        const uint32_t w = (uint32_t)o - w0;  // wraps when o < w0
+        s = w < kSpecWindow ? s_mem[(tid * (k - 1u) + j - 1u) * kSpecWindow + w]
+                            : __ldcg(&ms->table[tid][j][(uint32_t)o]);
+      }
+      s_res[tid] = s;
+      s_hit[tid] = (int)j;
+    }
+    __syncthreads();
+    const uint32_t z = (uint32_t)s_hit[0] < k ? 0u : 1u;
+    const uint32_t j = (uint32_t)s_hit[z];
+    if (j >= k) break;  // both walks are through (the same for every thread)
+    const uint32_t i0 = j * L;
+    const uint32_t nq = stage_terms(z ? uy : ux, sol, i0, min(L, nb - i0), seg);
+    __syncthreads();
+    if (tid == 0) {
+      s_res[z] = add_in_order(s_res[z], reinterpret_cast<const float4*>(seg), nq);
+      s_hit[z] = (int)j + 1;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const unsigned long long cnt = __ldcg(&ms->fluid);
+    const float n = cnt <= (1ull << 24) ? (float)cnt : 16777216.0f;
+    out[0] = n == 0.0f ? 0.0f : __fdiv_rn(s_res[0], n);
+    out[1] = n == 0.0f ? 0.0f : __fdiv_rn(s_res[1], n);
+    ms->counter = 0u;  // for the next launch
+  }
+}
+
+// The field analyses with the segmented mean: the first 1 + 2 (k - 1) kSpecParts
+// blocks the mean velocity's segments, the rest the vorticity when `vort` is set.
+__global__ void __launch_bounds__(kAnalysisThreads) lgx_field_mean_spec_kernel(
+    const float* __restrict__ ux, const float* __restrict__ uy, const float* __restrict__ sol,
+    uint32_t bw, uint32_t bh, float dx, float dy, float* __restrict__ vort,
+    float* __restrict__ mean, MeanScratch* ms, uint32_t L, uint32_t k, int mode) {
+  const uint32_t nmean = 1u + 2u * (k - 1u) * kSpecParts;
+  if (blockIdx.x < nmean) {
+    mean_spec_block(ux, uy, sol, bw * bh, L, k, blockIdx.x, ms, mean, mode);
+    return;
+  }
+  const uint32_t kk = (blockIdx.x - nmean) * kAnalysisThreads + threadIdx.x;
+  if (vort && kk < bw * bh) vort[kk] = vorticity_at(ux, uy, kk, bw, bh, dx, dy);
+}
+
+// LGX_MEAN_SPECULATE (tests): 0 sums every segment in order in the combining block,
+// 2 takes the guess tables of even segments only; 1 (unset) takes every table.
+int mean_spec_mode() {
+  static const int mode = [] {
+    const char* v = getenv("LGX_MEAN_SPECULATE");
+    return v && v[0] == '0' ? 0 : v && v[0] == '2' ? 2 : 1;
+  }();
+  return mode;
+}
+
+size_t mean_scratch_bytes() { return sizeof(MeanScratch); }
+
 cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
-                                  uint32_t by, float* vort, float* mean, cudaStream_t st) {
+                                  uint32_t by, float* vort, float* mean, void* mean_scratch,
+                                  cudaStream_t st) {
   const uint32_t nb = bw * bh;
-  const uint32_t blocks = (mean ? 1u : 0u) + (vort ? (nb + kAnalysisThreads - 1u) /
-                                                         kAnalysisThreads : 0u);
-  if (blocks == 0) return cudaSuccess;
+  const uint32_t vblocks = vort ? (nb + kAnalysisThreads - 1u) / kAnalysisThreads : 0u;
   const float dx = (float)bx;
   const float dy = __fmul_rn_host((float)by, 0.8660254f);
+  if (mean && mean_scratch && nb <= kSpecMaxBlocks) {
+    uint32_t L = (nb + kSpecMaxSegments - 1u) / kSpecMaxSegments;
+    L = (L + 31u) & ~31u;
+    if (L < kSpecMinSegment) L = kSpecMinSegment;
+    const uint32_t k = nb ? (nb + L - 1u) / L : 1u;
+    lgx_field_mean_spec_kernel<<<1u + 2u * (k - 1u) * kSpecParts + vblocks, kAnalysisThreads,
+                                 0, st>>>(
+        field, field + nb, field + 3 * nb, bw, bh, dx, dy, vort, mean,
+        (MeanScratch*)mean_scratch, L, k, mean_spec_mode());
+    return cudaGetLastError();
+  }
+  const uint32_t blocks = (mean ? 1u : 0u) + vblocks;
+  if (blocks == 0) return cudaSuccess;
   lgx_field_analyses_kernel<<<blocks, kAnalysisThreads, 0, st>>>(
       field, field + nb, field + 3 * nb, bw, bh, dx, dy, vort, mean);
   return cudaGetLastError();

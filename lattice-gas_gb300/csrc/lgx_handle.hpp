@@ -67,6 +67,7 @@ struct lgx_lattice {
   float* vort = nullptr;  // device address of vort_host: the field's vorticity (bw*bh),
                           // then its mean velocity (2)
   float* vort_host = nullptr;  // page-locked copy of the same, for the read-back
+  void* mean_scratch = nullptr;  // the mean velocity's segment tables (device)
 };
 
 // The equilibrium fill's scratch for this lattice, made at its first fill.

@@ -116,9 +116,13 @@ cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaSt
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
 // Field::vorticity and Field::mean_velocity of a field laid out ux | uy | rho |
 // sol (bw * bh each), in one launch: vort gets bw * bh floats and mean (mean ux,
-// mean uy); either may be null.
+// mean uy); either may be null.  mean_scratch: mean_scratch_bytes() of device
+// memory zeroed before its first use, kept for the field's later calls (null: the
+// mean velocity takes its single-chain kernel).
+size_t mean_scratch_bytes();
 cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
-                                  uint32_t by, float* vort, float* mean, cudaStream_t st);
+                                  uint32_t by, float* vort, float* mean, void* mean_scratch,
+                                  cudaStream_t st);
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
                          cudaStream_t st);
 // The WITH_WALLS moments of every cell (src/moments.rs:37-74, 126-138): out[0..2] =

@@ -101,6 +101,7 @@ void free_lattice(lgx_lattice* lat) {
   cudaFree(lat->prof);
   cudaFree(lat->fill_scratch);
   if (lat->vort_host) cudaFreeHost(lat->vort_host);  // lat->vort maps into it
+  cudaFree(lat->mean_scratch);
   cudaFree(lat->done);
   cudaFree(lat->error);
   for (auto& e : lat->ev)
@@ -697,6 +698,15 @@ static int field_scratch(lgx_lattice* lat, float** out) {
       LGX_CUDA(e);
     }
   }
+  if (!lat->mean_scratch) {  // the mean velocity's segment tables (and their counter at 0)
+    LGX_CUDA(cudaMalloc(&lat->mean_scratch, lgx::mean_scratch_bytes()));
+    const cudaError_t e = cudaMemset(lat->mean_scratch, 0, lgx::mean_scratch_bytes());
+    if (e != cudaSuccess) {
+      cudaFree(lat->mean_scratch);
+      lat->mean_scratch = nullptr;
+      LGX_CUDA(e);
+    }
+  }
   *out = lat->vort;
   return LGX_OK;
 }
@@ -710,7 +720,8 @@ static int field_analyses(lgx_lattice* lat, float* w, float* mx, float* my) {
   const size_t nb = (size_t)lat->bw * lat->bh;
   const bool mean = mx != nullptr;
   LGX_CUDA(lgx::launch_field_analyses(lat->field, lat->bw, lat->bh, lat->bx, lat->by,
-                                      w ? d : nullptr, mean ? d + nb : nullptr, lat->stream));
+                                      w ? d : nullptr, mean ? d + nb : nullptr,
+                                      lat->mean_scratch, lat->stream));
   lat->launches += 1;
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
   if (w) memcpy(w, lat->vort_host, nb * 4);
