@@ -133,8 +133,11 @@ __global__ void __launch_bounds__(64, 8) lgx_batch_lanes4_kernel(BatchStepArgs p
   batch_lane_words<RULE, 4, INFLOW>(p, d, (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 4u);
 }
 
+// Six blocks per SM, five with the inflow compiled in (at six it spilled 28 bytes:
+// one 2048 x 1280 lattice with an inflow, replayed from graphs, 4.95 -> 4.01 us per
+// step; without one, five blocks cost the transport sweep 1272 -> 1209 Gsite/s).
 template <int RULE, bool INFLOW>
-__global__ void __launch_bounds__(128, 6) lgx_batch_lanes_kernel(BatchStepArgs p) {
+__global__ void __launch_bounds__(128, INFLOW ? 5 : 6) lgx_batch_lanes_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];

@@ -40,9 +40,15 @@ namespace {
 // words per lane, lgx_step_lanes_kernel) come after them.
 constexpr uint32_t kTwoChunkMinWords = 152u * 6u * 256u;  // one wave of two-chunk blocks
 constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
-// Resident blocks per SM the register allocation must allow (64 registers).
+// Resident blocks per SM the register allocation must allow: six 128-thread
+// blocks of two chunks per warp (85 registers); four 256-thread blocks of one
+// chunk per warp (64 registers: at six, 40 registers, the update spilled 72 bytes
+// and a 2048 x 1280 step took 5.03 us against 3.57).
 #ifndef LGX_STEP_MINB
 #define LGX_STEP_MINB 6
+#endif
+#ifndef LGX_STEP_MINB1
+#define LGX_STEP_MINB1 4
 #endif
 
 #ifndef LGX_WAVE_SLEEP
@@ -57,7 +63,8 @@ constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
 // step N's last blocks leave idle.  Without a programmatic predecessor the
 // wait returns at once, so the kernel is also correct launched plainly.
 template <bool REST, int WORDS>
-__global__ void __launch_bounds__(256 / WORDS, LGX_STEP_MINB) lgx_step_kernel(const StepArgs p) {
+__global__ void __launch_bounds__(256 / WORDS, WORDS == 1 ? LGX_STEP_MINB1 : LGX_STEP_MINB)
+    lgx_step_kernel(const StepArgs p) {
   // a warp takes WORDS consecutive 32-word chunks; a block covers 256 words
   constexpr int kStepWords = WORDS;
   const uint32_t g0 = blockIdx.x * 256u + (threadIdx.x & ~31u) * kStepWords + (threadIdx.x & 31u);
@@ -90,9 +97,12 @@ __global__ void __launch_bounds__(256 / WORDS, LGX_STEP_MINB) lgx_step_kernel(co
 // fill the previous step's drain); half of them before it, 6.93 / 315;
 // three resident blocks of 155 registers, 7.35 / 339; five of 96, draws
 // after the wait, 9.11 / 290.1.  The hash outputs' shifts as multiplies on the
-// FMA pipe: 6.03 / 297.0.
+// FMA pipe: 6.03 / 297.0.  Two words per lane are allowed six blocks per SM (80
+// registers), five with the inflow compiled in: at six it spilled 24 bytes, and a
+// 2048 x 1280 step with an 8-column inflow took 4.55 us against 3.89.
 template <bool REST, int V, bool INFLOW>
-__global__ void __launch_bounds__(128, V == 4 ? 4 : 6) lgx_step_lanes_kernel(const StepArgs p) {
+__global__ void __launch_bounds__(128, V == 4 ? 4 : (INFLOW ? 5 : 6))
+    lgx_step_lanes_kernel(const StepArgs p) {
   constexpr int E = V;  // draws made before the wait
   const uint32_t warp = blockIdx.x * 4u + (threadIdx.x >> 5);
   uint32_t gq = warp * (32u * V) + (threadIdx.x & 31u) * V;
