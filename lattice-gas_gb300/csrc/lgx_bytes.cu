@@ -406,7 +406,8 @@ __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_co
 // mass, px2, py2 as 64-bit two's-complement sums.
 __global__ void __launch_bounds__(256) lgx_byte_moments_kernel(const uint8_t* __restrict__ cells,
                                                                size_t n,
-                                                               unsigned long long* out) {
+                                                               unsigned long long* out,
+                                                               unsigned long long* ticket) {
   constexpr unsigned long long kBit0 = 0x0101010101010101ull;
   long long mass = 0, px2 = 0, py2 = 0;
   const uint64_t* w = reinterpret_cast<const uint64_t*>(cells);
@@ -431,16 +432,23 @@ __global__ void __launch_bounds__(256) lgx_byte_moments_kernel(const uint8_t* __
     py2 += c[1] + c[2] - c[4] - c[5];
   }
   long long v[3] = {mass, px2, py2};
-  lgx::block_add<3>(v, out);
+  if (ticket)
+    lgx::block_total_to_host<3>(v, ticket, out);
+  else
+    lgx::block_add<3>(v, out);
 }
 
+// ticket null: out is device memory, zeroed first; else out is mapped host memory
+// the last block writes and ticket the counter buffer's word 4 (one operation).
 cudaError_t launch_byte_moments(const uint8_t* cells, size_t n, unsigned long long* out,
-                                cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
-  if (e != cudaSuccess) return e;
+                                cudaStream_t st, unsigned long long* ticket = nullptr) {
+  if (!ticket) {
+    cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+  }
   size_t blocks = (n / 8 + 255) / 256;
-  blocks = std::max<size_t>(1, std::min<size_t>(blocks, 152 * 2));
-  lgx_byte_moments_kernel<<<(unsigned)blocks, 256, 0, st>>>(cells, n, out);
+  blocks = std::max<size_t>(1, std::min<size_t>(blocks, lgx::kReduceMaxBlocks));
+  lgx_byte_moments_kernel<<<(unsigned)blocks, 256, 0, st>>>(cells, n, out, ticket);
   return cudaGetLastError();
 }
 
@@ -690,7 +698,9 @@ int lgx_byte_create(size_t w, size_t h, float density, float ux, float uy, size_
   if (e == cudaSuccess) e = cudaMalloc(&L->planes, total * 7 * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->solid, total * 4);
   if (e == cudaSuccess) e = cudaMalloc(&L->anysolid, ((total + 31) / 32) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&L->counter, 4 * 8);  // count, then the three moments
+  // count, the three moments, one-launch totals' slots (zeroed)
+  if (e == cudaSuccess) e = cudaMalloc(&L->counter, lgx::kCounterWords * 8);
+  if (e == cudaSuccess) e = cudaMemset(L->counter, 0, lgx::kCounterWords * 8);
   if (e == cudaSuccess) e = cudaMemset(L->cells[0], 0, cells);
   if (e == cudaSuccess) e = cudaMemcpy(L->table, table.data(), table.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = ensure_step_attributes(L->device);
@@ -892,11 +902,18 @@ int lgx_byte_total_particles(lgx_byte_lattice* L, uint64_t* out) {
     return LGX_ERR_ARG;
   }
   LGX_CUDA(cudaSetDevice(L->device));
-  LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1, L->stream));
   unsigned long long local = 0;
   unsigned long long* v = lgx::host_result_words();
-  if (!v) v = &local;
-  LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 8, cudaMemcpyDeviceToHost, L->stream));
+  unsigned long long* dv = lgx::host_result_device();
+  if (v && dv) {  // one launch that writes the moments into the mapped result words
+    LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, dv, L->stream,
+                                 L->counter + 4));
+  } else {
+    if (!v) v = &local;
+    LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1,
+                                 L->stream));
+    LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 8, cudaMemcpyDeviceToHost, L->stream));
+  }
   LGX_CUDA(cudaStreamSynchronize(L->stream));
   *out = *v;
   return LGX_OK;
@@ -910,11 +927,19 @@ int lgx_byte_mean_velocity(lgx_byte_lattice* L, float* ux, float* uy) {
     return LGX_ERR_ARG;
   }
   LGX_CUDA(cudaSetDevice(L->device));
-  LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1, L->stream));
   unsigned long long local[3];
   unsigned long long* v = lgx::host_result_words();
-  if (!v) v = local;
-  LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost, L->stream));
+  unsigned long long* dv = lgx::host_result_device();
+  if (v && dv) {
+    LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, dv, L->stream,
+                                 L->counter + 4));
+  } else {
+    if (!v) v = local;
+    LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1,
+                                 L->stream));
+    LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost,
+                             L->stream));
+  }
   LGX_CUDA(cudaStreamSynchronize(L->stream));
   lgx::moments_velocity((int64_t)v[0], (int64_t)v[1], (int64_t)v[2], ux, uy);
   return LGX_OK;

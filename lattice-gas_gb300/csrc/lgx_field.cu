@@ -27,8 +27,11 @@ __global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p) {
 
 // Particles on the lattice, obstacle sites included, tail-masked
 // (lgca_count, src/gpu.rs:381-395), into a 64-bit counter.
+// out: device counter (zeroed before the launch), or, with ticket set, mapped host
+// memory that the last block writes (block_total_to_host).
 __global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restrict__ a, Dims dm,
-                                                        unsigned long long* out) {
+                                                        unsigned long long* out,
+                                                        unsigned long long* ticket) {
   unsigned long long acc = 0;
   const size_t S = dm.total;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < dm.total;
@@ -41,13 +44,17 @@ __global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restri
     acc += c;
   }
   long long v[1] = {(long long)acc};
-  block_add<1>(v, out);
+  if (ticket)
+    block_total_to_host<1>(v, ticket, out);
+  else
+    block_add<1>(v, out);
 }
 
 // Lattice mass and momentum, obstacle sites included: per word the popcounts
 // of the seven planes weighted by CX2 and CY2 (src/hex.rs), summed exactly.
 __global__ void __launch_bounds__(256) lgx_moments_kernel(const uint32_t* __restrict__ a, Dims dm,
-                                                          unsigned long long* out) {
+                                                          unsigned long long* out,
+                                                          unsigned long long* ticket) {
   long long mass = 0, px2 = 0, py2 = 0;
   const size_t S = dm.total;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < dm.total;
@@ -62,7 +69,10 @@ __global__ void __launch_bounds__(256) lgx_moments_kernel(const uint32_t* __rest
     py2 += c[1] + c[2] - c[4] - c[5];
   }
   long long v[3] = {mass, px2, py2};
-  block_add<3>(v, out);
+  if (ticket)
+    block_total_to_host<3>(v, ticket, out);
+  else
+    block_add<3>(v, out);
 }
 
 // Bytes -> planes: one warp per lattice word; lane k reads column 32 j + k and
@@ -576,12 +586,14 @@ cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, 
 }
 
 cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long* out,
-                           cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
-  if (e != cudaSuccess) return e;
+                           cudaStream_t st, unsigned long long* ticket) {
+  if (!ticket) {
+    cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+  }
   uint32_t blocks = (dm.total + 255) / 256;
-  if (blocks > 304) blocks = 304;  // two blocks per SM, grid-stride beyond
-  lgx_moments_kernel<<<blocks, 256, 0, st>>>(a, dm, out);
+  if (blocks > kReduceMaxBlocks) blocks = kReduceMaxBlocks;  // two per SM, grid-stride beyond
+  lgx_moments_kernel<<<blocks, 256, 0, st>>>(a, dm, out, ticket);
   return cudaGetLastError();
 }
 
@@ -593,12 +605,14 @@ cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st) {
 }
 
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
-                         cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
-  if (e != cudaSuccess) return e;
+                         cudaStream_t st, unsigned long long* ticket) {
+  if (!ticket) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+  }
   uint32_t blocks = (dm.total + 255) / 256;
-  if (blocks > 304) blocks = 304;  // two blocks per SM, grid-stride beyond
-  lgx_count_kernel<<<blocks, 256, 0, st>>>(a, dm, out);
+  if (blocks > kReduceMaxBlocks) blocks = kReduceMaxBlocks;  // two per SM, grid-stride beyond
+  lgx_count_kernel<<<blocks, 256, 0, st>>>(a, dm, out, ticket);
   return cudaGetLastError();
 }
 

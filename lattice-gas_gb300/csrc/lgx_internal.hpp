@@ -123,19 +123,30 @@ size_t mean_scratch_bytes();
 cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
                                   uint32_t by, float* vort, float* mean, void* mean_scratch,
                                   cudaStream_t st);
+// A lattice's counter buffer: the particle count (word 0), the three moments
+// (1..3), and the ticket (4) and per-block slots of one-launch totals for grids
+// of up to kReduceMaxBlocks blocks; zeroed when made.
+constexpr unsigned kReduceMaxBlocks = 304;
+constexpr size_t kCounterWords = 5 + (size_t)kReduceMaxBlocks * 3;
+// Particles on the lattice into out[0]; the WITH_WALLS moments of every cell
+// (src/moments.rs:37-74, 126-138) into out[0..2] = mass, px2, py2 as 64-bit
+// two's-complement sums.  ticket null: out is device memory, zeroed first (two
+// operations); else ticket is a lattice counter buffer's word 4 (zero between
+// launches) and out mapped host memory the kernel writes (one operation).
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
-                         cudaStream_t st);
-// The WITH_WALLS moments of every cell (src/moments.rs:37-74, 126-138): out[0..2] =
-// mass, px2, py2 as 64-bit two's-complement sums.
+                         cudaStream_t st, unsigned long long* ticket = nullptr);
 cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long* out,
-                           cudaStream_t st);
+                           cudaStream_t st, unsigned long long* ticket = nullptr);
 // Moments::velocity (src/moments.rs:91-97): momentum per particle in f32, (0, 0)
 // for no particles.
 void moments_velocity(int64_t mass, int64_t px2, int64_t py2, float* ux, float* uy);
 // Eight page-locked 64-bit words for this host thread, for results of a few
 // bytes read back by a call that synchronises before it returns (a copy to
-// pageable memory goes through a staging copy); null if none could be had.
+// pageable memory goes through a staging copy); null if none could be had.  The
+// words are mapped into the devices' address space: host_result_device gives
+// their device address (null if it cannot), for kernels that write them.
 unsigned long long* host_result_words();
+unsigned long long* host_result_device();
 // Byte cells (w*h, row-major) <-> planes + solid + anysolid.
 cudaError_t launch_pack(const uint8_t* cells, const Dims& dm, uint32_t* planes, uint32_t* solid,
                         uint32_t* anysolid, cudaStream_t st);

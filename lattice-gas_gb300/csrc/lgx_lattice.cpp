@@ -440,8 +440,9 @@ int lgx_create(size_t w, size_t h, int rest, uint64_t seed, lgx_lattice** out) {
   if (e == cudaSuccess) e = cudaMalloc(&lat->solid, total * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&lat->anysolid, ((total + 31) / 32) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&lat->cells, w * h);
-  // the particle count, then the three WITH_WALLS moments
-  if (e == cudaSuccess) e = cudaMalloc(&lat->counter, 4 * sizeof(unsigned long long));
+  // the particle count, the three WITH_WALLS moments, one-launch totals' slots
+  if (e == cudaSuccess) e = cudaMalloc(&lat->counter, lgx::kCounterWords * 8);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lat->counter, 0, lgx::kCounterWords * 8, lat->stream);
   for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&lat->ev[i]);
   if (e == cudaSuccess) e = cudaMemsetAsync(lat->planes[0], 0, total * 7 * 4, lat->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(lat->planes[1], 0, total * 7 * 4, lat->stream);
@@ -856,6 +857,15 @@ int lgx_total_particles(lgx_lattice* lat, uint64_t* out) {
   }
   unsigned long long local = 0;
   unsigned long long* v = lgx::host_result_words();
+  unsigned long long* dv = lgx::host_result_device();
+  if (v && dv) {  // one launch that writes the total into the mapped result word
+    LGX_CUDA(lgx::launch_count(lat->planes[lat->cur], lat->dm, dv, lat->stream,
+                               lat->counter + 4));
+    lat->launches += 1;
+    LGX_CUDA(cudaStreamSynchronize(lat->stream));
+    *out = v[0];
+    return LGX_OK;
+  }
   if (!v) v = &local;
   LGX_CUDA(lgx::launch_count(lat->planes[lat->cur], lat->dm, lat->counter, lat->stream));
   lat->launches += 1;
@@ -874,11 +884,17 @@ int lgx_mean_velocity(lgx_lattice* lat, float* ux, float* uy) {
   }
   unsigned long long local[3];
   unsigned long long* v = lgx::host_result_words();
-  if (!v) v = local;
-  LGX_CUDA(lgx::launch_moments(lat->planes[lat->cur], lat->dm, lat->counter + 1, lat->stream));
+  unsigned long long* dv = lgx::host_result_device();
+  if (v && dv) {  // one launch that writes the moments into the mapped result words
+    LGX_CUDA(lgx::launch_moments(lat->planes[lat->cur], lat->dm, dv, lat->stream,
+                                 lat->counter + 4));
+  } else {
+    if (!v) v = local;
+    LGX_CUDA(lgx::launch_moments(lat->planes[lat->cur], lat->dm, lat->counter + 1, lat->stream));
+    LGX_CUDA(cudaMemcpyAsync(v, lat->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost,
+                             lat->stream));
+  }
   lat->launches += 1;
-  LGX_CUDA(cudaMemcpyAsync(v, lat->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost,
-                           lat->stream));
   LGX_CUDA(cudaStreamSynchronize(lat->stream));
   lgx::moments_velocity((int64_t)v[0], (int64_t)v[1], (int64_t)v[2], ux, uy);
   return LGX_OK;

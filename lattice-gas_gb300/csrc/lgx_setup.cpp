@@ -40,12 +40,28 @@ unsigned long long* host_result_words() {
   if (!tried) {
     tried = true;
     void* p = nullptr;
-    if (cudaHostAlloc(&p, 8 * sizeof(unsigned long long), cudaHostAllocPortable) == cudaSuccess)
+    if (cudaHostAlloc(&p, 8 * sizeof(unsigned long long),
+                      cudaHostAllocPortable | cudaHostAllocMapped) == cudaSuccess)
       words = (unsigned long long*)p;
     else
       cudaGetLastError();
   }
   return words;
+}
+
+unsigned long long* host_result_device() {
+  thread_local unsigned long long* dev = nullptr;
+  thread_local bool tried = false;
+  if (!tried) {
+    tried = true;
+    unsigned long long* h = host_result_words();
+    void* d = nullptr;
+    if (h && cudaHostGetDevicePointer(&d, h, 0) == cudaSuccess)
+      dev = (unsigned long long*)d;
+    else
+      cudaGetLastError();
+  }
+  return dev;
 }
 
 namespace {
