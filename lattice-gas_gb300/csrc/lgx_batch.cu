@@ -133,11 +133,14 @@ __global__ void __launch_bounds__(64, 8) lgx_batch_lanes4_kernel(BatchStepArgs p
   batch_lane_words<RULE, 4, INFLOW>(p, d, (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 4u);
 }
 
-// Six blocks per SM, five with the inflow compiled in (at six it spilled 28 bytes:
-// one 2048 x 1280 lattice with an inflow, replayed from graphs, 4.95 -> 4.01 us per
-// step; without one, five blocks cost the transport sweep 1272 -> 1209 Gsite/s).
-template <int RULE, bool INFLOW>
-__global__ void __launch_bounds__(128, INFLOW ? 5 : 6) lgx_batch_lanes_kernel(BatchStepArgs p) {
+// Six blocks per SM; with the inflow compiled in the update then spills 28 bytes,
+// which costs latency-bound launches most, so launches of less than one wave of
+// such blocks take a five-block build that does not spill (one 2048 x 1280 lattice
+// with an inflow, replayed from graphs, 4.95 -> 4.01 us per step), and larger ones
+// keep six (five cost the request stream's larger chains about 5%, and without the
+// inflow the transport sweep 1272 -> 1209 Gsite/s).
+template <int RULE, bool INFLOW, int MINB = 6>
+__global__ void __launch_bounds__(128, MINB) lgx_batch_lanes_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
@@ -251,6 +254,12 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule
     return cudaLaunchKernelEx(&cfg, lgx_batch_lanes4_kernel<0, false>, a);
   }
   if (words == kBatchLanes2) {
+    if (inflow && nblocks < 152u * 6u) {
+      if (rule == kRuleMixed)
+        return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, true, 5>, a);
+      if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, true, 5>, a);
+      return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0, true, 5>, a);
+    }
     if (inflow) {
       if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, true>, a);
       if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, true>, a);
