@@ -407,7 +407,9 @@ __global__ void __launch_bounds__(kThreads) lgx_byte_step_kernel(const __grid_co
 __global__ void __launch_bounds__(256) lgx_byte_moments_kernel(const uint8_t* __restrict__ cells,
                                                                size_t n,
                                                                unsigned long long* out,
-                                                               unsigned long long* ticket) {
+                                                               unsigned long long* ticket,
+                                                               unsigned long long* flag,
+                                                               unsigned long long seq) {
   constexpr unsigned long long kBit0 = 0x0101010101010101ull;
   long long mass = 0, px2 = 0, py2 = 0;
   const uint64_t* w = reinterpret_cast<const uint64_t*>(cells);
@@ -433,7 +435,7 @@ __global__ void __launch_bounds__(256) lgx_byte_moments_kernel(const uint8_t* __
   }
   long long v[3] = {mass, px2, py2};
   if (ticket)
-    lgx::block_total_to_host<3>(v, ticket, out);
+    lgx::block_total_to_host<3>(v, ticket, out, flag, seq);
   else
     lgx::block_add<3>(v, out);
 }
@@ -441,14 +443,15 @@ __global__ void __launch_bounds__(256) lgx_byte_moments_kernel(const uint8_t* __
 // ticket null: out is device memory, zeroed first; else out is mapped host memory
 // the last block writes and ticket the counter buffer's word 4 (one operation).
 cudaError_t launch_byte_moments(const uint8_t* cells, size_t n, unsigned long long* out,
-                                cudaStream_t st, unsigned long long* ticket = nullptr) {
+                                cudaStream_t st, unsigned long long* ticket = nullptr,
+                                unsigned long long* flag = nullptr, unsigned long long seq = 0) {
   if (!ticket) {
     cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
   }
   size_t blocks = (n / 8 + 255) / 256;
   blocks = std::max<size_t>(1, std::min<size_t>(blocks, lgx::kReduceMaxBlocks));
-  lgx_byte_moments_kernel<<<(unsigned)blocks, 256, 0, st>>>(cells, n, out, ticket);
+  lgx_byte_moments_kernel<<<(unsigned)blocks, 256, 0, st>>>(cells, n, out, ticket, flag, seq);
   return cudaGetLastError();
 }
 
@@ -906,15 +909,17 @@ int lgx_byte_total_particles(lgx_byte_lattice* L, uint64_t* out) {
   unsigned long long* v = lgx::host_result_words();
   unsigned long long* dv = lgx::host_result_device();
   if (v && dv) {  // one launch that writes the moments into the mapped result words
+    const unsigned long long seq = lgx::host_result_seq();
     LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, dv, L->stream,
-                                 L->counter + 4));
+                                 L->counter + 4, dv + 7, seq));
+    LGX_CUDA(lgx::host_result_wait(seq, L->stream));
   } else {
     if (!v) v = &local;
     LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1,
                                  L->stream));
     LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 8, cudaMemcpyDeviceToHost, L->stream));
+    LGX_CUDA(cudaStreamSynchronize(L->stream));
   }
-  LGX_CUDA(cudaStreamSynchronize(L->stream));
   *out = *v;
   return LGX_OK;
 }
@@ -931,16 +936,18 @@ int lgx_byte_mean_velocity(lgx_byte_lattice* L, float* ux, float* uy) {
   unsigned long long* v = lgx::host_result_words();
   unsigned long long* dv = lgx::host_result_device();
   if (v && dv) {
+    const unsigned long long seq = lgx::host_result_seq();
     LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, dv, L->stream,
-                                 L->counter + 4));
+                                 L->counter + 4, dv + 7, seq));
+    LGX_CUDA(lgx::host_result_wait(seq, L->stream));
   } else {
     if (!v) v = local;
     LGX_CUDA(launch_byte_moments(L->cells[L->cur], (size_t)L->w * L->h, L->counter + 1,
                                  L->stream));
     LGX_CUDA(cudaMemcpyAsync(v, L->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost,
                              L->stream));
+    LGX_CUDA(cudaStreamSynchronize(L->stream));
   }
-  LGX_CUDA(cudaStreamSynchronize(L->stream));
   lgx::moments_velocity((int64_t)v[0], (int64_t)v[1], (int64_t)v[2], ux, uy);
   return LGX_OK;
 }

@@ -31,7 +31,9 @@ __global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p) {
 // memory that the last block writes (block_total_to_host).
 __global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restrict__ a, Dims dm,
                                                         unsigned long long* out,
-                                                        unsigned long long* ticket) {
+                                                        unsigned long long* ticket,
+                                                        unsigned long long* flag,
+                                                        unsigned long long seq) {
   unsigned long long acc = 0;
   const size_t S = dm.total;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < dm.total;
@@ -45,7 +47,7 @@ __global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restri
   }
   long long v[1] = {(long long)acc};
   if (ticket)
-    block_total_to_host<1>(v, ticket, out);
+    block_total_to_host<1>(v, ticket, out, flag, seq);
   else
     block_add<1>(v, out);
 }
@@ -54,7 +56,9 @@ __global__ void __launch_bounds__(256) lgx_count_kernel(const uint32_t* __restri
 // of the seven planes weighted by CX2 and CY2 (src/hex.rs), summed exactly.
 __global__ void __launch_bounds__(256) lgx_moments_kernel(const uint32_t* __restrict__ a, Dims dm,
                                                           unsigned long long* out,
-                                                          unsigned long long* ticket) {
+                                                          unsigned long long* ticket,
+                                                          unsigned long long* flag,
+                                                          unsigned long long seq) {
   long long mass = 0, px2 = 0, py2 = 0;
   const size_t S = dm.total;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < dm.total;
@@ -70,7 +74,7 @@ __global__ void __launch_bounds__(256) lgx_moments_kernel(const uint32_t* __rest
   }
   long long v[3] = {mass, px2, py2};
   if (ticket)
-    block_total_to_host<3>(v, ticket, out);
+    block_total_to_host<3>(v, ticket, out, flag, seq);
   else
     block_add<3>(v, out);
 }
@@ -589,14 +593,15 @@ cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, 
 }
 
 cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long* out,
-                           cudaStream_t st, unsigned long long* ticket) {
+                           cudaStream_t st, unsigned long long* ticket, unsigned long long* flag,
+                           unsigned long long seq) {
   if (!ticket) {
     cudaError_t e = cudaMemsetAsync(out, 0, 3 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
   }
   uint32_t blocks = (dm.total + 255) / 256;
   if (blocks > kReduceMaxBlocks) blocks = kReduceMaxBlocks;  // two per SM, grid-stride beyond
-  lgx_moments_kernel<<<blocks, 256, 0, st>>>(a, dm, out, ticket);
+  lgx_moments_kernel<<<blocks, 256, 0, st>>>(a, dm, out, ticket, flag, seq);
   return cudaGetLastError();
 }
 
@@ -608,14 +613,15 @@ cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st) {
 }
 
 cudaError_t launch_count(const uint32_t* a, const Dims& dm, unsigned long long* out,
-                         cudaStream_t st, unsigned long long* ticket) {
+                         cudaStream_t st, unsigned long long* ticket, unsigned long long* flag,
+                         unsigned long long seq) {
   if (!ticket) {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
   }
   uint32_t blocks = (dm.total + 255) / 256;
   if (blocks > kReduceMaxBlocks) blocks = kReduceMaxBlocks;  // two per SM, grid-stride beyond
-  lgx_count_kernel<<<blocks, 256, 0, st>>>(a, dm, out, ticket);
+  lgx_count_kernel<<<blocks, 256, 0, st>>>(a, dm, out, ticket, flag, seq);
   return cudaGetLastError();
 }
 

@@ -859,10 +859,11 @@ int lgx_total_particles(lgx_lattice* lat, uint64_t* out) {
   unsigned long long* v = lgx::host_result_words();
   unsigned long long* dv = lgx::host_result_device();
   if (v && dv) {  // one launch that writes the total into the mapped result word
+    const unsigned long long seq = lgx::host_result_seq();
     LGX_CUDA(lgx::launch_count(lat->planes[lat->cur], lat->dm, dv, lat->stream,
-                               lat->counter + 4));
+                               lat->counter + 4, dv + 7, seq));
     lat->launches += 1;
-    LGX_CUDA(cudaStreamSynchronize(lat->stream));
+    LGX_CUDA(lgx::host_result_wait(seq, lat->stream));
     *out = v[0];
     return LGX_OK;
   }
@@ -886,16 +887,18 @@ int lgx_mean_velocity(lgx_lattice* lat, float* ux, float* uy) {
   unsigned long long* v = lgx::host_result_words();
   unsigned long long* dv = lgx::host_result_device();
   if (v && dv) {  // one launch that writes the moments into the mapped result words
+    const unsigned long long seq = lgx::host_result_seq();
     LGX_CUDA(lgx::launch_moments(lat->planes[lat->cur], lat->dm, dv, lat->stream,
-                                 lat->counter + 4));
+                                 lat->counter + 4, dv + 7, seq));
+    LGX_CUDA(lgx::host_result_wait(seq, lat->stream));
   } else {
     if (!v) v = local;
     LGX_CUDA(lgx::launch_moments(lat->planes[lat->cur], lat->dm, lat->counter + 1, lat->stream));
     LGX_CUDA(cudaMemcpyAsync(v, lat->counter + 1, 3 * sizeof(*v), cudaMemcpyDeviceToHost,
                              lat->stream));
+    LGX_CUDA(cudaStreamSynchronize(lat->stream));
   }
   lat->launches += 1;
-  LGX_CUDA(cudaStreamSynchronize(lat->stream));
   lgx::moments_velocity((int64_t)v[0], (int64_t)v[1], (int64_t)v[2], ux, uy);
   return LGX_OK;
 }

@@ -41,10 +41,14 @@ __device__ __forceinline__ void block_add(long long (&v)[N], unsigned long long*
 // to zero) adds the slots and writes the totals to `out`, page-locked host memory
 // mapped into the device's address space.  No zeroing before the launch and no
 // copy after it: one operation on the stream instead of three.  Integer sums, so
-// the order of the blocks does not matter.  Every thread of the block must call it.
+// the order of the blocks does not matter.  With `flag` set, the totals are followed
+// (after a system-scope fence) by `seq` in *flag, which the host can wait for
+// instead of synchronising the stream.  Every thread of the block must call it.
 template <int N>
 __device__ __forceinline__ void block_total_to_host(long long (&v)[N], unsigned long long* ticket,
-                                                    unsigned long long* out) {
+                                                    unsigned long long* out,
+                                                    unsigned long long* flag = nullptr,
+                                                    unsigned long long seq = 0) {
   __shared__ long long part[32][N];
   __shared__ bool last;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -82,7 +86,13 @@ __device__ __forceinline__ void block_total_to_host(long long (&v)[N], unsigned 
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) out[k] = s;
   }
-  if (lane == 0) *ticket = 0ull;
+  if (lane == 0) {
+    *ticket = 0ull;
+    if (flag) {
+      __threadfence_system();
+      *reinterpret_cast<volatile unsigned long long*>(flag) = seq;
+    }
+  }
 }
 
 }  // namespace lgx

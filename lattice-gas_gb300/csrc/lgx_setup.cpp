@@ -9,6 +9,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
+#include <chrono>
+
 #include <cuda_runtime.h>
 
 #include "../../include/lgx.h"
@@ -47,6 +50,26 @@ unsigned long long* host_result_words() {
       cudaGetLastError();
   }
   return words;
+}
+
+unsigned long long host_result_seq() {
+  thread_local unsigned long long seq = 0;
+  return ++seq;
+}
+
+cudaError_t host_result_wait(unsigned long long seq, cudaStream_t st) {
+  volatile unsigned long long* flag = host_result_words() + 7;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (unsigned n = 0;; ++n) {
+    if (*flag == seq) {
+      std::atomic_thread_fence(std::memory_order_acquire);  // the results were written first
+      return cudaSuccess;
+    }
+    if ((n & 1023u) == 1023u &&
+        std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(20))
+      break;
+  }
+  return cudaStreamSynchronize(st);
 }
 
 unsigned long long* host_result_device() {
