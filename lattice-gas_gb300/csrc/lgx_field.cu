@@ -310,20 +310,36 @@ __device__ __forceinline__ void mean_velocity_block(const float* __restrict__ ux
 // The field analyses of one field in one launch: block 0 forms the mean velocity
 // when `mean` is set, the other blocks the vorticity (one thread per field block)
 // when `vort` is set.
+// The end of every block of an analyses launch whose results the host waits for
+// on a flag: each thread's results are made visible to the host, and the last
+// block to finish (a counter it sets back to zero) writes seq to *flag.  Every
+// thread of the block must call it.
+__device__ __forceinline__ void analyses_done(unsigned int* done, unsigned long long* flag,
+                                              unsigned long long seq) {
+  if (!flag) return;
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(done, 1u) == gridDim.x - 1u) {
+    *done = 0u;
+    __threadfence_system();
+    *reinterpret_cast<volatile unsigned long long*>(flag) = seq;
+  }
+}
+
 __global__ void __launch_bounds__(kAnalysisThreads) lgx_field_analyses_kernel(
     const float* __restrict__ ux, const float* __restrict__ uy, const float* __restrict__ sol,
     uint32_t bw, uint32_t bh, float dx, float dy, float* __restrict__ vort,
-    float* __restrict__ mean) {
+    float* __restrict__ mean, unsigned int* done, unsigned long long* flag,
+    unsigned long long seq) {
   uint32_t b = blockIdx.x;
-  if (mean) {
-    if (b == 0) {
-      mean_velocity_block(ux, uy, sol, bw * bh, mean);
-      return;
-    }
-    b -= 1u;
+  if (mean && b == 0) {
+    mean_velocity_block(ux, uy, sol, bw * bh, mean);
+  } else {
+    if (mean) b -= 1u;
+    const uint32_t k = b * kAnalysisThreads + threadIdx.x;
+    if (vort && k < bw * bh) vort[k] = vorticity_at(ux, uy, k, bw, bh, dx, dy);
   }
-  const uint32_t k = b * kAnalysisThreads + threadIdx.x;
-  if (vort && k < bw * bh) vort[k] = vorticity_at(ux, uy, k, bw, bh, dx, dy);
+  analyses_done(done, flag, seq);
 }
 
 // ---- the mean velocity's sums in segments, speculatively ----
@@ -357,7 +373,7 @@ constexpr uint32_t kSpecMaxBlocks = kSpecMaxSegments * kSpecMaxSegment;  // 65,5
 // (the block counter returns to zero at the end of every launch).
 struct MeanScratch {
   unsigned int counter;
-  unsigned int pad;
+  unsigned int done;  // blocks of the launch finished (analyses_done)
   unsigned long long fluid;
   float first[2];
   float pad2[2];
@@ -545,14 +561,16 @@ __device__ __forceinline__ void mean_spec_block(const float* __restrict__ ux,
 __global__ void __launch_bounds__(kAnalysisThreads) lgx_field_mean_spec_kernel(
     const float* __restrict__ ux, const float* __restrict__ uy, const float* __restrict__ sol,
     uint32_t bw, uint32_t bh, float dx, float dy, float* __restrict__ vort,
-    float* __restrict__ mean, MeanScratch* ms, uint32_t L, uint32_t k, int mode) {
+    float* __restrict__ mean, MeanScratch* ms, uint32_t L, uint32_t k, int mode,
+    unsigned long long* flag, unsigned long long seq) {
   const uint32_t nmean = 1u + 2u * (k - 1u) * kSpecParts;
   if (blockIdx.x < nmean) {
     mean_spec_block(ux, uy, sol, bw * bh, L, k, blockIdx.x, ms, mean, mode);
-    return;
+  } else {
+    const uint32_t kk = (blockIdx.x - nmean) * kAnalysisThreads + threadIdx.x;
+    if (vort && kk < bw * bh) vort[kk] = vorticity_at(ux, uy, kk, bw, bh, dx, dy);
   }
-  const uint32_t kk = (blockIdx.x - nmean) * kAnalysisThreads + threadIdx.x;
-  if (vort && kk < bw * bh) vort[kk] = vorticity_at(ux, uy, kk, bw, bh, dx, dy);
+  analyses_done(&ms->done, flag, seq);
 }
 
 // LGX_MEAN_SPECULATE (tests): 0 sums every segment in order in the combining block,
@@ -569,7 +587,9 @@ size_t mean_scratch_bytes() { return sizeof(MeanScratch); }
 
 cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
                                   uint32_t by, float* vort, float* mean, void* mean_scratch,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, unsigned long long* flag,
+                                  unsigned long long seq) {
+  if (!mean_scratch) flag = nullptr;  // the done counter lives there
   const uint32_t nb = bw * bh;
   const uint32_t vblocks = vort ? (nb + kAnalysisThreads - 1u) / kAnalysisThreads : 0u;
   const float dx = (float)bx;
@@ -582,13 +602,14 @@ cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, 
     lgx_field_mean_spec_kernel<<<1u + 2u * (k - 1u) * kSpecParts + vblocks, kAnalysisThreads,
                                  0, st>>>(
         field, field + nb, field + 3 * nb, bw, bh, dx, dy, vort, mean,
-        (MeanScratch*)mean_scratch, L, k, mean_spec_mode());
+        (MeanScratch*)mean_scratch, L, k, mean_spec_mode(), flag, seq);
     return cudaGetLastError();
   }
   const uint32_t blocks = (mean ? 1u : 0u) + vblocks;
   if (blocks == 0) return cudaSuccess;
+  unsigned int* done = mean_scratch ? &((MeanScratch*)mean_scratch)->done : nullptr;
   lgx_field_analyses_kernel<<<blocks, kAnalysisThreads, 0, st>>>(
-      field, field + nb, field + 3 * nb, bw, bh, dx, dy, vort, mean);
+      field, field + nb, field + 3 * nb, bw, bh, dx, dy, vort, mean, done, flag, seq);
   return cudaGetLastError();
 }
 

@@ -120,9 +120,12 @@ cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
 // memory zeroed before its first use, kept for the field's later calls (null: the
 // mean velocity takes its single-chain kernel).
 size_t mean_scratch_bytes();
+// With flag set (and mean_scratch, which holds the launch's done counter), the
+// last block to finish writes seq to *flag after every result (host_result_wait).
 cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, uint32_t bx,
                                   uint32_t by, float* vort, float* mean, void* mean_scratch,
-                                  cudaStream_t st);
+                                  cudaStream_t st, unsigned long long* flag = nullptr,
+                                  unsigned long long seq = 0);
 // A lattice's counter buffer: the particle count (word 0), the three moments
 // (1..3), and the ticket (4) and per-block slots of one-launch totals for grids
 // of up to kReduceMaxBlocks blocks; zeroed when made.

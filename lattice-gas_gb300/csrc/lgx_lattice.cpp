@@ -720,11 +720,17 @@ static int field_analyses(lgx_lattice* lat, float* w, float* mx, float* my) {
   if (rc) return rc;
   const size_t nb = (size_t)lat->bw * lat->bh;
   const bool mean = mx != nullptr;
+  unsigned long long* flag = lgx::host_result_device();
+  const unsigned long long seq = flag ? lgx::host_result_seq() : 0;
   LGX_CUDA(lgx::launch_field_analyses(lat->field, lat->bw, lat->bh, lat->bx, lat->by,
                                       w ? d : nullptr, mean ? d + nb : nullptr,
-                                      lat->mean_scratch, lat->stream));
+                                      lat->mean_scratch, lat->stream, flag ? flag + 7 : nullptr,
+                                      seq));
   lat->launches += 1;
-  LGX_CUDA(cudaStreamSynchronize(lat->stream));
+  if (flag)
+    LGX_CUDA(lgx::host_result_wait(seq, lat->stream));
+  else
+    LGX_CUDA(cudaStreamSynchronize(lat->stream));
   if (w) memcpy(w, lat->vort_host, nb * 4);
   if (mean) {
     *mx = lat->vort_host[nb];
