@@ -19,10 +19,20 @@ static inline float __fmul_rn_host(float a, float b) { return a * b; }
 
 namespace {
 
-__global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p) {
+__global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p, unsigned int* done,
+                                                         unsigned long long* flag,
+                                                         unsigned long long seq) {
   const uint32_t blk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (blk >= p.bw * p.bh) return;  // whole warp leaves together
-  sample_block(p, blk);
+  if (blk < p.bw * p.bh) sample_block(p, blk);  // whole warps
+  if (!flag) return;
+  // a call that waits for the field: the last block to finish says so
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(done, 1u) == gridDim.x - 1u) {
+    *done = 0u;
+    __threadfence_system();
+    *reinterpret_cast<volatile unsigned long long*>(flag) = seq;
+  }
 }
 
 // Particles on the lattice, obstacle sites included, tail-masked
@@ -626,10 +636,11 @@ cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long
   return cudaGetLastError();
 }
 
-cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st) {
+cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st, unsigned int* done,
+                          unsigned long long* flag, unsigned long long seq) {
   const uint32_t nb = s.bw * s.bh;
   if (nb == 0) return cudaSuccess;
-  lgx_sample_kernel<<<(nb + 7) / 8, 256, 0, st>>>(s);
+  lgx_sample_kernel<<<(nb + 7) / 8, 256, 0, st>>>(s, done, flag, seq);
   return cudaGetLastError();
 }
 

@@ -113,7 +113,10 @@ cudaError_t launch_wave(const WaveArgs& w, bool rest, uint32_t grid, cudaStream_
 bool temporal_supported(const Dims& dm, uint32_t k);
 void temporal_tiling(const Dims& dm, uint32_t k, TemporalArgs* t);  // k steps per pass
 cudaError_t launch_temporal(const TemporalArgs& t, bool rest, uint32_t k, cudaStream_t st);
-cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st);
+// flag set: the last block to finish (done: a zeroed counter it sets back) writes
+// seq to *flag, mapped host memory, after the field (host_result_wait).
+cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st, unsigned int* done = nullptr,
+                          unsigned long long* flag = nullptr, unsigned long long seq = 0);
 // Field::vorticity and Field::mean_velocity of a field laid out ux | uy | rho |
 // sol (bw * bh each), in one launch: vort gets bw * bh floats and mean (mean ux,
 // mean uy); either may be null.  mean_scratch: mean_scratch_bytes() of device
@@ -127,10 +130,11 @@ cudaError_t launch_field_analyses(const float* field, uint32_t bw, uint32_t bh, 
                                   cudaStream_t st, unsigned long long* flag = nullptr,
                                   unsigned long long seq = 0);
 // A lattice's counter buffer: the particle count (word 0), the three moments
-// (1..3), and the ticket (4) and per-block slots of one-launch totals for grids
-// of up to kReduceMaxBlocks blocks; zeroed when made.
+// (1..3), the ticket of one-launch totals (4), the done counter of a waited-for
+// coarse-graining launch (5), and the totals' per-block slots (6..) for grids of
+// up to kReduceMaxBlocks blocks; zeroed when made.
 constexpr unsigned kReduceMaxBlocks = 304;
-constexpr size_t kCounterWords = 5 + (size_t)kReduceMaxBlocks * 3;
+constexpr size_t kCounterWords = 6 + (size_t)kReduceMaxBlocks * 3;
 // Particles on the lattice into out[0]; the WITH_WALLS moments of every cell
 // (src/moments.rs:37-74, 126-138) into out[0..2] = mass, px2, py2 as 64-bit
 // two's-complement sums.  ticket null: out is device memory, zeroed first (two

@@ -144,7 +144,8 @@ int ensure_inlet(lgx_lattice* lat, uint64_t want) {
   return LGX_OK;
 }
 
-int launch_sample(lgx_lattice* lat, float alpha) {
+int launch_sample(lgx_lattice* lat, float alpha, unsigned long long* flag = nullptr,
+                  unsigned long long seq = 0) {
   if (!lat->has_field) return LGX_OK;
   const size_t nb = (size_t)lat->bw * lat->bh;
   lgx::SampleArgs sa;
@@ -161,7 +162,8 @@ int launch_sample(lgx_lattice* lat, float alpha) {
   sa.rho = lat->field + 2 * nb;
   sa.sol = lat->field + 3 * nb;
   sa.sums = lat->sums;
-  LGX_CUDA(lgx::launch_sample(sa, lat->stream));
+  LGX_CUDA(lgx::launch_sample(sa, lat->stream, reinterpret_cast<unsigned int*>(lat->counter + 5),
+                              flag, seq));
   lat->launches += 1;
   return LGX_OK;
 }
@@ -651,6 +653,14 @@ int lgx_set_temporal_depth(lgx_lattice* lat, int k) {
 int lgx_sample_field(lgx_lattice* lat, float alpha) {
   int rc = check_lat(lat);
   if (rc) return rc;
+  unsigned long long* flag = lgx::host_result_device();
+  if (flag && lat->has_field && lat->bw * lat->bh > 0) {  // the kernel says when it is done
+    const unsigned long long seq = lgx::host_result_seq();
+    rc = launch_sample(lat, alpha, flag + 7, seq);
+    if (rc) return rc;
+    LGX_CUDA(lgx::host_result_wait(seq, lat->stream));
+    return LGX_OK;
+  }
   rc = launch_sample(lat, alpha);
   if (rc) return rc;
   LGX_CUDA(cudaStreamSynchronize(lat->stream));

@@ -36,7 +36,7 @@ __device__ __forceinline__ void block_add(long long (&v)[N], unsigned long long*
 }
 
 // One-launch totals for a call that waits for them: every block writes its sums
-// of v[0..N) to its own slot (slots = ticket + 1, N words per block, at most
+// of v[0..N) to its own slot (slots = ticket + 2, N words per block, at most
 // kReduceMaxBlocks blocks), and the last block to finish (a ticket it sets back
 // to zero) adds the slots and writes the totals to `out`, page-locked host memory
 // mapped into the device's address space.  No zeroing before the launch and no
@@ -60,7 +60,7 @@ __device__ __forceinline__ void block_total_to_host(long long (&v)[N], unsigned 
 #pragma unroll
     for (int k = 0; k < N; ++k) part[warp][k] = v[k];
   __syncthreads();
-  unsigned long long* slots = ticket + 1;
+  unsigned long long* slots = ticket + 2;
   if (warp == 0) {
     const unsigned nw = (blockDim.x + 31u) >> 5;
 #pragma unroll
