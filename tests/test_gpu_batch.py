@@ -280,3 +280,18 @@ def test_resident_steps_per_cluster_barrier_equal_alone(k, fixed):
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "ok" in r.stdout
+
+
+def test_small_lattices_take_the_one_word_per_thread_kernels(LG):
+    """Under the tuner's own choice, a batch of 64 x 64 lattices and one 256 x 256
+    lattice run resident on the kernels that keep each thread on one word of its
+    band (about twice as fast as the others there, so the choice does not flip), and
+    one lattice of 256 x 256 steps through its one-lattice batch."""
+    lats = [LG.GpuLattice(64, 64, True, i) for i in range(8)]
+    plan = LG.Batch(lats, LG.BATCH_AUTO).plan
+    assert len(plan) == 1 and plan[0]["resident"] and plan[0]["word_per_thread"], plan
+    one = LG.Batch([LG.GpuLattice(256, 256, True, 9)], LG.BATCH_AUTO).plan
+    assert one[0]["resident"] and one[0]["word_per_thread"] and one[0]["cluster"] > 1, one
+    g = LG.GpuLattice(256, 256, True, 10)
+    g.advance(8)
+    assert g.step_plan["mode"] == g.STEP_GRAPH, g.step_plan
