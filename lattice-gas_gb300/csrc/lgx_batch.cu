@@ -27,13 +27,16 @@ namespace {
 // compiled for 4 * WORDS resident blocks per SM (64 registers).
 
 template <bool REST>
-__device__ __forceinline__ void batch_word(const LatDesc& d, uint64_t local, uint32_t k,
-                                           uint32_t g, bool live, const Draws& s) {
+// dm: the lattice's Dims copied into registers (read through d at every use, as
+// the update reads them, they are loads from global memory on the step's path:
+// one 2048 x 1280 lattice replayed from graphs ran 4.0 against 3.2 us per step).
+__device__ __forceinline__ void batch_word(const LatDesc& d, const Dims& dm, uint64_t local,
+                                           uint32_t k, uint32_t g, bool live, const Draws& s) {
   const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
   const uint32_t* src = par ? d.planes[1] : d.planes[0];
   uint32_t* dst = par ? d.planes[0] : d.planes[1];
-  const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)k * d.dm.h * d.dm.iw * 7u : nullptr;
-  step_word<REST, false>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, g, live);
+  const uint32_t* inlet = dm.iw ? d.inlet + (size_t)k * dm.h * dm.iw * 7u : nullptr;
+  step_word<REST, false>(src, dst, d.solid, d.anysolid, inlet, dm, s, g, live);
 }
 
 // One step of every lattice of one rule in the batch (blocks first_block ..
@@ -58,6 +61,7 @@ __device__ __forceinline__ void batch_block(const BatchStepArgs& p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
+  const Dims dm = d.dm;
   const uint32_t g0 = (blk - __ldg(p.block0 + li)) * 256u + (threadIdx.x & ~31u) * WORDS +
                       (threadIdx.x & 31u);
   const uint64_t local = *p.base + p.k;
@@ -68,8 +72,8 @@ __device__ __forceinline__ void batch_block(const BatchStepArgs& p) {
 #pragma unroll
   for (int q = 0; q < WORDS; ++q) {
     g[q] = g0 + 32u * q;
-    live[q] = g[q] < d.dm.total;
-    if (!live[q]) g[q] = d.dm.total - 1u;
+    live[q] = g[q] < dm.total;
+    if (!live[q]) g[q] = dm.total - 1u;
     s[q] = draws(g[q] ^ seed32);
   }
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -77,9 +81,9 @@ __device__ __forceinline__ void batch_block(const BatchStepArgs& p) {
 #pragma unroll
   for (int q = 0; q < WORDS; ++q) {
     if (RULE == 2 ? d.rest != 0 : RULE == 1)
-      batch_word<true>(d, local, p.k, g[q], live[q], s[q]);
+      batch_word<true>(d, dm, local, p.k, g[q], live[q], s[q]);
     else
-      batch_word<false>(d, local, p.k, g[q], live[q], s[q]);
+      batch_word<false>(d, dm, local, p.k, g[q], live[q], s[q]);
   }
 }
 
@@ -97,8 +101,9 @@ __global__ void __launch_bounds__(256 / WORDS, 4 * WORDS) lgx_batch_step_kernel(
 template <int RULE, int V, bool INFLOW>
 __device__ __forceinline__ void batch_lane_words(const BatchStepArgs& p, const LatDesc& d,
                                                  uint32_t gq) {
-  const bool live = gq < d.dm.total;
-  if (!live) gq = d.dm.total - V;
+  const Dims dm = d.dm;  // in registers (batch_word)
+  const bool live = gq < dm.total;
+  if (!live) gq = dm.total - V;
   const uint64_t local = *p.base + p.k;
   const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
   Draws s[V];
@@ -109,12 +114,12 @@ __device__ __forceinline__ void batch_lane_words(const BatchStepArgs& p, const L
   const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
   const uint32_t* src = par ? d.planes[1] : d.planes[0];
   uint32_t* dst = par ? d.planes[0] : d.planes[1];
-  const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)p.k * d.dm.h * d.dm.iw * 7u : nullptr;
+  const uint32_t* inlet = dm.iw ? d.inlet + (size_t)p.k * dm.h * dm.iw * 7u : nullptr;
   if (RULE == 2 ? d.rest != 0 : RULE == 1)
-    step_lane_words<true, V, V, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
+    step_lane_words<true, V, V, INFLOW>(src, dst, d.solid, d.anysolid, inlet, dm, s, seed32, gq,
                                         live);
   else
-    step_lane_words<false, V, V, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32,
+    step_lane_words<false, V, V, INFLOW>(src, dst, d.solid, d.anysolid, inlet, dm, s, seed32,
                                          gq, live);
 }
 
@@ -133,24 +138,24 @@ __global__ void __launch_bounds__(64, 8) lgx_batch_lanes4_kernel(BatchStepArgs p
   batch_lane_words<RULE, 4, INFLOW>(p, d, (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 4u);
 }
 
-// Six blocks per SM; with the inflow compiled in the update then spills 28 bytes,
-// which costs latency-bound launches most, so launches of less than one wave of
-// such blocks take a five-block build that does not spill (one 2048 x 1280 lattice
-// with an inflow, replayed from graphs, 4.95 -> 4.01 us per step), and larger ones
-// keep six (five cost the request stream's larger chains about 5%, and without the
-// inflow the transport sweep 1272 -> 1209 Gsite/s).
+// Six blocks per SM for launches of a wave or more (five cost the transport sweep
+// 1272 -> 1209 Gsite/s); launches of less than one wave of such blocks, which are
+// latency-bound, take a five-block build with room for more registers (with the
+// inflow compiled in, the six-block build spilled: one 2048 x 1280 lattice with an
+// inflow replayed from graphs, 4.95 -> 4.01 us per step; without one, 3.70 -> 3.41).
 template <int RULE, bool INFLOW, int MINB = 6>
 __global__ void __launch_bounds__(128, MINB) lgx_batch_lanes_kernel(BatchStepArgs p) {
   const uint32_t blk = p.first_block + blockIdx.x;
   const uint32_t li = p.owner ? __ldg(p.owner + blk) : owner_of(p.block0, p.nlat, blk);
   const LatDesc& d = p.descs[li];
-  if (d.dm.wpr & 1u) {
+  const Dims dm = d.dm;  // in registers (batch_word)
+  if (dm.wpr & 1u) {
     batch_block<RULE, 2>(p);
     return;
   }
   uint32_t gq = (blk - __ldg(p.block0 + li)) * 256u + threadIdx.x * 2u;
-  const bool live = gq < d.dm.total;
-  if (!live) gq = d.dm.total - 2u;
+  const bool live = gq < dm.total;
+  if (!live) gq = dm.total - 2u;
   const uint64_t local = *p.base + p.k;
   const uint32_t seed32 = step_seed32(d.seed, d.steps0 + local);
   Draws s[2];
@@ -161,12 +166,12 @@ __global__ void __launch_bounds__(128, MINB) lgx_batch_lanes_kernel(BatchStepArg
   const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
   const uint32_t* src = par ? d.planes[1] : d.planes[0];
   uint32_t* dst = par ? d.planes[0] : d.planes[1];
-  const uint32_t* inlet = d.dm.iw ? d.inlet + (size_t)p.k * d.dm.h * d.dm.iw * 7u : nullptr;
+  const uint32_t* inlet = dm.iw ? d.inlet + (size_t)p.k * dm.h * dm.iw * 7u : nullptr;
   if (RULE == 2 ? d.rest != 0 : RULE == 1)
-    step_lane_words<true, 2, 2, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32, gq,
+    step_lane_words<true, 2, 2, INFLOW>(src, dst, d.solid, d.anysolid, inlet, dm, s, seed32, gq,
                                         live);
   else
-    step_lane_words<false, 2, 2, INFLOW>(src, dst, d.solid, d.anysolid, inlet, d.dm, s, seed32,
+    step_lane_words<false, 2, 2, INFLOW>(src, dst, d.solid, d.anysolid, inlet, dm, s, seed32,
                                          gq, live);
 }
 
@@ -264,6 +269,12 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, uint32_t nblocks, int rule
       if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, true>, a);
       if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, true>, a);
       return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0, true>, a);
+    }
+    if (nblocks < 152u * 6u) {
+      if (rule == kRuleMixed)
+        return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, false, 5>, a);
+      if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, false, 5>, a);
+      return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<0, false, 5>, a);
     }
     if (rule == kRuleMixed) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<2, false>, a);
     if (rule == kRuleRest) return cudaLaunchKernelEx(&cfg, lgx_batch_lanes_kernel<1, false>, a);

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_kernel(const ResidentArg
   const uint32_t li = p.first_lat + blockIdx.x / C;
   const LatDesc& d = p.descs[li];
   const ResSched sch = p.sched[li];
-  const Dims& dm = d.dm;
+  const Dims dm = d.dm;  // in registers, not read through d at every use
   const size_t S = dm.total;
   const uint32_t y0 = band_start(rank, dm.h, C), y1 = band_start(rank + 1u, dm.h, C);
   const uint32_t cap = (dm.h + C - 1u) / C;      // rows of the largest band
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(THREADS) lgx_resident_multi_kernel(const Resid
   const uint32_t li = p.first_lat + blockIdx.x / C;
   const LatDesc& d = p.descs[li];
   const ResSched sch = p.sched[li];
-  const Dims& dm = d.dm;
+  const Dims dm = d.dm;  // in registers, not read through d at every use
   const size_t S = dm.total;
   const uint32_t K = p.ksteps;
   const uint32_t y0 = band_start(rank, dm.h, C), y1 = band_start(rank + 1u, dm.h, C);
