@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kThreads) lgx_profile_kernel(const ProfArgs p)
   if (d.every == 0 ? rel != 0 : rel % d.every != 0) return;
   const uint64_t slot = d.every ? rel / d.every : 0;
   if (slot >= d.count) return;
-  const Dims& dm = d.dm;
+  const Dims dm = d.dm;  // in registers, not read through d at every use
   const uint32_t nchunks = (dm.h + kRows - 1) / kRows;
   if (blockIdx.x >= nchunks) return;
   const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
