@@ -167,11 +167,13 @@ __device__ __forceinline__ void fixed_step(const FixedWord& f, const Draws& cur,
 }
 
 // The inflow draws of step k of the launch for this thread's word (zeros off
-// the inflow or past the launch's last step).
-__device__ __forceinline__ void load_bern(const LatDesc& d, const FixedWord& f, bool lane_inflow,
-                                          uint32_t k, uint32_t len, uint32_t bern[7]) {
+// the inflow or past the launch's last step); inlet and its per-step stride held
+// in registers.
+__device__ __forceinline__ void load_bern(const uint32_t* inlet, size_t stride,
+                                          const FixedWord& f, bool lane_inflow, uint32_t k,
+                                          uint32_t len, uint32_t bern[7]) {
   const bool on = lane_inflow && k < len;
-  const uint32_t* bp = d.inlet + (size_t)k * d.dm.h * d.dm.iw * 7u + f.boff;
+  const uint32_t* bp = inlet + (size_t)k * stride + f.boff;
 #pragma unroll
   for (int q = 0; q < 7; ++q) bern[q] = on ? __ldg(bp + q) : 0u;
 }
@@ -263,14 +265,16 @@ __device__ __forceinline__ void fixed_single(const ResidentArgs& p, uint32_t* sh
   const bool inflow = dm.iw != 0u, lane_inflow = inflow && j < dm.iw;
   const bool ragged = dm.tail != 0xffffffffu;
   SampleClock clock(p.sched[li], d.bw * d.bh != 0u);
-  const uint64_t s0 = d.steps0 + base;
-  Draws cur = draws(f.g ^ step_seed32(d.seed, s0)), nxt;
+  const uint64_t s0 = d.steps0 + base, seed = d.seed;
+  const uint32_t* inl = d.inlet;
+  const size_t istride = (size_t)dm.h * dm.iw * 7u;
+  Draws cur = draws(f.g ^ step_seed32(seed, s0)), nxt;
   uint32_t bern[7], bnext[7];
-  if (inflow) load_bern(d, f, lane_inflow, 0, p.len, bern);
+  if (inflow) load_bern(inl, istride, f, lane_inflow, 0, p.len, bern);
   __syncthreads();  // the lattice is in buffer 0
   for (uint32_t k = 0; k < p.len; ++k) {
-    const uint32_t key = f.g ^ step_seed32(d.seed, s0 + k + 1u);
-    if (inflow) load_bern(d, f, lane_inflow, k + 1u, p.len, bnext);
+    const uint32_t key = f.g ^ step_seed32(seed, s0 + k + 1u);
+    if (inflow) load_bern(inl, istride, f, lane_inflow, k + 1u, p.len, bnext);
     if (k & 1u)
       fixed_step<1, REST>(f, cur, nxt, key, any_solid, inflow, bern, ragged, live);
     else
@@ -355,10 +359,12 @@ __device__ __forceinline__ void fixed_multi(const ResidentArgs& p, uint32_t* shm
   const bool inflow = dm.iw != 0u, lane_inflow = inflow && j < dm.iw;
   const bool ragged = dm.tail != 0xffffffffu;
   SampleClock clock(p.sched[li], d.bw * d.bh != 0u);
-  const uint64_t s0 = d.steps0 + base;
-  Draws cur = draws(f.g ^ step_seed32(d.seed, s0)), nxt;
+  const uint64_t s0 = d.steps0 + base, seed = d.seed;
+  const uint32_t* inl = d.inlet;
+  const size_t istride = (size_t)dm.h * dm.iw * 7u;
+  Draws cur = draws(f.g ^ step_seed32(seed, s0)), nxt;
   uint32_t bern[7], bnext[7];
-  if (inflow) load_bern(d, f, lane_inflow, 0, p.len, bern);
+  if (inflow) load_bern(inl, istride, f, lane_inflow, 0, p.len, bern);
 
   uint32_t buf = 0;  // the buffer holding the state after step t
   for (uint32_t t = 0; t < p.len;) {
@@ -382,9 +388,9 @@ __device__ __forceinline__ void fixed_multi(const ResidentArgs& p, uint32_t* shm
     __syncthreads();
     for (uint32_t s = 1; s <= k; ++s) {
       const uint32_t ks = t + s - 1u;  // step of the launch
-      const uint32_t key = f.g ^ step_seed32(d.seed, s0 + ks + 1u);
+      const uint32_t key = f.g ^ step_seed32(seed, s0 + ks + 1u);
       const bool act = live && r - (K - k + s) < nb + 2u * (k - s);
-      if (inflow) load_bern(d, f, lane_inflow, ks + 1u, p.len, bnext);
+      if (inflow) load_bern(inl, istride, f, lane_inflow, ks + 1u, p.len, bnext);
       if (__any_sync(0xffffffffu, act)) {
         if (buf)
           fixed_step<1, REST>(f, cur, nxt, key, any_solid, inflow, bern, ragged, act);
