@@ -198,8 +198,12 @@ __global__ void __launch_bounds__(128) lgx_batch_inlet_kernel(BatchInletArgs p) 
 
 // Coarse-graining of every lattice with a field: one warp per field block,
 // the lattice found by binary search over the block prefix.  The state read
-// is the one after batch step *base + k_after.
+// is the one after batch step *base + k_after.  Launched with programmatic
+// stream serialisation, as the one-lattice sampling kernel is: the next step's
+// grid may start its draws at once; this one waits for the step before it.
 __global__ void __launch_bounds__(256) lgx_batch_sample_kernel(BatchSampleArgs p) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const uint32_t task = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (task >= p.total_blocks) return;
   const uint32_t lo = owner_of(p.blk0, p.nlat, task);
@@ -221,7 +225,7 @@ __global__ void __launch_bounds__(256) lgx_batch_sample_kernel(BatchSampleArgs p
   sa.rho = d.field + 2 * nb;
   sa.sol = d.field + 3 * nb;
   sa.sums = d.sums;
-  sample_block(sa, task - p.blk0[lo]);
+  sample_block<true>(sa, task - p.blk0[lo]);
 }
 
 __global__ void lgx_batch_base_kernel(uint64_t* base, uint32_t n) { *base += n; }
@@ -298,8 +302,16 @@ cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st) {
 
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st) {
   if (a.total_blocks == 0) return cudaSuccess;
-  lgx_batch_sample_kernel<<<(a.total_blocks + 7) / 8, 256, 0, st>>>(a);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((a.total_blocks + 7) / 8);
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, lgx_batch_sample_kernel, a);
 }
 
 cudaError_t launch_batch_owner(const uint32_t* block0, uint32_t nlat, uint32_t nblocks,

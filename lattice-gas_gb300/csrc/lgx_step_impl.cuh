@@ -340,6 +340,35 @@ __device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
   }
 }
 
+// The end of one field block's coarse-graining, from its exact sums and its
+// running averages before the blend (u0, v0, r0): the sums out, the block's
+// f32 velocity (Moments::velocity, src/moments.rs:91-97) and its blend into the
+// averages with round-to-nearest intrinsics, so no fused multiply-add can
+// change the last bit (lgca_sample, src/gpu.rs:324-377).
+__device__ __forceinline__ void sample_finish(const SampleArgs& p, uint32_t blk, int mass, int px,
+                                              int py, int nsolid, float u0, float v0, float r0) {
+  constexpr float kSqrt3_2 = 0.8660254f;  // src/hex.rs:25
+  const uint32_t nb = p.bw * p.bh;
+  if (p.sums) {
+    p.sums[blk] = mass;
+    p.sums[nb + blk] = px;
+    p.sums[2 * nb + blk] = py;
+    p.sums[3 * nb + blk] = nsolid;
+  }
+  const float n = __uint2float_rn(p.bx * p.by);
+  const float m = __int2float_rn(mass);
+  float vx = 0.0f, vy = 0.0f;
+  if (mass > 0) {
+    vx = __fdiv_rn(__fmul_rn(__int2float_rn(px), 0.5f), m);
+    vy = __fdiv_rn(__fmul_rn(__int2float_rn(py), kSqrt3_2), m);
+  }
+  const float a = p.alpha;
+  p.ux[blk] = __fadd_rn(u0, __fmul_rn(a, __fsub_rn(vx, u0)));
+  p.uy[blk] = __fadd_rn(v0, __fmul_rn(a, __fsub_rn(vy, v0)));
+  p.rho[blk] = __fadd_rn(r0, __fmul_rn(a, __fsub_rn(__fdiv_rn(m, n), r0)));
+  p.sol[blk] = __fdiv_rn(__int2float_rn(nsolid), n);
+}
+
 // Coarse-graining of field block `blk` of one lattice by one whole warp
 // (lgca_sample, src/gpu.rs:324-377).  Lanes take rows of the block; each row
 // contributes the masked popcounts of the one to several words the block's
@@ -347,10 +376,19 @@ __device__ __forceinline__ void step_lane_words(const uint32_t* __restrict__ a,
 // CX2 * count, py2, nsolid), reduced across the warp, and only then turned
 // into f32 velocity and blended into the running average with
 // round-to-nearest intrinsics, so no fused multiply-add can change the last
-// bit (Moments::velocity, src/moments.rs:91).
+// bit (Moments::velocity, src/moments.rs:91).  EARLY: lane 0 reads the block's
+// running averages before the planes, so the two reads' latencies overlap (the
+// stand-alone sampling kernel; the resident kernels, short of registers, read
+// them after the sums).
+template <bool EARLY = false>
 __device__ __forceinline__ void sample_block(const SampleArgs& p, uint32_t blk) {
-  constexpr float kSqrt3_2 = 0.8660254f;  // src/hex.rs:25
   const uint32_t lane = threadIdx.x & 31u;
+  float u0 = 0.0f, v0 = 0.0f, r0 = 0.0f;
+  if (EARLY && lane == 0) {
+    u0 = p.ux[blk];
+    v0 = p.uy[blk];
+    r0 = p.rho[blk];
+  }
   const uint32_t jb = blk / p.bw, ib = blk - jb * p.bw;
   const uint32_t x0 = ib * p.bx, x1 = x0 + p.bx;
   const uint32_t w0 = x0 >> 5, w1 = (x1 - 1u) >> 5;
@@ -384,26 +422,12 @@ __device__ __forceinline__ void sample_block(const SampleArgs& p, uint32_t blk) 
   py = __reduce_add_sync(FULL, py);
   nsolid = __reduce_add_sync(FULL, nsolid);
   if (lane != 0) return;
-  const uint32_t nb = p.bw * p.bh;
-  if (p.sums) {
-    p.sums[blk] = mass;
-    p.sums[nb + blk] = px;
-    p.sums[2 * nb + blk] = py;
-    p.sums[3 * nb + blk] = nsolid;
+  if (!EARLY) {
+    u0 = p.ux[blk];
+    v0 = p.uy[blk];
+    r0 = p.rho[blk];
   }
-  const float n = __uint2float_rn(p.bx * p.by);
-  const float m = __int2float_rn(mass);
-  float vx = 0.0f, vy = 0.0f;
-  if (mass > 0) {
-    vx = __fdiv_rn(__fmul_rn(__int2float_rn(px), 0.5f), m);
-    vy = __fdiv_rn(__fmul_rn(__int2float_rn(py), kSqrt3_2), m);
-  }
-  const float a = p.alpha;
-  const float u0 = p.ux[blk], v0 = p.uy[blk], r0 = p.rho[blk];
-  p.ux[blk] = __fadd_rn(u0, __fmul_rn(a, __fsub_rn(vx, u0)));
-  p.uy[blk] = __fadd_rn(v0, __fmul_rn(a, __fsub_rn(vy, v0)));
-  p.rho[blk] = __fadd_rn(r0, __fmul_rn(a, __fsub_rn(__fdiv_rn(m, n), r0)));
-  p.sol[blk] = __fdiv_rn(__int2float_rn(nsolid), n);
+  sample_finish(p, blk, mass, px, py, nsolid, u0, v0, r0);
 }
 
 }  // namespace lgx

@@ -148,6 +148,52 @@ def test_the_gpu_coarse_grains_the_same_field(LG, O, w, h, block):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("w,h,bx,by", [
+    (200, 40, 15, 8),      # below 16 columns: one warp per block
+    (256, 64, 16, 16), (250, 42, 16, 7), (300, 40, 17, 20), (2048, 80, 20, 20),
+    (263, 66, 31, 33), (4096, 64, 32, 32), (330, 36, 33, 1), (500, 50, 48, 5),
+    (1000, 24, 100, 12), (900, 30, 250, 3),
+    (2400, 14, 1100, 7),   # one block per CTA, its words past one warp's lanes
+])
+def test_the_coarse_graining_tiles_match_the_oracle(LG, O, w, h, bx, by):
+    """Field::sample (src/gpu.rs:324-377) for block widths on either side of the
+    tiled kernel's 16 columns, blocks that straddle words and tiles, narrow and tall
+    blocks and a partial last block column, with obstacles: the block sums and the
+    running average after two blended samples, bit for bit, through both the
+    waiting call (sample_field) and the sampling steps (advance_sampling)."""
+    cells = np.zeros(w * h, np.uint8)
+    LG.add_circle(cells, w, h, w * 0.37, h * 0.5, h * 0.3)
+    LG.add_box(cells, w, h, w * 0.7, w * 0.75, 0.0, h * 0.4, False)
+    LG.init_equilibrium(cells, 0.3, 0.2, 0.05, True, 91)
+    want = O.Field(w, h, bx, by)
+    want.sample(cells, w, h, np.float32(0.3))
+    g = LG.GpuLattice(w, h, True, 3)
+    g.attach_field(bx, by)
+    g.load(cells)
+    g.sample_field(0.3)
+    o = O.BitplaneLattice(w, h, True, 3, THREADS)
+    o.attach_field(bx, by)
+    o.load(cells)
+    g.advance_sampling(12, 5, 0.6)
+    o.advance_sampling(12, 5, 0.6)
+    assert_same(g, o, with_field=False)
+    for x, y in zip(g.read_block_sums(), o.read_block_sums()):
+        assert np.array_equal(x, y)
+    h2 = LG.GpuLattice(w, h, True, 3)
+    h2.attach_field(bx, by)
+    h2.load(cells)
+    h2.sample_field(0.3)
+    h2.advance(7)
+    cur = h2.store()
+    want.sample(cur, w, h, np.float32(0.7))
+    h2.sample_field(0.7)
+    f = h2.read_field()
+    for a, b in zip((want.ux, want.uy, want.rho, want.solid), (f.ux, f.uy, f.rho, f.solid)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    for a, b in zip(O.block_sums(cur, w, h, bx, by), h2.read_block_sums()):
+        assert np.array_equal(a, b)
+
+
 def test_the_gpu_field_averages_over_time(LG, O):
     """src/gpu.rs:999-1032, bit-exact."""
     ALPHA = 0.2
