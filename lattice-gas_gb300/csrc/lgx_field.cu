@@ -43,109 +43,19 @@ __global__ void __launch_bounds__(256) lgx_sample_kernel(const SampleArgs p, uns
   }
 }
 
-// Coarse-graining by tiles, for fields whose blocks are at least
-// kTileMinWidth columns wide: a CTA takes `per` consecutive blocks of one block
-// row; its 32 x 8 threads take the words those blocks' columns cover (x: one
-// word per lane, so a warp's loads are coalesced) and the block row's rows (y:
-// every eighth row).  A word meets at most three such blocks; a thread sums,
-// over its rows, its word's masked popcounts for each block it meets, and adds
-// them into the CTA's per-block totals in shared memory.  The totals are the
-// same exact integers as sample_block's, so the field is the same; the warp
-// per block there reads each word's 32-byte sector once per block that meets
-// it, with lanes 4 KB apart.
-constexpr uint32_t kTileMinWidth = 16;
-constexpr uint32_t kTileRows = 8;
-constexpr uint32_t kTileBatch = 4;
-constexpr uint32_t kTileMaxBlocks = 64;
-
-__device__ __forceinline__ uint32_t bit_range(uint32_t lo, uint32_t hi) {  // bits [lo, hi)
-  return hi - lo >= 32u ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << lo);
-}
-
+// The tiles of sample_tile as a grid of their own (256 threads: eight rows
+// apart), launched with programmatic serialisation as lgx_sample_kernel is.
 __global__ void __launch_bounds__(256) lgx_sample_tiles_kernel(const SampleArgs p, uint32_t per,
                                                                uint32_t ncx, unsigned int* done,
                                                                unsigned long long* flag,
                                                                unsigned long long seq) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   __shared__ int acc[4][kTileMaxBlocks];
-  const uint32_t t = threadIdx.x;
-  for (uint32_t i = t; i < 4u * kTileMaxBlocks; i += blockDim.x) (&acc[0][0])[i] = 0;
-  const uint32_t jb = blockIdx.x / ncx, ib0 = (blockIdx.x - jb * ncx) * per;
-  const uint32_t nb = min(per, p.bw - ib0);
-  const uint32_t fb = jb * p.bw + ib0;  // field index of the CTA's first block
-  __syncthreads();
-  // the previous grid (a step) complete; the running averages were written by
-  // an earlier grid still, so they are read only after the wait too
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  float u0 = 0.0f, v0 = 0.0f, r0 = 0.0f;
-  if (t < nb) {
-    u0 = p.ux[fb + t];
-    v0 = p.uy[fb + t];
-    r0 = p.rho[fb + t];
-  }
-  const uint32_t x0 = ib0 * p.bx, x1 = x0 + nb * p.bx;  // the CTA's columns
-  const uint32_t w0 = x0 >> 5, nw = ((x1 - 1u) >> 5) - w0 + 1u;
-  const size_t S = p.dm.total;
-  const size_t row0 = (size_t)jb * p.by;
-  for (uint32_t wo = t & 31u; wo < nw; wo += 32u) {
-    const uint32_t wi = w0 + wo;
-    const uint32_t lo = max(x0, wi << 5), hi = min(x1, (wi << 5) + 32u);
-    const uint32_t b0 = lo / p.bx;  // the first block the word meets
-    uint32_t m[3];
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const uint32_t c0 = max(lo, (b0 + s) * p.bx), c1 = min(hi, (b0 + s + 1u) * p.bx);
-      m[s] = c1 > c0 ? bit_range(c0 - (wi << 5), c1 - (wi << 5)) : 0u;
-    }
-    int mass[3] = {0, 0, 0}, px[3] = {0, 0, 0}, py[3] = {0, 0, 0}, ns[3] = {0, 0, 0};
-    // kTileBatch rows' words are loaded before any is counted, so their loads
-    // are in flight together (a row past the block row loads nothing and counts 0)
-    for (uint32_t r0w = t >> 5; r0w < p.by; r0w += kTileRows * kTileBatch) {
-      uint32_t sw[kTileBatch], pl[kTileBatch][7];
-#pragma unroll
-      for (int q = 0; q < (int)kTileBatch; ++q) {
-        const uint32_t r = r0w + q * kTileRows;
-        const size_t at = (row0 + r) * p.dm.wpr + wi;
-        const bool in = r < p.by;
-        sw[q] = in ? __ldg(p.solid + at) : 0u;
-#pragma unroll
-        for (int d = 0; d < 7; ++d) pl[q][d] = in ? __ldg(p.a + d * S + at) : 0u;
-      }
-#pragma unroll
-      for (int q = 0; q < (int)kTileBatch; ++q) {
-#pragma unroll
-        for (int s = 0; s < 3; ++s) {
-          if (!m[s]) continue;  // most words meet one or two blocks
-          const uint32_t sm = sw[q] & m[s];
-          const uint32_t fm = m[s] & ~sm;
-          ns[s] += __popc(sm);
-          const int c0 = __popc(pl[q][0] & fm), c1 = __popc(pl[q][1] & fm);
-          const int c2 = __popc(pl[q][2] & fm), c3 = __popc(pl[q][3] & fm);
-          const int c4 = __popc(pl[q][4] & fm), c5 = __popc(pl[q][5] & fm);
-          const int c6 = __popc(pl[q][6] & fm);
-          mass[s] += c0 + c1 + c2 + c3 + c4 + c5 + c6;
-          // CX2 = {2, 1, -1, -2, -1, 1}, CY2 = {0, 1, 1, 0, -1, -1}
-          px[s] += 2 * (c0 - c3) + c1 - c2 - c4 + c5;
-          py[s] += c1 + c2 - c4 - c5;
-        }
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      if (!m[s]) continue;
-      const uint32_t k = b0 + s - ib0;
-      atomicAdd(&acc[0][k], mass[s]);
-      atomicAdd(&acc[1][k], px[s]);
-      atomicAdd(&acc[2][k], py[s]);
-      atomicAdd(&acc[3][k], ns[s]);
-    }
-  }
-  __syncthreads();
-  if (t < nb) sample_finish(p, fb + t, acc[0][t], acc[1][t], acc[2][t], acc[3][t], u0, v0, r0);
+  sample_tile<4>(p, blockIdx.x, per, ncx, acc);
   if (!flag) return;
   __threadfence_system();
   __syncthreads();
-  if (t == 0 && atomicAdd(done, 1u) == gridDim.x - 1u) {
+  if (threadIdx.x == 0 && atomicAdd(done, 1u) == gridDim.x - 1u) {
     *done = 0u;
     __threadfence_system();
     *reinterpret_cast<volatile unsigned long long*>(flag) = seq;
@@ -753,6 +663,20 @@ cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long
   return cudaGetLastError();
 }
 
+bool sample_tiling(const SampleArgs& s, SampleTiles* t) {
+  if (s.bx < kTileMinWidth || s.bw * s.bh == 0) return false;
+  // as many blocks per CTA as keep their words within one warp's lanes (a
+  // block-aligned start can sit 31 columns into its first word), spread evenly
+  // over the block row
+  uint32_t most = (1024u - 31u) / s.bx;
+  most = most < 1u ? 1u : (most > kTileMaxBlocks ? kTileMaxBlocks : most);
+  t->s = s;
+  t->ncx = (s.bw + most - 1u) / most;
+  t->per = (s.bw + t->ncx - 1u) / t->ncx;
+  t->nblocks = t->ncx * s.bh;
+  return true;
+}
+
 cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st, unsigned int* done,
                           unsigned long long* flag, unsigned long long seq) {
   const uint32_t nb = s.bw * s.bh;
@@ -766,16 +690,10 @@ cudaError_t launch_sample(const SampleArgs& s, cudaStream_t st, unsigned int* do
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (s.bx >= kTileMinWidth) {
-    // as many blocks per CTA as keep their words within one warp's lanes
-    // (a block-aligned start can sit 31 columns into its first word), spread
-    // evenly over the block row
-    uint32_t most = (1024u - 31u) / s.bx;
-    most = most < 1u ? 1u : (most > kTileMaxBlocks ? kTileMaxBlocks : most);
-    const uint32_t ncx = (s.bw + most - 1u) / most;
-    const uint32_t per = (s.bw + ncx - 1u) / ncx;
-    cfg.gridDim = dim3(ncx * s.bh);
-    return cudaLaunchKernelEx(&cfg, lgx_sample_tiles_kernel, s, per, ncx, done, flag, seq);
+  SampleTiles t;
+  if (sample_tiling(s, &t)) {
+    cfg.gridDim = dim3(t.nblocks);
+    return cudaLaunchKernelEx(&cfg, lgx_sample_tiles_kernel, s, t.per, t.ncx, done, flag, seq);
   }
   cfg.gridDim = dim3((nb + 7) / 8);
   return cudaLaunchKernelEx(&cfg, lgx_sample_kernel, s, done, flag, seq);

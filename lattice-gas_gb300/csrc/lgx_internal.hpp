@@ -28,6 +28,33 @@ struct Dims {
 Dims make_dims(uint32_t w, uint32_t h, uint32_t inlet_cols);
 
 // One step of one lattice: a -> b.
+// Coarse-graining of one lattice into bw x bh blocks of bx x by cells.
+struct SampleArgs {
+  const uint32_t* a;
+  const uint32_t* solid;
+  Dims dm;
+  uint32_t bx, by, bw, bh;
+  float alpha;
+  float* ux;
+  float* uy;
+  float* rho;
+  float* sol;
+  int32_t* sums;  // [4][bw*bh]: mass, px2, py2, nsolid
+};
+
+// Coarse-graining by tiles (blocks at least kTileMinWidth columns wide): CTAs
+// over `per` consecutive blocks of one block row each, `ncx` of them per block
+// row, `nblocks` in all (0: none).  A single step can carry one: its grid then
+// leads with these CTAs, which coarse-grain the step's input state.
+constexpr uint32_t kTileMinWidth = 16;
+constexpr uint32_t kTileMaxBlocks = 64;
+struct SampleTiles {
+  SampleArgs s;
+  uint32_t per, ncx, nblocks;
+};
+// The tiling of a field, or false when its blocks are too narrow for tiles.
+bool sample_tiling(const SampleArgs& s, SampleTiles* t);
+
 struct StepArgs {
   const uint32_t* a;
   uint32_t* b;
@@ -38,6 +65,7 @@ struct StepArgs {
   uint64_t seed;
   uint64_t steps;  // steps taken before this one
   uint32_t words;  // the kernel's shape, a kShape* value (0: chosen by the lattice's size)
+  SampleTiles tiles = {};  // the state this step reads, coarse-grained alongside (nblocks > 0)
 };
 
 // Shapes of the single-step kernel.  Chunk1, Chunk2: one word per lane, a warp
@@ -87,20 +115,6 @@ struct InletArgs {
   uint64_t steps;
   uint32_t nsteps;
   uint32_t thresh[7];
-};
-
-// Coarse-graining of one lattice into bw x bh blocks of bx x by cells.
-struct SampleArgs {
-  const uint32_t* a;
-  const uint32_t* solid;
-  Dims dm;
-  uint32_t bx, by, bw, bh;
-  float alpha;
-  float* ux;
-  float* uy;
-  float* rho;
-  float* sol;
-  int32_t* sums;  // [4][bw*bh]: mass, px2, py2, nsolid
 };
 
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st);

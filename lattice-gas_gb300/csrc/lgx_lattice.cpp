@@ -144,9 +144,7 @@ int ensure_inlet(lgx_lattice* lat, uint64_t want) {
   return LGX_OK;
 }
 
-int launch_sample(lgx_lattice* lat, float alpha, unsigned long long* flag = nullptr,
-                  unsigned long long seq = 0) {
-  if (!lat->has_field) return LGX_OK;
+lgx::SampleArgs sample_args(const lgx_lattice* lat, float alpha) {
   const size_t nb = (size_t)lat->bw * lat->bh;
   lgx::SampleArgs sa;
   sa.a = lat->planes[lat->cur];
@@ -162,6 +160,13 @@ int launch_sample(lgx_lattice* lat, float alpha, unsigned long long* flag = null
   sa.rho = lat->field + 2 * nb;
   sa.sol = lat->field + 3 * nb;
   sa.sums = lat->sums;
+  return sa;
+}
+
+int launch_sample(lgx_lattice* lat, float alpha, unsigned long long* flag = nullptr,
+                  unsigned long long seq = 0) {
+  if (!lat->has_field) return LGX_OK;
+  const lgx::SampleArgs sa = sample_args(lat, alpha);
   LGX_CUDA(lgx::launch_sample(sa, lat->stream, reinterpret_cast<unsigned int*>(lat->counter + 5),
                               flag, seq));
   lat->launches += 1;
@@ -221,7 +226,9 @@ int enqueue_temporal(lgx_lattice* lat, uint32_t k) {
   return LGX_OK;
 }
 
-int enqueue_single(lgx_lattice* lat) {
+// tiles: coarse-graining of the state this step reads, run in the step's grid
+// (null: none).
+int enqueue_single(lgx_lattice* lat, const lgx::SampleTiles* tiles = nullptr) {
   lgx::StepArgs sa;
   sa.a = lat->planes[lat->cur];
   sa.b = lat->planes[lat->cur ^ 1];
@@ -236,6 +243,7 @@ int enqueue_single(lgx_lattice* lat) {
   sa.words = lat->step_words ? lat->step_words
              : (lat->step_mode == LGX_STEP_AUTO && lat->auto_resolved) ? lat->auto_words
                                                                         : 0u;
+  if (tiles) sa.tiles = *tiles;
   LGX_CUDA(lgx::launch_step(sa, lat->rest, lat->stream));
   lat->launches += 1;
   lat->cur ^= 1;
@@ -310,6 +318,12 @@ int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
   }
   const bool wave = mode == LGX_STEP_WAVE;
   const bool temporal = mode == LGX_STEP_TEMPORAL && lgx::temporal_supported(lat->dm, tk);
+  // One launch per step: a sampling point followed by another step of the run
+  // is coarse-grained inside that step's grid (its tiles read the state the
+  // step reads), which saves the sampling kernel's launch and the drain of the
+  // steps around it; the run's last sampling point takes the sampling kernel.
+  lgx::SampleTiles tiles;
+  bool pending = false;
   while (left > 0) {
     int rc = ensure_inlet(lat, left);
     if (rc) return rc;
@@ -325,14 +339,19 @@ int enqueue_steps(lgx_lattice* lat, uint64_t n, uint64_t every, float alpha) {
       if (lat->dm.iw) k = std::min<uint64_t>(k, lat->inlet_first + lat->inlet_valid - lat->steps);
       rc = enqueue_wave(lat, (uint32_t)k);
     } else {
-      rc = enqueue_single(lat);
+      rc = enqueue_single(lat, pending ? &tiles : nullptr);
+      pending = false;
     }
     if (rc) return rc;
     left -= k;
     since += k;
     if (every > 0 && (since >= every || left == 0)) {
       since = 0;
-      rc = launch_sample(lat, alpha);
+      if (left > 0 && !wave && !temporal && lat->has_field &&
+          lgx::sample_tiling(sample_args(lat, alpha), &tiles))
+        pending = true;
+      else
+        rc = launch_sample(lat, alpha);
       if (rc) return rc;
     }
   }

@@ -62,12 +62,26 @@ constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
 // visible (griddepcontrol.wait).  Step N+1's draws thereby fill the SMs that
 // step N's last blocks leave idle.  Without a programmatic predecessor the
 // wait returns at once, so the kernel is also correct launched plainly.
-template <bool REST, int WORDS>
+//
+// SAMPLE: the grid leads with p.tiles.nblocks coarse-graining tiles of the
+// state the step reads (sample_tile), which run beside the step's blocks; the
+// step writes the other plane set, and the next grid waits for both.
+template <bool REST, int WORDS, bool SAMPLE = false>
 __global__ void __launch_bounds__(256 / WORDS, WORDS == 1 ? LGX_STEP_MINB1 : LGX_STEP_MINB)
     lgx_step_kernel(const StepArgs p) {
+  uint32_t bid = blockIdx.x;
+  if (SAMPLE) {
+    if (bid < p.tiles.nblocks) {
+      asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+      __shared__ int acc[4][kTileMaxBlocks];
+      sample_tile<WORDS == 1 ? 2 : 4>(p.tiles.s, bid, p.tiles.per, p.tiles.ncx, acc);
+      return;
+    }
+    bid -= p.tiles.nblocks;
+  }
   // a warp takes WORDS consecutive 32-word chunks; a block covers 256 words
   constexpr int kStepWords = WORDS;
-  const uint32_t g0 = blockIdx.x * 256u + (threadIdx.x & ~31u) * kStepWords + (threadIdx.x & 31u);
+  const uint32_t g0 = bid * 256u + (threadIdx.x & ~31u) * kStepWords + (threadIdx.x & 31u);
   const uint32_t seed32 = step_seed32(p.seed, p.steps);
   uint32_t g[kStepWords];
   bool live[kStepWords];
@@ -100,11 +114,22 @@ __global__ void __launch_bounds__(256 / WORDS, WORDS == 1 ? LGX_STEP_MINB1 : LGX
 // FMA pipe: 6.03 / 297.0.  Two words per lane are allowed six blocks per SM (80
 // registers), five with the inflow compiled in: at six it spilled 24 bytes, and a
 // 2048 x 1280 step with an 8-column inflow took 4.55 us against 3.89.
-template <bool REST, int V, bool INFLOW>
+// SAMPLE: coarse-graining tiles lead the grid, as in lgx_step_kernel.
+template <bool REST, int V, bool INFLOW, bool SAMPLE = false>
 __global__ void __launch_bounds__(128, V == 4 ? 4 : (INFLOW ? 5 : 6))
     lgx_step_lanes_kernel(const StepArgs p) {
+  uint32_t bid = blockIdx.x;
+  if (SAMPLE) {
+    if (bid < p.tiles.nblocks) {
+      asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+      __shared__ int acc[4][kTileMaxBlocks];
+      sample_tile<4>(p.tiles.s, bid, p.tiles.per, p.tiles.ncx, acc);
+      return;
+    }
+    bid -= p.tiles.nblocks;
+  }
   constexpr int E = V;  // draws made before the wait
-  const uint32_t warp = blockIdx.x * 4u + (threadIdx.x >> 5);
+  const uint32_t warp = bid * 4u + (threadIdx.x >> 5);
   uint32_t gq = warp * (32u * V) + (threadIdx.x & 31u) * V;
   const bool live = gq < p.dm.total;
   if (!live) gq = p.dm.total - V;
@@ -263,6 +288,31 @@ uint32_t step_shape(const Dims& dm, uint32_t shape) {
   return dm.wpr % 2u == 0u ? kShapeLanes2 : kShapeChunk1;
 }
 
+template <bool S>
+cudaError_t launch_shape(const cudaLaunchConfig_t& cfg, const StepArgs& s, uint32_t shape,
+                         bool rest, bool in) {
+  switch (shape) {
+    case kShapeLanes4:
+      if (in)
+        return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4, true, S>, s)
+                    : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4, true, S>, s);
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4, false, S>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4, false, S>, s);
+    case kShapeLanes2:
+      if (in)
+        return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2, true, S>, s)
+                    : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2, true, S>, s);
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2, false, S>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2, false, S>, s);
+    case kShapeChunk2:
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 2, S>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 2, S>, s);
+    default:
+      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 1, S>, s)
+                  : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 1, S>, s);
+  }
+}
+
 cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   uint32_t shape = step_shape(s.dm, s.words);
@@ -288,26 +338,9 @@ cudaError_t launch_step(const StepArgs& s, bool rest, cudaStream_t st) {
   // registers: 0.8% on 32768 x 16384 without one, against 2.9% gained on the
   // wake run and 5.7% at 1024 x 512 with one)
   const bool in = s.dm.iw != 0u;
-  switch (shape) {
-    case kShapeLanes4:
-      if (in)
-        return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4, true>, s)
-                    : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4, true>, s);
-      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 4, false>, s)
-                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 4, false>, s);
-    case kShapeLanes2:
-      if (in)
-        return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2, true>, s)
-                    : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2, true>, s);
-      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<true, 2, false>, s)
-                  : cudaLaunchKernelEx(&cfg, lgx_step_lanes_kernel<false, 2, false>, s);
-    case kShapeChunk2:
-      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 2>, s)
-                  : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 2>, s);
-    default:
-      return rest ? cudaLaunchKernelEx(&cfg, lgx_step_kernel<true, 1>, s)
-                  : cudaLaunchKernelEx(&cfg, lgx_step_kernel<false, 1>, s);
-  }
+  if (s.tiles.nblocks == 0u) return launch_shape<false>(cfg, s, shape, rest, in);
+  cfg.gridDim.x += s.tiles.nblocks;
+  return launch_shape<true>(cfg, s, shape, rest, in);
 }
 
 cudaError_t wave_grid(bool rest, uint32_t total, uint32_t* grid) {

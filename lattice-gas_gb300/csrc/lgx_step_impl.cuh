@@ -369,6 +369,98 @@ __device__ __forceinline__ void sample_finish(const SampleArgs& p, uint32_t blk,
   p.sol[blk] = __fdiv_rn(__int2float_rn(nsolid), n);
 }
 
+// Coarse-graining by tiles (SampleTiles): CTA `tile` takes `per` consecutive
+// blocks of one block row; its lanes take the words those blocks' columns cover
+// (one word per lane, so a warp's loads are coalesced) and its warps the block
+// row's rows (every blockDim.x / 32-th row).  A word meets at most three blocks
+// of kTileMinWidth or more columns; a thread sums, over its rows, its word's
+// masked popcounts for each block it meets and adds them into the CTA's
+// per-block totals in shared memory (acc), which a thread per block then
+// finishes.  The totals are the same exact integers as sample_block's, so the
+// field is the same; the warp per block there reads each word's 32-byte sector
+// once per block that meets it, with lanes a row apart.  BATCH rows' words are
+// loaded before any is counted, so their loads are in flight together.  The
+// caller has let its dependents launch; this waits for the previous grid
+// (griddepcontrol.wait) before it reads the state or the running averages.
+__device__ __forceinline__ uint32_t bit_range(uint32_t lo, uint32_t hi) {  // bits [lo, hi)
+  return hi - lo >= 32u ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << lo);
+}
+
+template <int BATCH>
+__device__ __forceinline__ void sample_tile(const SampleArgs& p, uint32_t tile, uint32_t per,
+                                            uint32_t ncx, int (*acc)[kTileMaxBlocks]) {
+  const uint32_t t = threadIdx.x, rows = blockDim.x >> 5;
+  for (uint32_t i = t; i < 4u * kTileMaxBlocks; i += blockDim.x) (&acc[0][0])[i] = 0;
+  const uint32_t jb = tile / ncx, ib0 = (tile - jb * ncx) * per;
+  const uint32_t nb = min(per, p.bw - ib0);
+  const uint32_t fb = jb * p.bw + ib0;  // field index of the tile's first block
+  __syncthreads();
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  float u0 = 0.0f, v0 = 0.0f, r0 = 0.0f;
+  if (t < nb) {
+    u0 = p.ux[fb + t];
+    v0 = p.uy[fb + t];
+    r0 = p.rho[fb + t];
+  }
+  const uint32_t x0 = ib0 * p.bx, x1 = x0 + nb * p.bx;  // the tile's columns
+  const uint32_t w0 = x0 >> 5, nw = ((x1 - 1u) >> 5) - w0 + 1u;
+  const size_t S = p.dm.total;
+  const size_t row0 = (size_t)jb * p.by;
+  for (uint32_t wo = t & 31u; wo < nw; wo += 32u) {
+    const uint32_t wi = w0 + wo;
+    const uint32_t lo = max(x0, wi << 5), hi = min(x1, (wi << 5) + 32u);
+    const uint32_t b0 = lo / p.bx;  // the first block the word meets
+    uint32_t m[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const uint32_t c0 = max(lo, (b0 + s) * p.bx), c1 = min(hi, (b0 + s + 1u) * p.bx);
+      m[s] = c1 > c0 ? bit_range(c0 - (wi << 5), c1 - (wi << 5)) : 0u;
+    }
+    int mass[3] = {0, 0, 0}, px[3] = {0, 0, 0}, py[3] = {0, 0, 0}, ns[3] = {0, 0, 0};
+    for (uint32_t rb = t >> 5; rb < p.by; rb += rows * BATCH) {
+      uint32_t sw[BATCH], pl[BATCH][7];
+#pragma unroll
+      for (int q = 0; q < BATCH; ++q) {  // a row past the block row loads nothing, counts 0
+        const uint32_t r = rb + q * rows;
+        const size_t at = (row0 + r) * p.dm.wpr + wi;
+        const bool in = r < p.by;
+        sw[q] = in ? __ldg(p.solid + at) : 0u;
+#pragma unroll
+        for (int d = 0; d < 7; ++d) pl[q][d] = in ? __ldg(p.a + d * S + at) : 0u;
+      }
+#pragma unroll
+      for (int q = 0; q < BATCH; ++q) {
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          if (!m[s]) continue;  // most words meet one or two blocks
+          const uint32_t sm = sw[q] & m[s];
+          const uint32_t fm = m[s] & ~sm;
+          ns[s] += __popc(sm);
+          const int c0 = __popc(pl[q][0] & fm), c1 = __popc(pl[q][1] & fm);
+          const int c2 = __popc(pl[q][2] & fm), c3 = __popc(pl[q][3] & fm);
+          const int c4 = __popc(pl[q][4] & fm), c5 = __popc(pl[q][5] & fm);
+          const int c6 = __popc(pl[q][6] & fm);
+          mass[s] += c0 + c1 + c2 + c3 + c4 + c5 + c6;
+          // CX2 = {2, 1, -1, -2, -1, 1}, CY2 = {0, 1, 1, 0, -1, -1}
+          px[s] += 2 * (c0 - c3) + c1 - c2 - c4 + c5;
+          py[s] += c1 + c2 - c4 - c5;
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      if (!m[s]) continue;
+      const uint32_t k = b0 + s - ib0;
+      atomicAdd(&acc[0][k], mass[s]);
+      atomicAdd(&acc[1][k], px[s]);
+      atomicAdd(&acc[2][k], py[s]);
+      atomicAdd(&acc[3][k], ns[s]);
+    }
+  }
+  __syncthreads();
+  if (t < nb) sample_finish(p, fb + t, acc[0][t], acc[1][t], acc[2][t], acc[3][t], u0, v0, r0);
+}
+
 // Coarse-graining of field block `blk` of one lattice by one whole warp
 // (lgca_sample, src/gpu.rs:324-377).  Lanes take rows of the block; each row
 // contributes the masked popcounts of the one to several words the block's

@@ -326,6 +326,7 @@ def test_small_lattices_bit_exact(LG, O, w, h, inlet, rest, mode):
 SHAPES = [1, 2, 3, 4]   # chunk of one / two per warp, two / four consecutive words per lane
 
 
+@pytest.mark.parametrize("block", [4, 20])  # a warp per field block; tiles, in the step's grid
 @pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("w,h,inlet,rest", [
     (128, 34, 40, True),    # four words per row: one four-word group per row
@@ -335,15 +336,17 @@ SHAPES = [1, 2, 3, 4]   # chunk of one / two per warp, two / four consecutive wo
     (1000, 40, 8, True),    # 32 words per row: a warp spans several rows
     (4000, 12, 40, False),  # 125 words per row: neither applies
 ])
-def test_step_shapes_bit_exact(LG, O, w, h, inlet, rest, shape):
+def test_step_shapes_bit_exact(LG, O, w, h, inlet, rest, shape, block):
     """Every kernel shape, pinned, against the oracle: obstacles, inflows,
-    ragged rows and both rules, across inlet chunks and sampling points."""
+    ragged rows and both rules, across inlet chunks and sampling points (with
+    20-column blocks a sampling point inside a run is coarse-grained by the next
+    step's grid; 4 x 4 blocks take the sampling kernel)."""
     cells = np.zeros(w * h, np.uint8)
     LG.add_circle(cells, w, h, w / 2.0, h * 0.43, min(w, h) / 5.0)
     LG.add_box(cells, w, h, w // 5, w // 5 + 2, 0, h // 3)
     LG.init_equilibrium(cells, 0.3, 0.2, 0.0, rest, 4321 + w)
     g, o = pair(LG, O, w, h, rest, 0xC0FFEE + w, cells,
-                inlet=(inlet, 0.3, (0.2, 0.0), rest) if inlet else None, block=4, mode=1)
+                inlet=(inlet, 0.3, (0.2, 0.0), rest) if inlet else None, block=block, mode=1)
     g.set_step_shape(shape)
     for chunk in (1, 7, 64, 130):
         g.advance_sampling(chunk, 10, 0.3)
