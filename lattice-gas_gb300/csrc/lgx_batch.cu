@@ -228,6 +228,37 @@ __global__ void __launch_bounds__(256) lgx_batch_sample_kernel(BatchSampleArgs p
   sample_block<true>(sa, task - p.blk0[lo]);
 }
 
+// The same for the lattices whose fields are coarse-grained by tiles: a CTA
+// per tile (sample_tile), its lattice found by binary search over the tile
+// prefix.
+__global__ void __launch_bounds__(256) lgx_batch_sample_tiles_kernel(BatchSampleArgs p) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  __shared__ int acc[4][kTileMaxBlocks];
+  const uint32_t lo = owner_of(p.tile0, p.nlat, blockIdx.x);
+  const LatDesc& d = p.descs[lo];
+  const uint64_t local = *p.base + p.k_after;
+  const uint32_t par = (d.cur0 + (uint32_t)local) & 1u;
+  SampleArgs sa;
+  sa.a = par ? d.planes[1] : d.planes[0];
+  sa.solid = d.solid;
+  sa.dm = d.dm;
+  sa.bx = d.bx;
+  sa.by = d.by;
+  sa.bw = d.bw;
+  sa.bh = d.bh;
+  sa.alpha = d.alpha;
+  const uint32_t nb = d.bw * d.bh;
+  sa.ux = d.field;
+  sa.uy = d.field + nb;
+  sa.rho = d.field + 2 * nb;
+  sa.sol = d.field + 3 * nb;
+  sa.sums = d.sums;
+  uint32_t per, ncx;
+  tile_shape(d.bx, d.bw, &per, &ncx);
+  sample_tile<4, false>(sa, blockIdx.x - p.tile0[lo], per, ncx, acc);
+}
+
 __global__ void lgx_batch_base_kernel(uint64_t* base, uint32_t n) { *base += n; }
 
 __global__ void lgx_batch_owner_kernel(const uint32_t* block0, uint32_t nlat, uint32_t nblocks,
@@ -301,9 +332,7 @@ cudaError_t launch_batch_inlet(const BatchInletArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st) {
-  if (a.total_blocks == 0) return cudaSuccess;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((a.total_blocks + 7) / 8);
   cfg.blockDim = dim3(256);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -311,7 +340,16 @@ cudaError_t launch_batch_sample(const BatchSampleArgs& a, cudaStream_t st) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, lgx_batch_sample_kernel, a);
+  cudaError_t e = cudaSuccess;
+  if (a.total_blocks) {
+    cfg.gridDim = dim3((a.total_blocks + 7) / 8);
+    e = cudaLaunchKernelEx(&cfg, lgx_batch_sample_kernel, a);
+  }
+  if (e == cudaSuccess && a.total_tiles) {
+    cfg.gridDim = dim3(a.total_tiles);
+    e = cudaLaunchKernelEx(&cfg, lgx_batch_sample_tiles_kernel, a);
+  }
+  return e;
 }
 
 cudaError_t launch_batch_owner(const uint32_t* block0, uint32_t nlat, uint32_t nblocks,

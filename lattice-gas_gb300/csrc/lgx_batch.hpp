@@ -50,6 +50,11 @@ struct BatchSampleArgs {
   uint32_t total_blocks;
   const uint64_t* base;
   uint32_t k_after;      // sample the state after batch step *base + k_after
+  // lattices coarse-grained by tiles (blocks >= kTileMinWidth columns): the
+  // prefix of their tile counts (tile_shape), nlat + 1 entries; their blocks
+  // are not in blk0.  Null / 0: none.
+  const uint32_t* tile0 = nullptr;
+  uint32_t total_tiles = 0;
 };
 
 // Sampling schedule of a lattice within one resident launch: it is

@@ -79,12 +79,14 @@ struct lgx_batch {
   lgx::LatDesc* d_descs = nullptr;
   uint32_t* d_item0 = nullptr;
   uint32_t* d_blk0 = nullptr;
+  uint32_t* d_tile0 = nullptr;
   uint64_t* d_base = nullptr;
   uint32_t nblocks = 0;
   uint32_t rest_blocks = 0;     // leading per-step blocks, those of rest-particle lattices
   uint32_t items_per_step = 0;  // inlet draw items of one step, all lattices
   uint64_t item0_len = 1;       // the interval length d_item0 holds the prefix for
-  uint32_t field_blocks = 0;
+  uint32_t field_blocks = 0;  // blocks coarse-grained a warp each
+  uint32_t field_tiles = 0;   // tiles of the lattices coarse-grained by tiles
   std::vector<uint32_t*> inlet_bufs;
   std::vector<GraphEntry> graphs;
   uint64_t launches = 0;
@@ -170,6 +172,7 @@ void free_batch(lgx_batch* b) {
   cudaFree(b->d_descs);
   cudaFree(b->d_item0);
   cudaFree(b->d_blk0);
+  cudaFree(b->d_tile0);
   cudaFree(b->d_base);
   for (auto& ev : b->ev)
     if (ev) cudaEventDestroy(ev);
@@ -270,8 +273,9 @@ int capture(lgx_batch* b, uint32_t len, bool sample, cudaGraphExec_t* out,
       if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, sg.done, 0);
     }
   }
-  if (e == cudaSuccess && sample && b->field_blocks) {
-    lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, b->nstep, b->field_blocks, b->d_base, len};
+  if (e == cudaSuccess && sample && (b->field_blocks || b->field_tiles)) {
+    lgx::BatchSampleArgs sp{b->d_descs, b->d_blk0, b->nstep,  b->field_blocks,
+                            b->d_base,  len,       b->d_tile0, b->field_tiles};
     e = lgx::launch_batch_sample(sp, b->stream);
   }
   if (e == cudaSuccess && res_branch) {
@@ -497,21 +501,31 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
   for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev[i]);
   // block table of the per-step lattices: each padded to whole 256-word blocks
-  std::vector<uint32_t> block0(n + 1, 0), item0(n + 1, 0), blk0(n + 1, 0);
+  // and the coarse-graining tables: a warp per block for fields of narrow
+  // blocks, tiles (tile_shape) for the others
+  std::vector<uint32_t> block0(n + 1, 0), item0(n + 1, 0), blk0(n + 1, 0), tile0(n + 1, 0);
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
-    const lgx::Dims& dm = lats[i]->dm;
+    const lgx_lattice* l = lats[i];
+    const lgx::Dims& dm = l->dm;
     const bool step = i < b->nstep;
     block0[i + 1] = block0[i] + (step ? (dm.total + 255) / 256 : 0);
-    if (step && lats[i]->rest) b->rest_blocks = block0[i + 1];
+    if (step && l->rest) b->rest_blocks = block0[i + 1];
     item0[i + 1] = item0[i] + dm.h * dm.iw;
-    blk0[i + 1] = blk0[i] + (step && lats[i]->has_field ? lats[i]->bw * lats[i]->bh : 0);
+    const bool field = step && l->has_field && l->bw * l->bh > 0;
+    const bool tiled = field && l->bx >= lgx::kTileMinWidth;
+    uint32_t per = 0, ncx = 0;
+    if (tiled) lgx::tile_shape(l->bx, l->bw, &per, &ncx);
+    blk0[i + 1] = blk0[i] + (field && !tiled ? l->bw * l->bh : 0);
+    tile0[i + 1] = tile0[i] + (tiled ? ncx * l->bh : 0);
   }
   b->nblocks = block0[n];
   b->items_per_step = item0[n];
   b->field_blocks = blk0[n];
+  b->field_tiles = tile0[n];
   if (e == cudaSuccess) e = cudaMalloc(&b->d_descs, n * sizeof(lgx::LatDesc));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_item0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_blk0, (n + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_tile0, (n + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_base, sizeof(uint64_t));
   uint32_t chains = 2;
   if (const char* v = getenv("LGX_BATCH_CHAINS")) chains = (uint32_t)std::max(1, atoi(v));
@@ -528,6 +542,7 @@ int lgx::batch_create(lgx_lattice* const* lats, size_t n, int policy, cudaStream
   }
   if (e == cudaSuccess) e = cudaMemcpy(b->d_item0, item0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_blk0, blk0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_tile0, tile0.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     const int rc = (e == cudaErrorMemoryAllocation) ? LGX_ERR_ALLOC : LGX_ERR_CUDA;
     lgx::set_error(std::string("lgx_batch_create: ") + cudaGetErrorString(e));
@@ -590,7 +605,8 @@ int lgx_batch_advance_sampling(lgx_batch* b, uint64_t n, uint64_t every, float a
     const uint64_t per_step = b->groups.size();
     b->launches += len * (per_step + (b->hook && b->hook_per_step ? 1 : 0)) + 1 +
                    (b->hook && !b->hook_per_step && sample ? 1 : 0) +
-                   (sample && b->field_blocks ? 1 : 0) + (b->items_per_step ? 1 : 0) +
+                   (sample && b->field_blocks ? 1 : 0) + (sample && b->field_tiles ? 1 : 0) +
+                   (b->items_per_step ? 1 : 0) +
                    b->classes.size();
     left -= len;
     since += len;

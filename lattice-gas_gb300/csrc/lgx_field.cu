@@ -665,14 +665,8 @@ cudaError_t launch_moments(const uint32_t* a, const Dims& dm, unsigned long long
 
 bool sample_tiling(const SampleArgs& s, SampleTiles* t) {
   if (s.bx < kTileMinWidth || s.bw * s.bh == 0) return false;
-  // as many blocks per CTA as keep their words within one warp's lanes (a
-  // block-aligned start can sit 31 columns into its first word), spread evenly
-  // over the block row
-  uint32_t most = (1024u - 31u) / s.bx;
-  most = most < 1u ? 1u : (most > kTileMaxBlocks ? kTileMaxBlocks : most);
   t->s = s;
-  t->ncx = (s.bw + most - 1u) / most;
-  t->per = (s.bw + t->ncx - 1u) / t->ncx;
+  tile_shape(s.bx, s.bw, &t->per, &t->ncx);
   t->nblocks = t->ncx * s.bh;
   return true;
 }

@@ -54,6 +54,16 @@ struct SampleTiles {
 };
 // The tiling of a field, or false when its blocks are too narrow for tiles.
 bool sample_tiling(const SampleArgs& s, SampleTiles* t);
+// A block row of bw blocks of bx columns in tiles: as many blocks per tile as
+// keep their words within one warp's lanes (a block-aligned start can sit 31
+// columns into its first word), spread evenly; bx >= kTileMinWidth.
+__host__ __device__ inline void tile_shape(uint32_t bx, uint32_t bw, uint32_t* per,
+                                           uint32_t* ncx) {
+  uint32_t most = (1024u - 31u) / bx;
+  most = most < 1u ? 1u : (most > kTileMaxBlocks ? kTileMaxBlocks : most);
+  *ncx = (bw + most - 1u) / most;
+  *per = (bw + *ncx - 1u) / *ncx;
+}
 
 struct StepArgs {
   const uint32_t* a;

@@ -381,12 +381,13 @@ __device__ __forceinline__ void sample_finish(const SampleArgs& p, uint32_t blk,
 // once per block that meets it, with lanes a row apart.  BATCH rows' words are
 // loaded before any is counted, so their loads are in flight together.  The
 // caller has let its dependents launch; this waits for the previous grid
-// (griddepcontrol.wait) before it reads the state or the running averages.
+// (griddepcontrol.wait) before it reads the state or the running averages
+// (WAIT false: the caller has waited already).
 __device__ __forceinline__ uint32_t bit_range(uint32_t lo, uint32_t hi) {  // bits [lo, hi)
   return hi - lo >= 32u ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << lo);
 }
 
-template <int BATCH>
+template <int BATCH, bool WAIT = true>
 __device__ __forceinline__ void sample_tile(const SampleArgs& p, uint32_t tile, uint32_t per,
                                             uint32_t ncx, int (*acc)[kTileMaxBlocks]) {
   const uint32_t t = threadIdx.x, rows = blockDim.x >> 5;
@@ -395,7 +396,7 @@ __device__ __forceinline__ void sample_tile(const SampleArgs& p, uint32_t tile, 
   const uint32_t nb = min(per, p.bw - ib0);
   const uint32_t fb = jb * p.bw + ib0;  // field index of the tile's first block
   __syncthreads();
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (WAIT) asm volatile("griddepcontrol.wait;" ::: "memory");
   float u0 = 0.0f, v0 = 0.0f, r0 = 0.0f;
   if (t < nb) {
     u0 = p.ux[fb + t];
