@@ -314,14 +314,16 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     }
     cfirst[nch] = n;
   }
-  // slot layout: descs[n] | item0[n+1] | per chain c: block0[nc+1] | blk[m][nc+1]
+  // slot layout: descs[n] | item0[n+1] | per chain c: block0[nc+1] | blk[m][nc+1] |
+  // tl[m][nc+1] (per sampling point, the prefixes of field blocks coarse-grained a
+  // warp each and of tiles, for the lattices that sample there)
   lgx::LatDesc* descs = (lgx::LatDesc*)slot.host;
   uint32_t* item0 = (uint32_t*)(descs + n);
   std::vector<size_t> off(nch);  // each chain's block0, in words from item0
   size_t words = n + 1;
   for (size_t c = 0; c < nch; ++c) {
     off[c] = words;
-    words += (1 + m) * (cfirst[c + 1] - cfirst[c] + 1);
+    words += (1 + 2 * m) * (cfirst[c + 1] - cfirst[c] + 1);
   }
   const size_t bytes = n * sizeof(lgx::LatDesc) + words * sizeof(uint32_t);
   item0[0] = 0;
@@ -332,8 +334,9 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
     const size_t nc = cfirst[c + 1] - cfirst[c];
     uint32_t* block0 = item0 + off[c];
     uint32_t* blk = block0 + nc + 1;
+    uint32_t* tl = blk + m * (nc + 1);
     block0[0] = 0;
-    for (size_t j = 0; j < m; ++j) blk[j * (nc + 1)] = 0;
+    for (size_t j = 0; j < m; ++j) blk[j * (nc + 1)] = tl[j * (nc + 1)] = 0;
     for (size_t q = 0; q < nc; ++q) {
       const size_t i = cfirst[c] + q;
       Req* r = s->active[i];
@@ -361,10 +364,19 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
       if (r->dm.wpr % 4u) wpr4[c] = 0;
       if (r->dm.iw) inflow[c] = 1;
       item0[i + 1] = item0[i] + (uint32_t)len * r->dm.h * r->dm.iw;
-      for (size_t j = 0; j < m; ++j) blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q];
+      for (size_t j = 0; j < m; ++j) {
+        blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q];
+        tl[j * (nc + 1) + q + 1] = tl[j * (nc + 1) + q];
+      }
+      const bool tiled = d.bx >= lgx::kTileMinWidth && r->bw * r->bh > 0;
+      uint32_t per = 0, ncx = 0;
+      if (tiled) lgx::tile_shape(d.bx, d.bw, &per, &ncx);
       due_points(r, len, [&](uint64_t k) {
         const size_t j = std::lower_bound(pts.begin(), pts.end(), (uint32_t)k) - pts.begin();
-        blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q] + r->bw * r->bh;
+        if (tiled)
+          tl[j * (nc + 1) + q + 1] = tl[j * (nc + 1) + q] + ncx * r->bh;
+        else
+          blk[j * (nc + 1) + q + 1] = blk[j * (nc + 1) + q] + r->bw * r->bh;
       });
     }
     nblocks[c] = block0[nc];
@@ -417,11 +429,13 @@ cudaError_t tick(lgx_server* s, uint64_t len) {
       s->launches += 1;
       if (e == cudaSuccess && j < m && pts[j] == k + 1) {
         const uint32_t* tb = blk + j * (nc + 1);
-        if (tb[nc]) {
-          lgx::BatchSampleArgs sp{dd, d_block0 + nc + 1 + j * (nc + 1), (uint32_t)nc, tb[nc],
-                                  s->d_zero, k + 1};
+        const uint32_t* tt = tb + m * (nc + 1);
+        if (tb[nc] || tt[nc]) {
+          const uint32_t* d_tb = d_block0 + nc + 1 + j * (nc + 1);
+          lgx::BatchSampleArgs sp{dd, d_tb, (uint32_t)nc, tb[nc], s->d_zero,
+                                  k + 1, d_tb + m * (nc + 1), tt[nc]};
           e = lgx::launch_batch_sample(sp, st);
-          s->launches += 1;
+          s->launches += (tb[nc] ? 1 : 0) + (tt[nc] ? 1 : 0);
         }
         ++j;
       }
@@ -616,7 +630,7 @@ int lgx_server_create(size_t budget_bytes, size_t max_active, lgx_server** out) 
     e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   s->slot_bytes = max_active * sizeof(lgx::LatDesc) +
-                  ((max_active + 1) + (1 + kMaxSamplePoints) * (max_active + kChains)) *
+                  ((max_active + 1) + (1 + 2 * kMaxSamplePoints) * (max_active + kChains)) *
                       sizeof(uint32_t);
   for (int i = 0; i < kRing && e == cudaSuccess; ++i) {
     e = cudaHostAlloc(&s->ring[i].host, s->slot_bytes, cudaHostAllocDefault);
