@@ -48,19 +48,20 @@ def peaks():
 
 # Figures from ncu captures of the wake run's step kernel in the shape the tuner
 # picks there, four words per lane (lgx_step_lanes_kernel; one launch = one
-# step): DRAM bytes read + written per launch (cold cache under ncu; the 18 MB of
-# planes stay in L2 between steps of a timed run) and the ALU-pipe warp
-# instructions per launch, which do not depend on timing; and, for the roofline
-# case, DRAM bytes per site-update from a 16384 x 8192 capture of the same kernel
-# (the full 32768 x 16384 case scales with its sites).  They hold for the kernel
-# sources they were captured from: STEP_SOURCES hashed to CAPTURED_SOURCES_SHA.
-# When the sources differ the line says "stale": true.
-STEP_TRAFFIC_BYTES = 9312768 + 256
+# step): DRAM bytes read + written per launch (cold cache under ncu, the mean of
+# three launches; the 18 MB of planes stay in L2 between steps of a timed run) and
+# the ALU-pipe warp instructions per launch, which do not depend on timing; and,
+# for the roofline case, DRAM bytes per site-update from a 16384 x 8192 capture of
+# the same kernel (the mean of two launches; the full 32768 x 16384 case scales
+# with its sites).  They hold for the kernel sources they were captured from:
+# STEP_SOURCES hashed to CAPTURED_SOURCES_SHA.  When the sources differ the line
+# says "stale": true.
+STEP_TRAFFIC_BYTES = (9318656 + 8651520 + 8638720) // 3
 STEP_ALU_WARP_INSTR = 3024084
-BIG_DRAM_BYTES_PER_SITE = (125285120 + 73829120) / (16384 * 8192)
+BIG_DRAM_BYTES_PER_SITE = (125201280 + 73544320) / (16384 * 8192)
 STEP_SOURCES = ("lgx_step.cu", "lgx_step_impl.cuh", "lgx_device.cuh",
                 os.path.join("generated", "collide.cuh"))
-CAPTURED_SOURCES_SHA = "7ffe273af946e9c2"
+CAPTURED_SOURCES_SHA = "621d9e53930f3c25"
 
 
 def step_sources_sha() -> str:
