@@ -63,21 +63,24 @@ constexpr int kWaveThreads = 256;  // the persistent kernel's blocks
 // step N's last blocks leave idle.  Without a programmatic predecessor the
 // wait returns at once, so the kernel is also correct launched plainly.
 //
-// SAMPLE: the grid leads with p.tiles.nblocks coarse-graining tiles of the
+// SAMPLE: the grid ends with p.tiles.nblocks coarse-graining tiles of the
 // state the step reads (sample_tile), which run beside the step's blocks; the
-// step writes the other plane set, and the next grid waits for both.
+// step writes the other plane set, and the next grid waits for both.  Last, so
+// that a step that fills the GPU in one wave starts whole and the tiles take
+// the slots its blocks leave (wake run: 3.8-3.9 us per sample against 4.3-4.7
+// with the tiles first).
 template <bool REST, int WORDS, bool SAMPLE = false>
 __global__ void __launch_bounds__(256 / WORDS, WORDS == 1 ? LGX_STEP_MINB1 : LGX_STEP_MINB)
     lgx_step_kernel(const StepArgs p) {
-  uint32_t bid = blockIdx.x;
+  const uint32_t bid = blockIdx.x;
   if (SAMPLE) {
-    if (bid < p.tiles.nblocks) {
+    const uint32_t nstep = gridDim.x - p.tiles.nblocks;
+    if (bid >= nstep) {
       asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
       __shared__ int acc[4][kTileMaxBlocks];
-      sample_tile<WORDS == 1 ? 2 : 4>(p.tiles.s, bid, p.tiles.per, p.tiles.ncx, acc);
+      sample_tile<WORDS == 1 ? 2 : 4>(p.tiles.s, bid - nstep, p.tiles.per, p.tiles.ncx, acc);
       return;
     }
-    bid -= p.tiles.nblocks;
   }
   // a warp takes WORDS consecutive 32-word chunks; a block covers 256 words
   constexpr int kStepWords = WORDS;
@@ -114,19 +117,19 @@ __global__ void __launch_bounds__(256 / WORDS, WORDS == 1 ? LGX_STEP_MINB1 : LGX
 // FMA pipe: 6.03 / 297.0.  Two words per lane are allowed six blocks per SM (80
 // registers), five with the inflow compiled in: at six it spilled 24 bytes, and a
 // 2048 x 1280 step with an 8-column inflow took 4.55 us against 3.89.
-// SAMPLE: coarse-graining tiles lead the grid, as in lgx_step_kernel.
+// SAMPLE: coarse-graining tiles end the grid, as in lgx_step_kernel.
 template <bool REST, int V, bool INFLOW, bool SAMPLE = false>
 __global__ void __launch_bounds__(128, V == 4 ? 4 : (INFLOW ? 5 : 6))
     lgx_step_lanes_kernel(const StepArgs p) {
-  uint32_t bid = blockIdx.x;
+  const uint32_t bid = blockIdx.x;
   if (SAMPLE) {
-    if (bid < p.tiles.nblocks) {
+    const uint32_t nstep = gridDim.x - p.tiles.nblocks;
+    if (bid >= nstep) {
       asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
       __shared__ int acc[4][kTileMaxBlocks];
-      sample_tile<4>(p.tiles.s, bid, p.tiles.per, p.tiles.ncx, acc);
+      sample_tile<4>(p.tiles.s, bid - nstep, p.tiles.per, p.tiles.ncx, acc);
       return;
     }
-    bid -= p.tiles.nblocks;
   }
   constexpr int E = V;  // draws made before the wait
   const uint32_t warp = bid * 4u + (threadIdx.x >> 5);
