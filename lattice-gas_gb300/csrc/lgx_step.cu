@@ -258,20 +258,31 @@ __global__ void __launch_bounds__(kWaveThreads) lgx_wave_kernel(const WaveArgs p
 
 // One thread per (step, row, inlet word): the inflow's Bernoulli words for
 // that step, the hash chain seeded by word ^ seed32 ^ 0x9e3779b9 and carried
-// across the seven planes (src/gpu.rs:300-305).
+// across the seven planes (src/gpu.rs:300-305).  Launched with programmatic
+// stream serialisation: the words depend only on (word, step), so a thread
+// makes all seven while the step before it drains, and waits for that step's
+// grid (griddepcontrol.wait) only to write them into the buffer the steps of
+// the previous chunk read.  The next step waits for this grid in turn.
 __global__ void __launch_bounds__(128) lgx_inlet_kernel(const InletArgs p) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const uint32_t per_step = p.dm.h * p.dm.iw;
   const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= per_step * p.nsteps) return;
-  const uint32_t s = idx / per_step;
-  const uint32_t rem = idx - s * per_step;
+  const bool live = idx < per_step * p.nsteps;
+  const uint32_t i = live ? idx : 0u;
+  const uint32_t s = i / per_step;
+  const uint32_t rem = i - s * per_step;
   const uint32_t y = rem / p.dm.iw;
   const uint32_t jw = rem - y * p.dm.iw;
   const uint32_t word = y * p.dm.wpr + jw;
   uint32_t r = mix(word ^ step_seed32(p.seed, p.steps + s) ^ kGolden32);
+  uint32_t v[7];
+#pragma unroll
+  for (int d = 0; d < 7; ++d) v[d] = bernoulli(p.thresh[d], r);
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (!live) return;
   uint32_t* out = p.out + (size_t)idx * 7u;
-#pragma unroll 1
-  for (int d = 0; d < 7; ++d) out[d] = bernoulli(p.thresh[d], r);
+#pragma unroll
+  for (int d = 0; d < 7; ++d) out[d] = v[d];
 }
 
 }  // namespace
@@ -373,8 +384,16 @@ cudaError_t launch_wave(const WaveArgs& w, bool rest, uint32_t grid, cudaStream_
 cudaError_t launch_inlet(const InletArgs& s, cudaStream_t st) {
   const uint32_t n = s.dm.h * s.dm.iw * s.nsteps;
   if (n == 0) return cudaSuccess;
-  lgx_inlet_kernel<<<(n + 127) / 128, 128, 0, st>>>(s);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((n + 127) / 128);
+  cfg.blockDim = dim3(128);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, lgx_inlet_kernel, s);
 }
 
 }  // namespace lgx
