@@ -194,6 +194,23 @@ def test_the_coarse_graining_tiles_match_the_oracle(LG, O, w, h, bx, by):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("block,separate", [(20, 1), (8, 10)])
+def test_sampling_points_ride_in_the_next_steps_grid(LG, O, block, separate):
+    """With one launch per step, a sampling point that another step of the run
+    follows is coarse-grained inside that step's grid (20-column blocks: only the
+    run's last point launches on its own); 8-column blocks take a sampling launch
+    at every point.  The field matches the oracle either way."""
+    w, h = 256, 64
+    cells = np.zeros(w * h, np.uint8)
+    LG.init_equilibrium(cells, 0.3, 0.2, 0.0, True, 7)
+    g, o = pair(LG, O, w, h, True, 9, cells, block=block, mode=1)
+    n0 = g.launches
+    g.advance_sampling(50, 5, 0.3)
+    o.advance_sampling(50, 5, 0.3)
+    assert g.launches - n0 == 50 + separate
+    assert_same(g, o)
+
+
 def test_the_gpu_field_averages_over_time(LG, O):
     """src/gpu.rs:999-1032, bit-exact."""
     ALPHA = 0.2
